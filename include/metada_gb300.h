@@ -1,0 +1,200 @@
+/*
+ * metada_gb300 — GB300-native (sm_103a) ensemble Kalman analysis for METADA.
+ *
+ * C-ABI of the CUDA library libmetada_gb300.so.  This is the boundary the
+ * C++ host layer (include/metada_gb300/*.hpp, mirroring METADA's backend
+ * traits and algorithm policies) and any other FFI caller bind.  Each entry
+ * point names the reference member function (open-x-da/metada tree,
+ * file:line) whose work it replaces.
+ *
+ * Conventions
+ *  - Every function returns an int status: MG_OK (0) or an MG_ERR_* code;
+ *    no C++ exception and no CUDA error crosses this boundary.  The message
+ *    for the last failure on a context is mg_last_error(ctx).
+ *  - Array arguments are DEVICE pointers owned by the caller unless a
+ *    comment says "host".  Work is enqueued on the context's stream
+ *    (mg_set_stream); entry points that return a host-visible count
+ *    synchronise that stream.
+ *  - Ensembles are member-major as in the reference (k separate state
+ *    vectors, SimpleState.hpp:265): member i starts at X + i*ld.
+ *  - Obs-space ensembles are p x k row-major: HX[o*k + i] = H(member i)_o.
+ *  - A context is not re-entrant; use one per host thread.
+ */
+#ifndef METADA_GB300_H
+#define METADA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define MG_OK 0
+#define MG_ERR_ARG 1      /* invalid argument (sizes, null pointers, flags) */
+#define MG_ERR_CUDA 2     /* a CUDA runtime call failed */
+#define MG_ERR_NOMEM 3    /* device workspace could not be allocated */
+#define MG_ERR_NUMERIC 4  /* k x k matrix not positive definite / not finite */
+#define MG_ERR_TIMEOUT 5  /* a bounded device-side wait gave up */
+#define MG_ERR_CAPACITY 6 /* caller's output buffer too small; *total says how large */
+
+/* Analysis semantics (bit flags).  MG_COMPAT reproduces the reference:
+ * LETKF.hpp:214 (R_local = I), :219 (Pa *= rho), :223-224 (Cholesky square
+ * root), :232-238 (per-member scalar update).  Without them the Hunt et al.
+ * (2007) LETKF is used: R^-1 = w/sigma^2 with Gaspari-Cohn weights w,
+ * Pa = [(k-1)/rho I + Y'^T R^-1 Y']^-1, symmetric square root from a Jacobi
+ * eigen-decomposition, Xa = xm + X'(wa 1^T + W). */
+#define MG_R_IDENTITY 1
+#define MG_SQRT_CHOLESKY 2
+#define MG_INFL_COMPAT 4
+#define MG_UPDATE_COMPAT 8
+#define MG_COMPAT 15
+#define MG_RTPS 16 /* relaxation to prior spread with alpha = rho (no multiplicative inflation) */
+
+/* Arithmetic of the analysis. */
+#define MG_PREC_FP64 0  /* every step in IEEE double */
+#define MG_PREC_MIXED 1 /* FP64 means/innovations; FP32 anomalies, Gram, eigen-solve, update */
+
+typedef struct mg_context mg_context;
+
+/* Context: device, stream, device workspace, last error.
+ * Replaces nothing in the reference (its analysis is host code); it owns the
+ * GPU resources the algorithm policies need. */
+int mg_create(mg_context** ctx, int device);
+void mg_destroy(mg_context* ctx);
+int mg_set_stream(mg_context* ctx, void* cuda_stream);
+int mg_synchronize(mg_context* ctx);
+const char* mg_last_error(const mg_context* ctx);
+/* Library version string (static). */
+const char* mg_version(void);
+
+/* Ensemble::RecomputeMean, src/framework/adapters/Ensemble.hpp:105-114:
+ * mean = (sum over members in member order) * (1.0/k).  Bit-exact. */
+int mg_ens_mean(mg_context* ctx, const double* X, int64_t n, int32_t k, int64_t ld,
+                double* mean);
+
+/* Ensemble::RecomputePerturbations, Ensemble.hpp:142-151: mean as above and
+ * Xp_i = X_i - mean (member-major, member i at Xp + i*ldp).  Bit-exact. */
+int mg_ens_mean_pert(mg_context* ctx, const double* X, int64_t n, int32_t k, int64_t ld,
+                     double* mean, double* Xp, int64_t ldp);
+
+/* IdentityObsOperator::apply, src/backends/common/obsoperator/
+ * IdentityObsOperator.hpp:154-180 with find4NearestGridPoints (:594-617)
+ * and idw4Interpolation (:643-676), for grid observations on the 2-D
+ * SimpleState (row-major y*nx + x).  obs_xy: p (x, y) int32 pairs; valid:
+ * p bytes or NULL (invalid obs give 0, :165-167).  Bit-exact. */
+int mg_hx_idw4(mg_context* ctx, const double* X, int32_t k, int64_t ld, int32_t nx,
+               int32_t ny, const int32_t* obs_xy, const uint8_t* valid, int64_t p,
+               double* HX);
+
+/* Bilinear-horizontal / linear-vertical H on a cell-centred lat-lon grid
+ * (lon_i = i+0.5 deg, lat_j = -89.5+j deg, integer levels), state layout
+ * ((v*nlev + l)*nlat + j)*nlon + i.  No reference counterpart (the reference
+ * has only IDW4); used for the lat-lon configurations.  Bit-exact with the
+ * oracle's fixed operation order. */
+int mg_hx_latlon(mg_context* ctx, const double* X, int32_t k, int64_t ld, int32_t nlon,
+                 int32_t nlat, int32_t nlev, const double* obs_lat, const double* obs_lon,
+                 const double* obs_lev, const int32_t* obs_var, int64_t p, double* HX);
+
+/* LETKF::updateGridPoint local search, src/framework/algorithms/
+ * LETKF.hpp:159-165 with Location::distance_to GRID branch
+ * (src/framework/base/Location.hpp:205-211): for each grid point of an
+ * nx*ny SimpleGeometry (row-major), the obs with distance <= radius, in obs
+ * order.  Writes offsets[nx*ny+1] (device) and idx[] (device, capacity cap);
+ * *total (host) receives the entry count.  Bit-exact. */
+int mg_select_grid(mg_context* ctx, int32_t nx, int32_t ny, const int32_t* obs_xy,
+                   int64_t p, double radius, int64_t* offsets, int32_t* idx, int64_t cap,
+                   int64_t* total);
+
+/* The same search with the GEOGRAPHIC branch (haversine km,
+ * Location.hpp:212-216, :349-357) over a device-built lat-lon spatial hash,
+ * for ncol query columns.  Lists are in obs order; dist_km (device, may be
+ * NULL) receives each entry's distance.  Pairs whose GPU distance lies within
+ * 1e-9 relative of the radius are re-decided on the host with the reference
+ * expression, so counts and lists are bit-exact. */
+int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
+                  int64_t ncol, const double* obs_lat, const double* obs_lon, int64_t p,
+                  double radius_km, int64_t* offsets, int32_t* idx, double* dist_km,
+                  int64_t cap, int64_t* total);
+
+/* ETKF::Analyse, src/framework/algorithms/ETKF.hpp:100-179, in place on the
+ * members X.  HX: obs-space ensemble of the raw background members
+ * (ETKF.hpp:128-132); yo, rvar: obs values and error variances (+inf for
+ * invalid obs).  flags: MG_COMPAT (X' *= rho, Cholesky W, ETKF.hpp:125,158)
+ * or 0 (Hunt: symmetric W, (k-1)/rho prior).  mean_out (device, may be
+ * NULL) receives the background mean the reference leaves in
+ * Ensemble::Mean().  precision: MG_PREC_*. */
+int mg_etkf(mg_context* ctx, double* X, int64_t n, int32_t k, int64_t ld, const double* HX,
+            const double* yo, const double* rvar, int64_t p, double rho, int32_t flags,
+            int32_t precision, double* mean_out);
+
+/* LETKF::Analyse exactly as the reference runs it, LETKF.hpp:63-119 and
+ * :152-243, on a 2-D SimpleState grid: grid points in row-major order, each
+ * analysed with the obs-space prior of the CURRENT, partly analysed members
+ * (IDW4 H), R_local = I, Pa *= rho, Cholesky W, the per-member scalar update,
+ * written in place; then Ensemble::RecomputeMean into mean_out (may be
+ * NULL).  Sequential by construction; for parity on small grids. */
+int mg_letkf_compat_grid(mg_context* ctx, double* X, int32_t k, int64_t ld, int32_t nx,
+                         int32_t ny, const int32_t* obs_xy, const uint8_t* valid,
+                         const double* yo, int64_t p, double radius, double rho,
+                         double* mean_out);
+
+/* Batched LETKF over columns x levels with the obs-space prior of the
+ * background (all local analyses independent). */
+typedef struct mg_letkf_desc {
+  double* X;             /* members, member-major, updated in place */
+  int64_t n;             /* state values per member */
+  int64_t ld;            /* member stride (>= n) */
+  int32_t k;             /* members, 2..128 */
+  int32_t n_var;         /* variables sharing one analysis point */
+  int32_t nlev;          /* levels per column */
+  int32_t precision;     /* MG_PREC_* */
+  int64_t ncol;          /* horizontal columns */
+  const int64_t* col_base; /* device, ncol: state index of (col, lev 0, var 0) */
+  int64_t lev_stride;    /* state index step between levels */
+  int64_t var_stride;    /* state index step between variables */
+  int64_t p;             /* observations */
+  const double* HX;      /* device p x k: H(raw background members) */
+  const double* yo;      /* device p */
+  const double* rvar;    /* device p: error variance */
+  const double* obs_lev; /* device p or NULL: vertical coordinate (level units) */
+  const int64_t* loc_off;  /* device ncol+1: per-column candidate lists */
+  const int32_t* loc_idx;  /* device: obs index */
+  const double* loc_dist;  /* device or NULL: horizontal distance of each entry */
+  double hsupport;       /* horizontal Gaspari-Cohn support (weight 0 beyond) */
+  double vsupport;       /* vertical support in levels (obs with |dl| > vsupport dropped) */
+  double rho;            /* inflation (MG_RTPS: relaxation alpha) */
+  int32_t flags;         /* MG_* semantics bits */
+  int32_t reserved;
+  double* mean_out;      /* device n or NULL: analysis ensemble mean */
+} mg_letkf_desc;
+
+/* Batched local analyses: replaces the serial grid-point loop of
+ * LETKF::Analyse (LETKF.hpp:101) and updateGridPoint (:152-243) with one
+ * local analysis per (column, level), all sharing the background obs-space
+ * prior.  With MG_COMPAT flags each analysis follows updateGridPoint's
+ * arithmetic; without them, the Hunt et al. (2007) LETKF with Gaspari-Cohn
+ * R-localisation.  Points are scheduled longest-list first. */
+int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* desc);
+
+/* Statistics of the last mg_letkf_batched call (host). */
+typedef struct mg_letkf_stats {
+  int64_t n_points;      /* local analyses run */
+  int64_t n_empty;       /* analyses with no local obs */
+  int64_t total_local;   /* sum of local obs counts */
+  int32_t max_local;     /* largest local obs count */
+  int32_t max_sweeps;    /* Jacobi sweeps of the slowest analysis */
+  double ms_prepare;     /* device time: perturbations, obs prior, ordering */
+  double ms_analysis;    /* device time of the local-analysis kernel */
+  double ms_writeback;   /* device time: write-back to members and mean */
+} mg_letkf_stats;
+int mg_letkf_last_stats(const mg_context* ctx, mg_letkf_stats* stats);
+
+/* Number of kernels this context has launched since creation (host). */
+int64_t mg_kernel_launches(const mg_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* METADA_GB300_H */

@@ -1,0 +1,240 @@
+// CTA-wide dense k x k routines on shared-memory matrices (row-major,
+// leading dimension lda).  Every thread of the block must call them; they
+// synchronise internally and return block-uniform results.
+//
+// These replace the Eigen calls of ETKF.hpp:150-159 and LETKF.hpp:215-224:
+//   inverse()        -> Cholesky factor + triangular inverse (A is SPD)
+//   llt().matrixL()  -> cta_cholesky
+// and, for the symmetric square root of the Hunt et al. (2007) transform,
+// a parallel two-sided Jacobi eigen-solver: round-robin (circle method)
+// ordering, k/2 disjoint rotations per round, rows then columns, with the
+// rotated 2 x 2 block written in closed form.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mg {
+
+template <typename T>
+__device__ __forceinline__ T dsqrt(T x);
+template <>
+__device__ __forceinline__ double dsqrt<double>(double x) { return sqrt(x); }
+template <>
+__device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+
+// In-place lower Cholesky factor (upper triangle zeroed).  Returns false if
+// a pivot is not positive and finite.
+template <typename T>
+__device__ bool cta_cholesky(T* A, int k, int lda, int* sflag) {
+  if (threadIdx.x == 0) *sflag = 1;
+  __syncthreads();
+  for (int j = 0; j < k; ++j) {
+    if (threadIdx.x == 0) {
+      const T d = A[j * lda + j];
+      if (!(d > T(0)) || !isfinite((double)d)) *sflag = 0;
+      A[j * lda + j] = dsqrt<T>(d > T(0) ? d : T(1));
+    }
+    __syncthreads();
+    const T ljj = A[j * lda + j];
+    for (int i = j + 1 + threadIdx.x; i < k; i += blockDim.x) A[i * lda + j] = A[i * lda + j] / ljj;
+    __syncthreads();
+    const int m = k - j - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = j + 1 + e / m, l = j + 1 + e % m;
+      if (l <= i) A[i * lda + l] -= A[i * lda + j] * A[l * lda + j];
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int i = e / k, l = e % k;
+    if (l > i) A[i * lda + l] = T(0);
+  }
+  __syncthreads();
+  return *sflag != 0;
+}
+
+// Li = L^-1 for lower-triangular L (row by row; columns in parallel).
+template <typename T>
+__device__ void cta_lower_inverse(const T* L, T* Li, int k, int lda) {
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) Li[(e / k) * lda + e % k] = T(0);
+  __syncthreads();
+  for (int i = 0; i < k; ++i) {
+    for (int c = threadIdx.x; c <= i; c += blockDim.x) {
+      T s = (c == i) ? T(1) : T(0);
+      for (int m = c; m < i; ++m) s -= L[i * lda + m] * Li[m * lda + c];
+      Li[i * lda + c] = s / L[i * lda + i];
+    }
+    __syncthreads();
+  }
+}
+
+// Ainv = Li^T Li (the inverse of A = L L^T), full symmetric matrix.
+template <typename T>
+__device__ void cta_gram_of_lower(const T* Li, T* Ainv, int k, int lda) {
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int i = e / k, j = e % k;
+    const int m0 = i > j ? i : j;
+    T s = T(0);
+    for (int m = m0; m < k; ++m) s += Li[m * lda + i] * Li[m * lda + j];
+    Ainv[i * lda + j] = s;
+  }
+  __syncthreads();
+}
+
+// Parallel cyclic Jacobi: A (kp x kp, kp even, symmetric) is diagonalised in
+// place, V receives the eigenvectors as columns (A_in = V diag(A_out) V^T).
+// A rotation of pair (p, q) is skipped when |a_pq| <= tol sqrt(|a_pp a_qq|).
+// Scratch: rot (4 * kp/2 values of T), pair (kp ints).  Returns sweeps run
+// (max_sweeps + 1 if it had not converged).
+template <typename T>
+__device__ int cta_jacobi(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T* rot, int* pair) {
+  for (int e = threadIdx.x; e < kp * kp; e += blockDim.x) {
+    const int i = e / kp, j = e % kp;
+    V[i * lda + j] = (i == j) ? T(1) : T(0);
+  }
+  __syncthreads();
+  const int h = kp >> 1, m = kp - 1;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    int rotated = 0;
+    for (int r = 0; r < m; ++r) {
+      for (int i = threadIdx.x; i < h; i += blockDim.x) {
+        int p, q;
+        if (i == 0) {
+          p = r;
+          q = m;
+        } else {
+          p = (r + i) % m;
+          q = (r - i + m) % m;
+        }
+        if (p > q) { const int t = p; p = q; q = t; }
+        const T app = A[p * lda + p], aqq = A[q * lda + q], apq = A[p * lda + q];
+        T c = T(1), s = T(0), t = T(0);
+        if (apq != T(0) && fabs((double)apq) > (double)tol * sqrt(fabs((double)app * (double)aqq))) {
+          const T theta = (aqq - app) / (T(2) * apq);
+          t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + dsqrt<T>(theta * theta + T(1)));
+          c = T(1) / dsqrt<T>(t * t + T(1));
+          s = t * c;
+          rotated = 1;
+        }
+        pair[2 * i] = p;
+        pair[2 * i + 1] = q;
+        rot[4 * i + 0] = c;
+        rot[4 * i + 1] = s;
+        rot[4 * i + 2] = app - t * apq;  // new a_pp
+        rot[4 * i + 3] = aqq + t * apq;  // new a_qq
+      }
+      __syncthreads();
+      // Rows p, q.
+      for (int e = threadIdx.x; e < h * kp; e += blockDim.x) {
+        const int i = e / kp, j = e % kp;
+        const T s = rot[4 * i + 1];
+        if (s == T(0)) continue;
+        const T c = rot[4 * i + 0];
+        const int p = pair[2 * i], q = pair[2 * i + 1];
+        const T a = A[p * lda + j], b = A[q * lda + j];
+        A[p * lda + j] = c * a - s * b;
+        A[q * lda + j] = s * a + c * b;
+      }
+      __syncthreads();
+      // Columns p, q of A (2 x 2 block in closed form) and of V.
+      for (int e = threadIdx.x; e < h * kp; e += blockDim.x) {
+        const int i = e / kp, j = e % kp;
+        const T s = rot[4 * i + 1];
+        if (s == T(0)) continue;
+        const T c = rot[4 * i + 0];
+        const int p = pair[2 * i], q = pair[2 * i + 1];
+        if (j == p) {
+          A[p * lda + p] = rot[4 * i + 2];
+          A[p * lda + q] = T(0);
+        } else if (j == q) {
+          A[q * lda + p] = T(0);
+          A[q * lda + q] = rot[4 * i + 3];
+        } else {
+          const T a = A[j * lda + p], b = A[j * lda + q];
+          A[j * lda + p] = c * a - s * b;
+          A[j * lda + q] = s * a + c * b;
+        }
+        const T va = V[j * lda + p], vb = V[j * lda + q];
+        V[j * lda + p] = c * va - s * vb;
+        V[j * lda + q] = s * va + c * vb;
+      }
+      __syncthreads();
+    }
+    if (!__syncthreads_or(rotated)) break;
+  }
+  return sweep + 1;
+}
+
+// The k x k part of one ensemble-space analysis.  On entry A holds
+// diag * I + Y'^T R^-1 Y' (k x k, padded to kp with a decoupled unit
+// diagonal when k is odd) and b = Y'^T R^-1 d.  On exit A holds W (k x k) and
+// wa the mean weights, so that
+//   compat square root (use_chol): W = sqrt(k-1) chol_L(Pa), Pa = A^-1 (x rho
+//     when infl_compat) -- ETKF.hpp:150-159, LETKF.hpp:215-224;
+//   symmetric (Hunt): A = V diag(lam) V^T, Pa = sc V diag(1/lam) V^T,
+//     W = V diag(sqrt((k-1) sc / lam)) V^T, sc = rho when infl_compat else 1;
+//   wa = Pa b in both.
+// Scratch: V (kp x lda), lam, uvec (k), rot (2 kp), pairbuf (kp ints),
+// misc (4 ints).  Returns false if the system was not positive definite.
+template <typename T>
+__device__ bool solve_transform(T* A, T* V, const T* bvec, T* wa, T* lam, T* uvec, T* rot,
+                                int* pairbuf, int* misc, int k, int kp, int lda, bool use_chol,
+                                bool infl_compat, double rho, T tol, int sweep_cap, int* sweeps) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  bool ok = true;
+  *sweeps = 0;
+  if (use_chol) {
+    ok = cta_cholesky<T>(A, k, lda, misc);
+    cta_lower_inverse<T>(A, V, k, lda);
+    cta_gram_of_lower<T>(V, A, k, lda);
+    if (infl_compat)
+      for (int e = tid; e < k * k; e += nt) A[(e / k) * lda + e % k] *= (T)rho;
+    __syncthreads();
+    for (int i = tid; i < k; i += nt) {
+      T s = T(0);
+      for (int j = 0; j < k; ++j) s += A[i * lda + j] * bvec[j];
+      wa[i] = s;
+    }
+    __syncthreads();
+    ok = cta_cholesky<T>(A, k, lda, misc) && ok;
+    const T sqk = (T)sqrt((double)(k - 1));
+    for (int e = tid; e < k * k; e += nt) A[(e / k) * lda + e % k] *= sqk;
+    __syncthreads();
+    return ok;
+  }
+  if (tid == 0) misc[1] = 0;
+  *sweeps = cta_jacobi<T>(A, V, kp, lda, tol, sweep_cap, rot, pairbuf);
+  const T sc = infl_compat ? (T)rho : T(1);
+  for (int i = tid; i < k; i += nt) {
+    const T l = A[i * lda + i];
+    lam[i] = l;
+    if (!(l > T(0)) || !isfinite((double)l)) misc[1] = 1;
+  }
+  __syncthreads();
+  ok = misc[1] == 0;
+  for (int i = tid; i < k; i += nt) {  // u = diag(sc / lam) V^T b
+    T s = T(0);
+    for (int j = 0; j < k; ++j) s += V[j * lda + i] * bvec[j];
+    uvec[i] = s * sc / lam[i];
+  }
+  __syncthreads();
+  for (int i = tid; i < k; i += nt) {  // wa = V u
+    T s = T(0);
+    for (int m = 0; m < k; ++m) s += V[i * lda + m] * uvec[m];
+    wa[i] = s;
+  }
+  __syncthreads();
+  for (int i = tid; i < k; i += nt) uvec[i] = dsqrt<T>(T(k - 1) * sc / lam[i]);
+  __syncthreads();
+  for (int e = tid; e < k * k; e += nt) {
+    const int i = e / k, j = e - i * k;
+    T s = T(0);
+    for (int m = 0; m < k; ++m) s += V[i * lda + m] * uvec[m] * V[j * lda + m];
+    A[i * lda + j] = s;
+  }
+  __syncthreads();
+  return ok;
+}
+
+}  // namespace mg

@@ -1,0 +1,668 @@
+// Batched LETKF local analyses (replaces LETKF.hpp:101 grid loop and
+// updateGridPoint :152-243) and the sequential reference-order LETKF.
+//
+// One CTA (256 threads) runs one local analysis at a time, inside a
+// persistent grid that pulls analysis points from a work counter in
+// longest-list-first order (lists are sorted by length on the device), so
+// the uneven local-observation counts balance across SMs without any
+// device-side wait.
+//
+// Per analysis: the column's candidate list is filtered (vertical support)
+// and weighted (Gaspari-Cohn x 1/sigma^2, or 1 for the reference's R = I),
+// the local rows of Y' are gathered chunk by chunk into shared memory and
+// the k x k Gram Y'^T R^-1 Y' accumulated in a 16 x 16 grid of register
+// tiles; the k x k transform comes from a Cholesky path (reference) or the
+// parallel Jacobi eigen-solver (Hunt), and the update is applied to every
+// variable of the point.
+//
+// TE is the arithmetic type of the Gram, eigen-solve and update: double for
+// the FP64 path, float for the mixed path (means, innovations and outputs
+// stay double).
+#include <cub/device/device_radix_sort.cuh>
+
+#include <algorithm>
+#include <vector>
+
+#include "mg_dense.cuh"
+#include "mg_internal.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kNVarMax = 8;
+
+struct LetkfParams {
+  int k, kp, n_var, nlev;
+  int64_t ncol, npoints;
+  const int64_t* col_base;
+  int64_t lev_stride, var_stride;
+  const void* Xp;        // point-major perturbations, TE, [s*k + i]
+  const double* xmean;   // n
+  double* Xa;            // point-major analysis, [s*k + i]
+  const void* Y;         // obs anomalies, TE, [o*k + i]
+  const double* dinn;    // innovation
+  const double* rinv;    // 1 / error variance
+  const double* obs_lev; // or null
+  const int64_t* loc_off;
+  const int32_t* loc_idx;
+  const double* loc_dist;  // or null
+  double hsupport, vsupport, rho;
+  int flags;
+  const int32_t* order;  // columns, longest list first
+  unsigned long long* next;
+  unsigned long long* n_empty;
+  unsigned long long* total_local;
+  int* max_local;
+  int* max_sweeps;
+  int* status;
+  double tol;
+  int sweep_cap;
+};
+
+__device__ __forceinline__ double gaspari_cohn(double z) {
+  z = fabs(z);
+  if (z >= 2.0) return 0.0;
+  if (z <= 1.0) return (((-0.25 * z + 0.5) * z + 0.625) * z - 5.0 / 3.0) * z * z + 1.0;
+  return ((((z / 12.0 - 0.5) * z + 0.625) * z + 5.0 / 3.0) * z - 5.0) * z + 4.0 - 2.0 / (3.0 * z);
+}
+
+template <typename TE, int KMAX>
+struct Smem {
+  static constexpr int LDA = KMAX + 1;
+  static constexpr int CH = (sizeof(TE) == 8 && KMAX > 64) ? 32 : 64;  // Gram chunk rows
+  static constexpr size_t bytes() {
+    return sizeof(TE) * (2 * (size_t)KMAX * LDA + (size_t)CH * KMAX + 3 * CH + 4 * KMAX +
+                         2 * KMAX + kNVarMax * KMAX) +
+           sizeof(double) * (2 * kNVarMax) + sizeof(int) * (CH + KMAX + 16) + 64;
+  }
+};
+
+template <typename TE, int KMAX>
+__global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm) {
+  using S = Smem<TE, KMAX>;
+  constexpr int LDA = S::LDA, CH = S::CH, R = KMAX / 16;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TE* A = reinterpret_cast<TE*>(smem_raw);
+  TE* V = A + KMAX * LDA;
+  TE* Ys = V + KMAX * LDA;        // CH x KMAX
+  TE* sel_r = Ys + CH * KMAX;     // CH
+  TE* sel_d = sel_r + CH;         // CH
+  TE* bvec = sel_d + CH;          // KMAX
+  TE* wa = bvec + KMAX;           // KMAX
+  TE* uvec = wa + KMAX;           // KMAX
+  TE* lam = uvec + KMAX;          // KMAX
+  TE* rot = lam + KMAX;           // 2*KMAX (4 per pair)
+  TE* Xs = rot + 2 * KMAX;        // kNVarMax x KMAX
+  double* xm = reinterpret_cast<double*>(Xs + kNVarMax * KMAX);  // kNVarMax
+  double* red = xm + kNVarMax;                                   // kNVarMax
+  int* sel_o = reinterpret_cast<int*>(red + kNVarMax);           // CH
+  int* pairbuf = sel_o + CH;                                     // KMAX
+  int* misc = pairbuf + KMAX;                                    // 16
+  __shared__ long long s_item;
+  __shared__ int wcnt[kThreads / 32];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k = prm.k, kp = prm.kp;
+  const TE* Y = static_cast<const TE*>(prm.Y);
+  const TE* Xp = static_cast<const TE*>(prm.Xp);
+  const int ti = tid / 16, tj = tid % 16;
+  const bool r_identity = prm.flags & MG_R_IDENTITY;
+  const bool use_chol = prm.flags & MG_SQRT_CHOLESKY;
+  const bool infl_compat = prm.flags & MG_INFL_COMPAT;
+  const bool upd_compat = prm.flags & MG_UPDATE_COMPAT;
+  const bool rtps = prm.flags & MG_RTPS;
+  const double hc = 0.5 * prm.hsupport, vc = 0.5 * prm.vsupport;
+
+  for (;;) {
+    if (tid == 0) s_item = (long long)atomicAdd(prm.next, 1ull);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= prm.npoints) break;
+    const int64_t col = prm.order[item / prm.nlev];
+    const int lev = (int)(item % prm.nlev);
+    const int64_t base = prm.col_base[col] + (int64_t)lev * prm.lev_stride;
+    const int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
+
+    // ---- Gram and b accumulation over the local list, chunk by chunk ----
+    TE acc[R][R];
+#pragma unroll
+    for (int a = 0; a < R; ++a)
+#pragma unroll
+      for (int b = 0; b < R; ++b) acc[a][b] = TE(0);
+    TE bacc = TE(0);
+    int nloc = 0;
+    for (int64_t c0 = e0; c0 < e1; c0 += CH) {
+      bool keep = false;
+      int o = 0;
+      TE rw = TE(0), dd = TE(0);
+      if (tid < CH && c0 + tid < e1) {
+        const int64_t e = c0 + tid;
+        o = prm.loc_idx[e];
+        double w = 1.0;
+        keep = true;
+        if (prm.obs_lev) {
+          const double dl = fabs((double)lev - prm.obs_lev[o]);
+          if (dl > prm.vsupport) keep = false;
+          else if (!r_identity) w *= gaspari_cohn(dl / vc);
+        }
+        if (keep && !r_identity) {
+          if (prm.loc_dist) w *= gaspari_cohn(prm.loc_dist[e] / hc);
+          w *= prm.rinv[o];
+          if (!(w > 0.0)) keep = false;
+        }
+        rw = (TE)w;
+        dd = (TE)prm.dinn[o];
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (lane == 0) wcnt[warp] = __popc(bal);
+      __syncthreads();
+      int wbase = 0, cnt = 0;
+#pragma unroll
+      for (int w = 0; w < kThreads / 32; ++w) {
+        if (w < warp) wbase += wcnt[w];
+        cnt += wcnt[w];
+      }
+      if (keep) {
+        const int pos = wbase + __popc(bal & ((1u << lane) - 1u));
+        sel_o[pos] = o;
+        sel_r[pos] = rw;
+        sel_d[pos] = dd;
+      }
+      __syncthreads();
+      for (int e = tid; e < cnt * KMAX; e += kThreads) {
+        const int r = e / KMAX, j = e - r * KMAX;
+        Ys[e] = (j < k) ? Y[(int64_t)sel_o[r] * k + j] : TE(0);
+      }
+      __syncthreads();
+      for (int r = 0; r < cnt; ++r) {
+        const TE w = sel_r[r];
+        TE av[R], bv[R];
+#pragma unroll
+        for (int a = 0; a < R; ++a) av[a] = Ys[r * KMAX + ti * R + a] * w;
+#pragma unroll
+        for (int b = 0; b < R; ++b) bv[b] = Ys[r * KMAX + tj * R + b];
+#pragma unroll
+        for (int a = 0; a < R; ++a)
+#pragma unroll
+          for (int b = 0; b < R; ++b) acc[a][b] += av[a] * bv[b];
+      }
+      if (tid < k)
+        for (int r = 0; r < cnt; ++r) bacc += (Ys[r * KMAX + tid] * sel_r[r]) * sel_d[r];
+      nloc += cnt;
+      __syncthreads();
+    }
+
+    // Load this point's perturbations and means (all variables).
+    for (int e = tid; e < prm.n_var * k; e += kThreads) {
+      const int v = e / k, i = e - v * k;
+      Xs[v * KMAX + i] = Xp[(base + (int64_t)v * prm.var_stride) * k + i];
+    }
+    if (tid < prm.n_var) xm[tid] = prm.xmean[base + (int64_t)tid * prm.var_stride];
+
+    if (nloc == 0) {
+      // LETKF.hpp:167-190: no local obs, x' *= sqrt(rho) (RTPS: unchanged).
+      __syncthreads();
+      const double sr = rtps ? 1.0 : sqrt(prm.rho);
+      for (int e = tid; e < prm.n_var * k; e += kThreads) {
+        const int v = e / k, i = e - v * k;
+        prm.Xa[(base + (int64_t)v * prm.var_stride) * k + i] = xm[v] + (double)Xs[v * KMAX + i] * sr;
+      }
+      if (tid == 0) atomicAdd(prm.n_empty, 1ull);
+      __syncthreads();
+      continue;
+    }
+
+    // ---- k x k system ----
+    const TE diag = (infl_compat || rtps) ? TE(k - 1) : TE((double)(k - 1) / prm.rho);
+#pragma unroll
+    for (int a = 0; a < R; ++a)
+#pragma unroll
+      for (int b = 0; b < R; ++b) {
+        const int i = ti * R + a, j = tj * R + b;
+        if (i < kp && j < kp) {
+          TE v = (i < k && j < k) ? acc[a][b] : TE(0);
+          if (i == j) v += (i < k) ? diag : TE(1);
+          A[i * LDA + j] = v;
+        }
+      }
+    if (tid < k) bvec[tid] = bacc;
+    __syncthreads();
+
+    int sweeps = 0;
+    const bool ok = mg::solve_transform<TE>(A, V, bvec, wa, lam, uvec, rot, pairbuf, misc, k, kp,
+                                            LDA, use_chol, infl_compat, prm.rho, (TE)prm.tol,
+                                            prm.sweep_cap, &sweeps);
+    if (!ok && tid == 0) atomicExch(prm.status, 1);
+
+    // ---- update every variable of the point ----
+    for (int e = tid; e < prm.n_var * k; e += kThreads) {
+      const int v = e / k, i = e - v * k;
+      const TE* x = Xs + v * KMAX;
+      double out;
+      if (upd_compat) {  // xa_i = (xm + x'_i wa_i) + sum_j x'_i W_ij, LETKF.hpp:232-238
+        const TE xp = x[i];
+        TE rs = TE(0);
+        for (int j = 0; j < k; ++j) rs += xp * A[i * LDA + j];
+        out = (xm[v] + (double)(xp * wa[i])) + (double)rs;
+      } else {  // xa_i = xm + sum_j x'_j (wa_j + W_ji)
+        TE inc = TE(0), s2 = TE(0);
+        for (int j = 0; j < k; ++j) {
+          inc += x[j] * wa[j];
+          s2 += x[j] * A[j * LDA + i];
+        }
+        out = (xm[v] + (double)inc) + (double)s2;
+        if (rtps) Ys[v * KMAX + i] = s2;  // analysis perturbation for the spread
+      }
+      prm.Xa[(base + (int64_t)v * prm.var_stride) * k + i] = out;
+    }
+    if (rtps && !upd_compat) {
+      __syncthreads();
+      if (tid < prm.n_var) {
+        double sb = 0.0, sa = 0.0;
+        for (int i = 0; i < k; ++i) {
+          const double xb = (double)Xs[tid * KMAX + i], xa = (double)Ys[tid * KMAX + i];
+          sb += xb * xb;
+          sa += xa * xa;
+        }
+        sb = sqrt(sb / (k - 1));
+        sa = sqrt(sa / (k - 1));
+        red[tid] = (sa > 0.0) ? prm.rho * (sb - sa) / sa : 0.0;  // factor - 1
+      }
+      __syncthreads();
+      for (int e = tid; e < prm.n_var * k; e += kThreads) {
+        const int v = e / k, i = e - v * k;
+        prm.Xa[(base + (int64_t)v * prm.var_stride) * k + i] += red[v] * (double)Ys[v * KMAX + i];
+      }
+    }
+    if (tid == 0) {
+      atomicAdd(prm.total_local, (unsigned long long)nloc);
+      atomicMax(prm.max_local, nloc);
+      atomicMax(prm.max_sweeps, sweeps);
+    }
+    __syncthreads();
+  }
+}
+
+// Column list lengths (keys) for the longest-first order.
+__global__ void list_len_kernel(const int64_t* __restrict__ off, int64_t ncol,
+                                uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncol) {
+    const int64_t len = off[c + 1] - off[c];
+    keys[c] = 0xffffffffu - (uint32_t)(len > 0xffffffffll ? 0xffffffffll : len);  // descending
+    vals[c] = (int32_t)c;
+  }
+}
+
+template <typename TE, int KMAX>
+int launch_batched(mg_context* ctx, LetkfParams& prm) {
+  const size_t smem = Smem<TE, KMAX>::bytes();
+  if (smem > 227 * 1024) return mg::fail(ctx, MG_ERR_ARG, "mg_letkf_batched: k too large for this precision");
+  MG_TRY_CUDA(cudaFuncSetAttribute(letkf_batched_kernel<TE, KMAX>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  MG_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, letkf_batched_kernel<TE, KMAX>,
+                                                            kThreads, smem));
+  if (per_sm < 1) return mg::fail(ctx, MG_ERR_ARG, "mg_letkf_batched: kernel does not fit on an SM");
+  int64_t grid = (int64_t)per_sm * ctx->num_sms;
+  if (grid > prm.npoints) grid = prm.npoints;
+  if (grid < 1) grid = 1;
+  letkf_batched_kernel<TE, KMAX><<<(unsigned)grid, kThreads, smem, ctx->stream>>>(prm);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+// ------------------------------------------------------------------------
+// Sequential LETKF in the reference's order (LETKF.hpp:101), one CTA.
+// ------------------------------------------------------------------------
+struct CompatSeqParams {
+  double* X;
+  int k, nx, ny;
+  int64_t ld;
+  const int32_t* obs_xy;
+  const uint8_t* valid;
+  const double* yo;
+  const int64_t* loc_off;
+  const int32_t* loc_idx;
+  double rho;
+  int* status;
+};
+
+__device__ __forceinline__ double idw4_seq(const double* x, int nx, int ny, int ox, int oy) {
+  const double xx = fmax(0.0, fmin((double)(nx - 1), (double)ox));
+  const double yy = fmax(0.0, fmin((double)(ny - 1), (double)oy));
+  const long long i0 = (long long)floor(xx), j0 = (long long)floor(yy);
+  const long long i1 = min(i0 + 1, (long long)nx - 1), j1 = min(j0 + 1, (long long)ny - 1);
+  const long long ii[4] = {i0, i1, i0, i1}, jj[4] = {j0, j0, j1, j1};
+  double ws = 0.0, wsum = 0.0;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const double dx = __dsub_rn(xx, (double)ii[t]), dy = __dsub_rn(yy, (double)jj[t]);
+    const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    const double w = (dist == 0.0) ? 1e12 : __ddiv_rn(1.0, dist);
+    ws = __dadd_rn(ws, __dmul_rn(w, x[jj[t] * nx + ii[t]]));
+    wsum = __dadd_rn(wsum, w);
+  }
+  return __ddiv_rn(ws, wsum);
+}
+
+template <int KMAX>
+__global__ void __launch_bounds__(kThreads) letkf_compat_seq_kernel(CompatSeqParams prm) {
+  constexpr int LDA = KMAX + 1, CH = 64;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* A = reinterpret_cast<double*>(smem_raw);
+  double* V = A + KMAX * LDA;
+  double* Ys = V + KMAX * LDA;  // CH x KMAX
+  double* dd = Ys + CH * KMAX;  // CH
+  double* bvec = dd + CH;       // KMAX
+  double* wa = bvec + KMAX;     // KMAX
+  double* xb = wa + KMAX;       // KMAX
+  int* misc = reinterpret_cast<int*>(xb + KMAX);
+  __shared__ double s_xm;
+  const int tid = threadIdx.x, k = prm.k;
+  const int npt = prm.nx * prm.ny;
+  const double sqk = sqrt((double)(k - 1));
+  for (int g = 0; g < npt; ++g) {
+    const int64_t e0 = prm.loc_off[g], e1 = prm.loc_off[g + 1];
+    double acc[KMAX / 16][KMAX / 16];
+    constexpr int R = KMAX / 16;
+    const int ti = tid / 16, tj = tid % 16;
+#pragma unroll
+    for (int a = 0; a < R; ++a)
+#pragma unroll
+      for (int b = 0; b < R; ++b) acc[a][b] = 0.0;
+    double bacc = 0.0;
+    for (int64_t c0 = e0; c0 < e1; c0 += CH) {
+      const int cnt = (int)(e1 - c0 < (int64_t)CH ? e1 - c0 : (int64_t)CH);
+      // H_local rows from the CURRENT members (LETKF.hpp:197-206).
+      for (int e = tid; e < cnt * KMAX; e += kThreads) {
+        const int r = e / KMAX, j = e - r * KMAX;
+        double v = 0.0;
+        if (j < k) {
+          const int o = prm.loc_idx[c0 + r];
+          if (!prm.valid || prm.valid[o])
+            v = idw4_seq(prm.X + (int64_t)j * prm.ld, prm.nx, prm.ny, prm.obs_xy[2 * o],
+                         prm.obs_xy[2 * o + 1]);
+        }
+        Ys[e] = v;
+      }
+      __syncthreads();
+      if (tid < cnt) {  // row mean, anomalies, innovation (:209-211)
+        double s = 0.0;
+        for (int j = 0; j < k; ++j) s += Ys[tid * KMAX + j];
+        const double ym = s / (double)k;
+        for (int j = 0; j < k; ++j) Ys[tid * KMAX + j] -= ym;
+        dd[tid] = prm.yo[prm.loc_idx[c0 + tid]] - ym;
+      }
+      __syncthreads();
+      for (int r = 0; r < cnt; ++r) {
+#pragma unroll
+        for (int a = 0; a < R; ++a)
+#pragma unroll
+          for (int b = 0; b < R; ++b)
+            acc[a][b] += Ys[r * KMAX + ti * R + a] * Ys[r * KMAX + tj * R + b];
+      }
+      if (tid < k)
+        for (int r = 0; r < cnt; ++r) bacc += Ys[r * KMAX + tid] * dd[r];
+      __syncthreads();
+    }
+    if (tid < k) xb[tid] = prm.X[(int64_t)tid * prm.ld + g];
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int i = 0; i < k; ++i) s += xb[i];
+      s_xm = s / (double)k;
+    }
+    __syncthreads();
+    const double xm = s_xm;
+    if (e1 == e0) {  // LETKF.hpp:167-190
+      const double sr = sqrt(prm.rho);
+      if (tid < k) prm.X[(int64_t)tid * prm.ld + g] = xm + (xb[tid] - xm) * sr;
+      __syncthreads();
+      continue;
+    }
+#pragma unroll
+    for (int a = 0; a < R; ++a)
+#pragma unroll
+      for (int b = 0; b < R; ++b) {
+        const int i = ti * R + a, j = tj * R + b;
+        if (i < k && j < k) A[i * LDA + j] = acc[a][b] + (i == j ? (double)(k - 1) : 0.0);
+      }
+    if (tid < k) bvec[tid] = bacc;
+    __syncthreads();
+    bool ok = mg::cta_cholesky<double>(A, k, LDA, misc);
+    mg::cta_lower_inverse<double>(A, V, k, LDA);
+    mg::cta_gram_of_lower<double>(V, A, k, LDA);
+    for (int e = tid; e < k * k; e += kThreads) A[(e / k) * LDA + e % k] *= prm.rho;
+    __syncthreads();
+    if (tid < k) {
+      double s = 0.0;
+      for (int j = 0; j < k; ++j) s += A[tid * LDA + j] * bvec[j];
+      wa[tid] = s;
+    }
+    __syncthreads();
+    ok = mg::cta_cholesky<double>(A, k, LDA, misc) && ok;
+    if (!ok && tid == 0) atomicExch(prm.status, 1);
+    if (tid < k) {  // :227-242, in place
+      const double xp = xb[tid] - xm;
+      double rs = 0.0;
+      for (int j = 0; j < k; ++j) rs += xp * (sqk * A[tid * LDA + j]);
+      prm.X[(int64_t)tid * prm.ld + g] = (xm + xp * wa[tid]) + rs;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(d != nullptr, "mg_letkf_batched: null descriptor");
+  MG_CHECK_ARG(d->X && d->n > 0 && d->ld >= d->n && d->k >= 2 && d->k <= 128 && d->n_var >= 1 &&
+                   d->n_var <= kNVarMax && d->nlev >= 1 && d->ncol >= 1 && d->col_base &&
+                   d->p >= 0 && d->loc_off && (d->p == 0 || (d->HX && d->yo && d->rvar)) &&
+                   d->rho > 0.0,
+               "mg_letkf_batched: bad descriptor");
+  MG_CHECK_ARG(d->precision == MG_PREC_FP64 || d->precision == MG_PREC_MIXED,
+               "mg_letkf_batched: bad precision");
+  MG_CHECK_ARG(!(d->flags & MG_RTPS) || !(d->flags & MG_UPDATE_COMPAT),
+               "mg_letkf_batched: RTPS needs the Hunt update");
+  const bool fp64 = d->precision == MG_PREC_FP64;
+  const int k = d->k;
+  MG_CHECK_ARG(!fp64 || k <= 96, "mg_letkf_batched: FP64 path supports k <= 96");
+  const int64_t n = d->n, p = d->p;
+  const int64_t npoints = d->ncol * d->nlev;
+  const size_t te = fp64 ? sizeof(double) : sizeof(float);
+  const size_t sort_bytes = [&] {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (const int32_t*)nullptr, (int32_t*)nullptr, (int)d->ncol);
+    return b + 256;
+  }();
+  mg::Carver cv;
+  cv.reserve<char>((size_t)n * k * te);            // Xp
+  cv.reserve<double>((size_t)n);                   // mean
+  cv.reserve<double>((size_t)n * k);               // Xa
+  cv.reserve<char>((size_t)(p + 1) * k * te);      // Y
+  cv.reserve<double>((size_t)p + 1);               // d
+  cv.reserve<double>((size_t)p + 1);               // rinv
+  cv.reserve<uint32_t>((size_t)d->ncol * 2);       // keys
+  cv.reserve<int32_t>((size_t)d->ncol * 2);        // vals
+  cv.reserve<unsigned long long>(8);               // counters
+  cv.reserve<char>(sort_bytes);
+  void* ws = mg::workspace(ctx, cv.off);
+  if (!ws) return MG_ERR_NOMEM;
+  cv = mg::Carver{static_cast<char*>(ws), 0};
+  void* Xp = cv.take<char>((size_t)n * k * te);
+  double* mean = cv.take<double>((size_t)n);
+  double* Xa = cv.take<double>((size_t)n * k);
+  void* Y = cv.take<char>((size_t)(p + 1) * k * te);
+  double* dinn = cv.take<double>((size_t)p + 1);
+  double* rinv = cv.take<double>((size_t)p + 1);
+  uint32_t* keys = cv.take<uint32_t>((size_t)d->ncol * 2);
+  int32_t* vals = cv.take<int32_t>((size_t)d->ncol * 2);
+  auto* cnt = cv.take<unsigned long long>(8);
+  void* sort_tmp = cv.take<char>(sort_bytes);
+  cudaStream_t s = ctx->stream;
+
+  MG_TRY_CUDA(cudaEventRecord(ctx->ev[0], s));
+  // Point-major perturbations and means (Ensemble.hpp:105-151).
+  MG_TRY_CUDA(mg::launch_to_point_major(d->X, n, k, d->ld, mean, fp64 ? (double*)Xp : nullptr,
+                                        fp64 ? nullptr : (float*)Xp, s));
+  // Obs-space prior from the background (snapshot).
+  if (p > 0)
+    MG_TRY_CUDA(mg::launch_obs_prior(d->HX, d->yo, d->rvar, p, k, fp64 ? (double*)Y : nullptr,
+                                     fp64 ? nullptr : (float*)Y, dinn, rinv, s));
+  // Longest-list-first order of the columns.
+  list_len_kernel<<<(unsigned)((d->ncol + 255) / 256), 256, 0, s>>>(d->loc_off, d->ncol, keys,
+                                                                   vals);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  size_t sb = sort_bytes - 256;
+  MG_TRY_CUDA(cub::DeviceRadixSort::SortPairs(sort_tmp, sb, keys, keys + d->ncol, vals,
+                                              vals + d->ncol, (int)d->ncol, 0, 32, s));
+  MG_TRY_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * 8, s));
+
+  LetkfParams prm{};
+  prm.k = k;
+  prm.kp = k + (k & 1);
+  prm.n_var = d->n_var;
+  prm.nlev = d->nlev;
+  prm.ncol = d->ncol;
+  prm.npoints = npoints;
+  prm.col_base = d->col_base;
+  prm.lev_stride = d->lev_stride;
+  prm.var_stride = d->var_stride;
+  prm.Xp = Xp;
+  prm.xmean = mean;
+  prm.Xa = Xa;
+  prm.Y = Y;
+  prm.dinn = dinn;
+  prm.rinv = rinv;
+  prm.obs_lev = d->obs_lev;
+  prm.loc_off = d->loc_off;
+  prm.loc_idx = d->loc_idx;
+  prm.loc_dist = d->loc_dist;
+  prm.hsupport = d->hsupport;
+  prm.vsupport = d->vsupport;
+  prm.rho = d->rho;
+  prm.flags = d->flags;
+  prm.order = vals + d->ncol;
+  prm.next = cnt + 0;
+  prm.n_empty = cnt + 1;
+  prm.total_local = cnt + 2;
+  prm.max_local = reinterpret_cast<int*>(cnt + 3);
+  prm.max_sweeps = reinterpret_cast<int*>(cnt + 3) + 1;
+  prm.status = reinterpret_cast<int*>(cnt + 4);
+  prm.tol = fp64 ? 1e-14 : 1e-6;
+  prm.sweep_cap = fp64 ? 30 : 20;
+  MG_TRY_CUDA(cudaEventRecord(ctx->ev[1], s));
+  int rc;
+  if (fp64) {
+    if (k <= 32) rc = launch_batched<double, 32>(ctx, prm);
+    else if (k <= 64) rc = launch_batched<double, 64>(ctx, prm);
+    else rc = launch_batched<double, 96>(ctx, prm);
+  } else {
+    if (k <= 32) rc = launch_batched<float, 32>(ctx, prm);
+    else if (k <= 64) rc = launch_batched<float, 64>(ctx, prm);
+    else if (k <= 96) rc = launch_batched<float, 96>(ctx, prm);
+    else rc = launch_batched<float, 128>(ctx, prm);
+  }
+  if (rc != MG_OK) return rc;
+  MG_TRY_CUDA(cudaEventRecord(ctx->ev[2], s));
+  // Write back member-major; the analysis mean as LETKF.hpp:116 recomputes it.
+  MG_TRY_CUDA(mg::launch_point_major_to_members(Xa, n, k, d->X, d->ld, s));
+  if (d->mean_out)
+    MG_TRY_CUDA(mg::launch_mean_pert_members(d->X, n, k, d->ld, d->mean_out, nullptr, nullptr, 0, s));
+  MG_TRY_CUDA(cudaEventRecord(ctx->ev[3], s));
+  unsigned long long host_cnt[5];
+  MG_TRY_CUDA(cudaMemcpyAsync(host_cnt, cnt, sizeof(host_cnt), cudaMemcpyDeviceToHost, s));
+  MG_TRY_CUDA(cudaStreamSynchronize(s));
+  float ms[3] = {0.f, 0.f, 0.f};
+  for (int i = 0; i < 3; ++i) MG_TRY_CUDA(cudaEventElapsedTime(&ms[i], ctx->ev[i], ctx->ev[i + 1]));
+  ctx->stats.ms_prepare = ms[0];
+  ctx->stats.ms_analysis = ms[1];
+  ctx->stats.ms_writeback = ms[2];
+  ctx->stats.n_points = npoints;
+  ctx->stats.n_empty = (int64_t)host_cnt[1];
+  ctx->stats.total_local = (int64_t)host_cnt[2];
+  ctx->stats.max_local = (int32_t)(host_cnt[3] & 0xffffffffull);
+  ctx->stats.max_sweeps = (int32_t)(host_cnt[3] >> 32);
+  if ((int)(host_cnt[4] & 0xffffffffull) != 0)
+    return mg::fail(ctx, MG_ERR_NUMERIC, "mg_letkf_batched: a local k x k system was not positive definite");
+  return MG_OK;
+}
+
+int mg_letkf_compat_grid(mg_context* ctx, double* X, int32_t k, int64_t ld, int32_t nx, int32_t ny,
+                         const int32_t* obs_xy, const uint8_t* valid, const double* yo, int64_t p,
+                         double radius, double rho, double* mean_out) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(X && k >= 2 && k <= 64 && nx > 0 && ny > 0 && ld >= (int64_t)nx * ny && p >= 0 &&
+                   (p == 0 || (obs_xy && yo)) && rho > 0.0,
+               "mg_letkf_compat_grid: bad arguments (k must be 2..64)");
+  const int64_t npt = (int64_t)nx * ny;
+  // Local lists by grid distance (independent of the in-place updates).
+  // mg_select_grid uses the context workspace, so these live apart from it.
+  int64_t total = 0;
+  int64_t* off_tmp = nullptr;
+  int32_t* idx = nullptr;
+  int* status = nullptr;
+  MG_TRY_CUDA(cudaMalloc(&off_tmp, sizeof(int64_t) * (npt + 1)));
+  int rc = mg_select_grid(ctx, nx, ny, obs_xy, p, radius, off_tmp, nullptr, 0, &total);
+  if (rc != MG_OK && rc != MG_ERR_CAPACITY) {
+    cudaFree(off_tmp);
+    return rc;
+  }
+  if (cudaMalloc(&idx, sizeof(int32_t) * (total + 1)) != cudaSuccess ||
+      cudaMalloc(&status, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(off_tmp);
+    cudaFree(idx);
+    return mg::fail(ctx, MG_ERR_NOMEM, "mg_letkf_compat_grid: allocation failed");
+  }
+  rc = mg_select_grid(ctx, nx, ny, obs_xy, p, radius, off_tmp, idx, total, &total);
+  if (rc == MG_OK) {
+    MG_TRY_CUDA(cudaMemsetAsync(status, 0, sizeof(int), ctx->stream));
+    CompatSeqParams prm{X, k, nx, ny, ld, obs_xy, valid, yo, off_tmp, idx, rho, status};
+    const int kmax = k <= 32 ? 32 : 64;
+    const size_t smem = sizeof(double) * (2 * (size_t)kmax * (kmax + 1) + 64 * (size_t)kmax + 64 +
+                                          3 * (size_t)kmax) + 64;
+    cudaError_t e;
+    if (kmax == 32) {
+      e = cudaFuncSetAttribute(letkf_compat_seq_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e == cudaSuccess) letkf_compat_seq_kernel<32><<<1, kThreads, smem, ctx->stream>>>(prm);
+      if (e == cudaSuccess) MG_COUNT_LAUNCH();
+    } else {
+      e = cudaFuncSetAttribute(letkf_compat_seq_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e == cudaSuccess) letkf_compat_seq_kernel<64><<<1, kThreads, smem, ctx->stream>>>(prm);
+      if (e == cudaSuccess) MG_COUNT_LAUNCH();
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) rc = mg::fail(ctx, MG_ERR_CUDA, std::string("letkf_compat_seq: ") + cudaGetErrorString(e));
+    if (rc == MG_OK && mean_out) {
+      e = mg::launch_mean_pert_members(X, npt, k, ld, mean_out, nullptr, nullptr, 0, ctx->stream);
+      if (e != cudaSuccess) rc = mg::fail(ctx, MG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    int hs = 0;
+    if (rc == MG_OK) {
+      e = cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) rc = mg::fail(ctx, MG_ERR_CUDA, cudaGetErrorString(e));
+      else if (hs != 0)
+        rc = mg::fail(ctx, MG_ERR_NUMERIC, "mg_letkf_compat_grid: a local k x k system was not positive definite");
+    }
+  }
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(idx);
+  cudaFree(status);
+  cudaFree(off_tmp);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,420 @@
+// Local observation search (LETKF.hpp:159-165 with Location::distance_to).
+//
+// Grid coordinates: exact integer distances, one warp per grid point, obs
+// scanned in order and compacted with warp ballots so every list comes out
+// in obs order, as the reference builds it.
+//
+// Geographic coordinates: a device-built spatial hash of 1 x 1 degree cells.
+// Each query column visits only the cells its radius can reach (latitude
+// band bound plus a longitude bound from the haversine inequality
+// a >= cos(lat_c) cos(lat_o) sin^2(dlon/2)), evaluates the reference
+// haversine on the candidates, then sorts its list by obs index in shared
+// memory.  Pairs whose GPU distance lies within 1e-9 relative of the radius
+// are re-decided on the host with the reference expression (glibc libm), so
+// the selection is bit-exact whatever the device's transcendental rounding.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mg_internal.h"
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kEarthKm = 6371.0;
+constexpr int kNBand = 180, kNLonCell = 360, kNCell = kNBand * kNLonCell;
+constexpr int kMaxList = 16384;   // longest per-column list sorted in shared memory
+constexpr int kBorderCap = 65536; // near-threshold pairs re-decided on the host
+constexpr double kBorderRel = 1e-9;
+
+struct BorderRec {
+  int64_t col;
+  int64_t obs;
+  double clat, clon, olat, olon;
+};
+
+// ---------------------------------------------------------------- grid ----
+__global__ void select_grid_kernel(int nx, int ny, const int32_t* __restrict__ obs_xy, int64_t p,
+                                   double radius, const int64_t* __restrict__ offsets,
+                                   int64_t* __restrict__ counts, int32_t* __restrict__ idx) {
+  const int lane = threadIdx.x & 31;
+  const int64_t npt = (int64_t)nx * ny;
+  const int64_t g = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (g >= npt) return;
+  const int gx = (int)(g % nx), gy = (int)(g / nx);
+  int64_t w = offsets ? offsets[g] : 0;
+  for (int64_t o0 = 0; o0 < p; o0 += 32) {
+    const int64_t o = o0 + lane;
+    bool in = false;
+    if (o < p) {
+      const double dx = (double)(gx - obs_xy[2 * o]);
+      const double dy = (double)(gy - obs_xy[2 * o + 1]);
+      in = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy))) <= radius;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, in);
+    if (idx && in) idx[w + __popc(b & ((1u << lane) - 1u))] = (int32_t)o;
+    w += __popc(b);
+  }
+  if (!offsets && lane == 0) counts[g] = w;
+}
+
+// ----------------------------------------------------------- geographic ---
+__device__ __forceinline__ int cell_of(double lat, double lon) {
+  int band = (int)floor(lat + 90.0);
+  band = band < 0 ? 0 : (band >= kNBand ? kNBand - 1 : band);
+  double l = lon - 360.0 * floor(lon / 360.0);
+  int c = (int)floor(l);
+  c = c < 0 ? 0 : (c >= kNLonCell ? kNLonCell - 1 : c);
+  return band * kNLonCell + c;
+}
+
+// Location::haversine (Location.hpp:349-357) with the device's libm.
+__device__ __forceinline__ double haversine_dev(double lat1, double lon1, double lat2, double lon2) {
+  const double dlat = (lat2 - lat1) * kPi / 180.0;
+  const double dlon = (lon2 - lon1) * kPi / 180.0;
+  const double s1 = sin(dlat / 2), s2 = sin(dlon / 2);
+  const double a = s1 * s1 + cos(lat1 * kPi / 180.0) * cos(lat2 * kPi / 180.0) * s2 * s2;
+  return kEarthKm * (2 * atan2(sqrt(a), sqrt(1 - a)));
+}
+
+__global__ void cell_count_kernel(const double* __restrict__ lat, const double* __restrict__ lon,
+                                  int64_t p, unsigned long long* __restrict__ cnt) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p; o += stride)
+    atomicAdd(&cnt[cell_of(lat[o], lon[o])], 1ull);
+}
+
+__global__ void cell_scatter_kernel(const double* __restrict__ lat, const double* __restrict__ lon,
+                                    int64_t p, const int64_t* __restrict__ start,
+                                    unsigned long long* __restrict__ cursor,
+                                    int32_t* __restrict__ cobs, double* __restrict__ clat,
+                                    double* __restrict__ clon) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p; o += stride) {
+    const int c = cell_of(lat[o], lon[o]);
+    const int64_t pos = start[c] + (int64_t)atomicAdd(&cursor[c], 1ull);
+    cobs[pos] = (int32_t)o;
+    clat[pos] = lat[o];
+    clon[pos] = lon[o];
+  }
+}
+
+// Visits every candidate obs of column (la, lo) and calls f(obs, dist, cls)
+// with cls = +1 (inside), 0 (near the threshold), -1 (outside: not called).
+template <typename F>
+__device__ void visit_candidates(double la, double lo, double radius_km,
+                                 const int64_t* __restrict__ start, const int32_t* __restrict__ cobs,
+                                 const double* __restrict__ clat, const double* __restrict__ clon,
+                                 F&& f) {
+  const double theta = radius_km / kEarthKm;  // radians
+  const double theta_deg = theta * 180.0 / kPi;
+  const double sh = sin(0.5 * theta);
+  const double a_r = sh * sh;
+  const double rlo = radius_km * (1.0 - kBorderRel), rhi = radius_km * (1.0 + kBorderRel);
+  int b0 = (int)floor(la + 90.0 - theta_deg - 1e-6);
+  int b1 = (int)floor(la + 90.0 + theta_deg + 1e-6);
+  b0 = b0 < 0 ? 0 : b0;
+  b1 = b1 >= kNBand ? kNBand - 1 : b1;
+  const double cosc = cos(la * kPi / 180.0);
+  for (int band = b0; band <= b1; ++band) {
+    const double e0 = (double)band - 90.0, e1 = e0 + 1.0;
+    const double emax = fmax(fabs(e0), fabs(e1));
+    const double cmin = cos(emax * kPi / 180.0);
+    const double denom = cosc * cmin;
+    int c0 = 0, c1 = kNLonCell - 1;
+    bool full = true;
+    if (denom > a_r * (1.0 + 1e-6)) {
+      const double sarg = sqrt(a_r / denom) * (1.0 + 1e-9);
+      if (sarg < 1.0) {
+        const double dl = 2.0 * asin(sarg) * 180.0 / kPi + 1e-6;
+        if (2.0 * dl + 2.0 < 360.0) {
+          full = false;
+          c0 = (int)floor(lo - dl);
+          c1 = (int)floor(lo + dl);
+        }
+      }
+    }
+    for (int cc = c0; cc <= c1; ++cc) {
+      int c = full ? cc : ((cc % kNLonCell) + kNLonCell) % kNLonCell;
+      c += band * kNLonCell;
+      const int64_t s0 = start[c], s1 = start[c + 1];
+      for (int64_t t = s0 + threadIdx.x; t < s1; t += blockDim.x) {
+        const double d = haversine_dev(la, lo, clat[t], clon[t]);
+        if (d <= rlo)
+          f(cobs[t], d, 1, clat[t], clon[t]);
+        else if (d <= rhi)
+          f(cobs[t], d, 0, clat[t], clon[t]);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ bool key_rejected(const unsigned long long* rej, int nrej,
+                                             unsigned long long key) {
+  int lo = 0, hi = nrej;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (rej[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  return lo < nrej && rej[lo] == key;
+}
+
+__global__ void __launch_bounds__(256) geo_count_kernel(
+    const double* __restrict__ col_lat, const double* __restrict__ col_lon, int64_t ncol,
+    double radius_km, const int64_t* __restrict__ start, const int32_t* __restrict__ cobs,
+    const double* __restrict__ clat, const double* __restrict__ clon, int64_t* __restrict__ counts,
+    BorderRec* __restrict__ border, unsigned long long* __restrict__ nborder) {
+  __shared__ unsigned long long scount;
+  const int64_t col = blockIdx.x;
+  if (threadIdx.x == 0) scount = 0;
+  __syncthreads();
+  const double la = col_lat[col], lo = col_lon[col];
+  unsigned long long mine = 0;
+  visit_candidates(la, lo, radius_km, start, cobs, clat, clon,
+                   [&](int32_t o, double, int cls, double ola, double olo) {
+                     ++mine;
+                     if (cls == 0) {
+                       const unsigned long long slot = atomicAdd(nborder, 1ull);
+                       if (slot < (unsigned long long)kBorderCap)
+                         border[slot] = BorderRec{col, (int64_t)o, la, lo, ola, olo};
+                     }
+                   });
+  atomicAdd(&scount, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) counts[col] = (int64_t)scount;
+}
+
+__global__ void apply_rejections_kernel(const unsigned long long* __restrict__ rej, int nrej,
+                                        int64_t* __restrict__ counts) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nrej) atomicAdd(reinterpret_cast<unsigned long long*>(&counts[rej[t] >> 32]),
+                          (unsigned long long)-1ll);
+}
+
+__global__ void __launch_bounds__(256) geo_fill_kernel(
+    const double* __restrict__ col_lat, const double* __restrict__ col_lon, int64_t ncol,
+    double radius_km, const int64_t* __restrict__ start, const int32_t* __restrict__ cobs,
+    const double* __restrict__ clat, const double* __restrict__ clon,
+    const int64_t* __restrict__ offsets, const unsigned long long* __restrict__ rej, int nrej,
+    const double* __restrict__ obs_lat, const double* __restrict__ obs_lon,
+    int32_t* __restrict__ idx, double* __restrict__ dist, int* __restrict__ overflow) {
+  extern __shared__ int32_t slist[];  // capacity: next power of two >= kMaxList
+  __shared__ int scount;
+  const int64_t col = blockIdx.x;
+  const int64_t base = offsets[col];
+  const int64_t n = offsets[col + 1] - base;
+  if (n == 0) return;
+  if (n > kMaxList) {
+    if (threadIdx.x == 0) atomicExch(overflow, 1);
+    return;
+  }
+  if (threadIdx.x == 0) scount = 0;
+  __syncthreads();
+  const double la = col_lat[col], lo = col_lon[col];
+  visit_candidates(la, lo, radius_km, start, cobs, clat, clon,
+                   [&](int32_t o, double, int cls, double, double) {
+                     if (cls == 0 && nrej > 0 &&
+                         key_rejected(rej, nrej, ((unsigned long long)col << 32) | (unsigned)o))
+                       return;
+                     const int pos = atomicAdd(&scount, 1);
+                     if (pos < kMaxList) slist[pos] = o;
+                   });
+  __syncthreads();
+  const int cnt = scount;
+  if (cnt != (int)n) {  // count and fill passes disagree: report, write nothing
+    if (threadIdx.x == 0) atomicExch(overflow, 2);
+    return;
+  }
+  int m = 1;
+  while (m < cnt) m <<= 1;
+  for (int t = cnt + threadIdx.x; t < m; t += blockDim.x) slist[t] = 0x7fffffff;
+  __syncthreads();
+  // Bitonic sort by obs index (obs order, as LETKF.hpp:160-165).
+  for (int size = 2; size <= m; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < (m >> 1); t += blockDim.x) {
+        const int lo_i = 2 * t - (t & (stride - 1));
+        const int hi_i = lo_i + stride;
+        const bool up = ((lo_i & size) == 0);
+        const int a = slist[lo_i], b = slist[hi_i];
+        if ((a > b) == up) {
+          slist[lo_i] = b;
+          slist[hi_i] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int o = slist[t];
+    idx[base + t] = o;
+    if (dist) dist[base + t] = haversine_dev(la, lo, obs_lat[o], obs_lon[o]);
+  }
+}
+
+// Host-side reference predicate for near-threshold pairs (Location.hpp:349-357).
+double haversine_host(double lat1, double lon1, double lat2, double lon2) {
+  auto deg2rad = [](double deg) { return deg * kPi / 180.0; };
+  const double dlat = deg2rad(lat2 - lat1);
+  const double dlon = deg2rad(lon2 - lon1);
+  const double a = std::sin(dlat / 2) * std::sin(dlat / 2) +
+                   std::cos(deg2rad(lat1)) * std::cos(deg2rad(lat2)) * std::sin(dlon / 2) *
+                       std::sin(dlon / 2);
+  const double c = 2 * std::atan2(std::sqrt(a), std::sqrt(1 - a));
+  return kEarthKm * c;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mg_select_grid(mg_context* ctx, int32_t nx, int32_t ny, const int32_t* obs_xy, int64_t p,
+                   double radius, int64_t* offsets, int32_t* idx, int64_t cap, int64_t* total) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(nx > 0 && ny > 0 && p >= 0 && offsets && total && (p == 0 || obs_xy),
+               "mg_select_grid: bad arguments");
+  const int64_t npt = (int64_t)nx * ny;
+  const size_t tmpb = mg::scan_temp_bytes(npt);
+  mg::Carver cv;
+  cv.reserve<int64_t>(npt + 1);
+  cv.reserve<char>(tmpb);
+  void* ws = mg::workspace(ctx, cv.off);
+  if (!ws) return MG_ERR_NOMEM;
+  cv = mg::Carver{static_cast<char*>(ws), 0};
+  int64_t* counts = cv.take<int64_t>(npt + 1);
+  void* tmp = cv.take<char>(tmpb);
+  const unsigned blocks = (unsigned)((npt + 7) / 8);
+  MG_TRY_CUDA(cudaMemsetAsync(counts, 0, sizeof(int64_t) * (npt + 1), ctx->stream));
+  select_grid_kernel<<<blocks, 256, 0, ctx->stream>>>(nx, ny, obs_xy, p, radius, nullptr, counts,
+                                                      nullptr);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  MG_TRY_CUDA(mg::exclusive_scan(counts, offsets, npt, tmp, tmpb, ctx->stream));
+  MG_TRY_CUDA(cudaMemcpyAsync(total, offsets + npt, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+  MG_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (*total > cap || (*total > 0 && !idx))
+    return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_grid: index buffer too small");
+  if (*total > 0) {
+    select_grid_kernel<<<blocks, 256, 0, ctx->stream>>>(nx, ny, obs_xy, p, radius, offsets, nullptr,
+                                                        idx);
+    MG_COUNT_LAUNCH();
+    MG_TRY_CUDA(cudaGetLastError());
+  }
+  return MG_OK;
+}
+
+int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon, int64_t ncol,
+                  const double* obs_lat, const double* obs_lon, int64_t p, double radius_km,
+                  int64_t* offsets, int32_t* idx, double* dist_km, int64_t cap, int64_t* total) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(col_lat && col_lon && ncol > 0 && p >= 0 && offsets && total && radius_km >= 0 &&
+                   (p == 0 || (obs_lat && obs_lon)),
+               "mg_select_geo: bad arguments");
+  MG_CHECK_ARG(radius_km < 0.5 * kPi * kEarthKm, "mg_select_geo: radius must be below a quarter great circle");
+  const size_t tmp_cells = mg::scan_temp_bytes(kNCell);
+  const size_t tmp_cols = mg::scan_temp_bytes(ncol);
+  const size_t tmpb = std::max(tmp_cells, tmp_cols);
+  mg::Carver cv;
+  cv.reserve<unsigned long long>(kNCell + 1);  // cell counts, then cursor
+  cv.reserve<unsigned long long>(kNCell + 1);
+  cv.reserve<int64_t>(kNCell + 1);             // cell start
+  cv.reserve<int32_t>(p + 1);
+  cv.reserve<double>(p + 1);
+  cv.reserve<double>(p + 1);
+  cv.reserve<int64_t>(ncol + 1);               // column counts
+  cv.reserve<BorderRec>(kBorderCap);
+  cv.reserve<unsigned long long>(kBorderCap);  // rejected keys
+  cv.reserve<unsigned long long>(2);           // n_border
+  cv.reserve<int>(2);                          // overflow flag
+  cv.reserve<char>(tmpb);
+  void* ws = mg::workspace(ctx, cv.off);
+  if (!ws) return MG_ERR_NOMEM;
+  cv = mg::Carver{static_cast<char*>(ws), 0};
+  auto* ccount = cv.take<unsigned long long>(kNCell + 1);
+  auto* ccursor = cv.take<unsigned long long>(kNCell + 1);
+  auto* cstart = cv.take<int64_t>(kNCell + 1);
+  auto* cobs = cv.take<int32_t>(p + 1);
+  auto* clat = cv.take<double>(p + 1);
+  auto* clon = cv.take<double>(p + 1);
+  auto* counts = cv.take<int64_t>(ncol + 1);
+  auto* border = cv.take<BorderRec>(kBorderCap);
+  auto* rej = cv.take<unsigned long long>(kBorderCap);
+  auto* nborder = cv.take<unsigned long long>(2);
+  auto* overflow = cv.take<int>(2);
+  void* tmp = cv.take<char>(tmpb);
+  cudaStream_t s = ctx->stream;
+
+  // Spatial hash: counting sort of obs into cells.
+  MG_TRY_CUDA(cudaMemsetAsync(ccount, 0, sizeof(unsigned long long) * (kNCell + 1), s));
+  MG_TRY_CUDA(cudaMemsetAsync(ccursor, 0, sizeof(unsigned long long) * (kNCell + 1), s));
+  MG_TRY_CUDA(cudaMemsetAsync(nborder, 0, sizeof(unsigned long long) * 2, s));
+  MG_TRY_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int) * 2, s));
+  MG_TRY_CUDA(cudaMemsetAsync(counts, 0, sizeof(int64_t) * (ncol + 1), s));
+  if (p > 0) {
+    const unsigned gb = (unsigned)std::min<int64_t>((p + 255) / 256, 152 * 16);
+    cell_count_kernel<<<gb, 256, 0, s>>>(obs_lat, obs_lon, p, ccount);
+    MG_COUNT_LAUNCH();
+    MG_TRY_CUDA(cudaGetLastError());
+    MG_TRY_CUDA(mg::exclusive_scan(reinterpret_cast<const int64_t*>(ccount), cstart, kNCell, tmp,
+                                   tmpb, s));
+    cell_scatter_kernel<<<gb, 256, 0, s>>>(obs_lat, obs_lon, p, cstart, ccursor, cobs, clat, clon);
+    MG_COUNT_LAUNCH();
+    MG_TRY_CUDA(cudaGetLastError());
+  } else {
+    MG_TRY_CUDA(cudaMemsetAsync(cstart, 0, sizeof(int64_t) * (kNCell + 1), s));
+  }
+  // Pass 1: counts (near-threshold pairs counted and recorded).
+  geo_count_kernel<<<(unsigned)ncol, 256, 0, s>>>(col_lat, col_lon, ncol, radius_km, cstart, cobs,
+                                                  clat, clon, counts, border, nborder);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  unsigned long long nb = 0;
+  MG_TRY_CUDA(cudaMemcpyAsync(&nb, nborder, sizeof(nb), cudaMemcpyDeviceToHost, s));
+  MG_TRY_CUDA(cudaStreamSynchronize(s));
+  if (nb > (unsigned long long)kBorderCap)
+    return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_geo: too many near-threshold pairs");
+  int nrej = 0;
+  if (nb > 0) {
+    std::vector<BorderRec> recs(nb);
+    MG_TRY_CUDA(cudaMemcpy(recs.data(), border, sizeof(BorderRec) * nb, cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> keys;
+    for (const auto& r : recs)
+      if (!(haversine_host(r.clat, r.clon, r.olat, r.olon) <= radius_km))
+        keys.push_back(((unsigned long long)r.col << 32) | (unsigned long long)(uint32_t)r.obs);
+    std::sort(keys.begin(), keys.end());
+    nrej = (int)keys.size();
+    if (nrej > 0) {
+      MG_TRY_CUDA(cudaMemcpy(rej, keys.data(), sizeof(unsigned long long) * nrej,
+                             cudaMemcpyHostToDevice));
+      apply_rejections_kernel<<<(nrej + 255) / 256, 256, 0, s>>>(rej, nrej, counts);
+      MG_COUNT_LAUNCH();
+      MG_TRY_CUDA(cudaGetLastError());
+    }
+  }
+  MG_TRY_CUDA(mg::exclusive_scan(counts, offsets, ncol, tmp, tmpb, s));
+  MG_TRY_CUDA(cudaMemcpyAsync(total, offsets + ncol, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MG_TRY_CUDA(cudaStreamSynchronize(s));
+  if (*total > cap || (*total > 0 && !idx))
+    return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_geo: index buffer too small");
+  if (*total == 0) return MG_OK;
+  // Pass 2: fill, sort each list by obs index, distances.
+  int smem_entries = 1;
+  while (smem_entries < kMaxList) smem_entries <<= 1;
+  const size_t smem = sizeof(int32_t) * smem_entries;
+  MG_TRY_CUDA(cudaFuncSetAttribute(geo_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  geo_fill_kernel<<<(unsigned)ncol, 256, smem, s>>>(col_lat, col_lon, ncol, radius_km, cstart, cobs,
+                                                    clat, clon, offsets, rej, nrej, obs_lat,
+                                                    obs_lon, idx, dist_km, overflow);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  int ovf = 0;
+  MG_TRY_CUDA(cudaMemcpyAsync(&ovf, overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MG_TRY_CUDA(cudaStreamSynchronize(s));
+  if (ovf == 1) return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_geo: a local list exceeds 16384 obs");
+  if (ovf == 2) return mg::fail(ctx, MG_ERR_NUMERIC, "mg_select_geo: count and fill passes disagree");
+  return MG_OK;
+}
+
+}  // extern "C"

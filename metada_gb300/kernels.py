@@ -1,0 +1,195 @@
+"""Thin tensor-level wrappers over the C-ABI.
+
+Every function takes CUDA tensors (torch is used only for device memory and
+streams), checks shapes/dtypes, and calls the corresponding ``mg_*`` entry
+point on the current torch stream.  Nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_int64, c_void_p
+
+import torch
+
+from . import _lib
+from ._lib import Context, LetkfDesc, LetkfStats
+
+_contexts: dict[int, Context] = {}
+
+
+def context(device: int | None = None) -> Context:
+    """Per-device context bound to torch's current stream."""
+    if device is None:
+        device = torch.cuda.current_device()
+    ctx = _contexts.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        _contexts[device] = ctx
+    ctx.set_stream(torch.cuda.current_stream(device).cuda_stream)
+    return ctx
+
+
+def _ptr(t: torch.Tensor | None) -> c_void_p:
+    if t is None:
+        return c_void_p(0)
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return c_void_p(t.data_ptr())
+
+
+def _need(t: torch.Tensor, dtype: torch.dtype, name: str) -> None:
+    if t.dtype != dtype:
+        raise TypeError(f"{name}: expected {dtype}, got {t.dtype}")
+
+
+def ens_mean(X: torch.Tensor) -> torch.Tensor:
+    """Ensemble mean of members X (k x n, float64), member-order sum * (1/k)."""
+    _need(X, torch.float64, "X")
+    k, n = X.shape
+    mean = torch.empty(n, dtype=torch.float64, device=X.device)
+    context(X.device.index).call("mg_ens_mean", _ptr(X), n, k, n, _ptr(mean))
+    return mean
+
+
+def ens_mean_pert(X: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+    _need(X, torch.float64, "X")
+    k, n = X.shape
+    mean = torch.empty(n, dtype=torch.float64, device=X.device)
+    Xp = torch.empty_like(X)
+    context(X.device.index).call("mg_ens_mean_pert", _ptr(X), n, k, n, _ptr(mean), _ptr(Xp), n)
+    return mean, Xp
+
+
+def hx_idw4(X: torch.Tensor, nx: int, ny: int, obs_xy: torch.Tensor,
+            valid: torch.Tensor | None = None) -> torch.Tensor:
+    """IDW4 obs operator for grid obs; returns HX (p x k)."""
+    _need(X, torch.float64, "X")
+    _need(obs_xy, torch.int32, "obs_xy")
+    k, n = X.shape
+    p = obs_xy.shape[0]
+    HX = torch.empty((p, k), dtype=torch.float64, device=X.device)
+    if valid is not None:
+        _need(valid, torch.uint8, "valid")
+    context(X.device.index).call("mg_hx_idw4", _ptr(X), k, n, nx, ny, _ptr(obs_xy), _ptr(valid), p, _ptr(HX))
+    return HX
+
+
+def hx_latlon(X: torch.Tensor, nlon: int, nlat: int, nlev: int, obs_lat: torch.Tensor,
+              obs_lon: torch.Tensor, obs_lev: torch.Tensor, obs_var: torch.Tensor) -> torch.Tensor:
+    _need(X, torch.float64, "X")
+    _need(obs_var, torch.int32, "obs_var")
+    k, n = X.shape
+    p = obs_lat.shape[0]
+    HX = torch.empty((p, k), dtype=torch.float64, device=X.device)
+    context(X.device.index).call("mg_hx_latlon", _ptr(X), k, n, nlon, nlat, nlev, _ptr(obs_lat),
+                                 _ptr(obs_lon), _ptr(obs_lev), _ptr(obs_var), p, _ptr(HX))
+    return HX
+
+
+def select_grid(nx: int, ny: int, obs_xy: torch.Tensor, radius: float) -> tuple[torch.Tensor, torch.Tensor]:
+    """Local obs lists for every grid point (CSR: offsets, idx)."""
+    _need(obs_xy, torch.int32, "obs_xy")
+    dev = obs_xy.device
+    ctx = context(dev.index)
+    p = obs_xy.shape[0]
+    offsets = torch.empty(nx * ny + 1, dtype=torch.int64, device=dev)
+    total = c_int64(0)
+    rc = ctx.lib.mg_select_grid(ctx.handle, nx, ny, _ptr(obs_xy), p, float(radius), _ptr(offsets), c_void_p(0),
+                                0, byref(total))
+    if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
+        ctx.check(rc)
+    idx = torch.empty(max(total.value, 1), dtype=torch.int32, device=dev)
+    ctx.call("mg_select_grid", nx, ny, _ptr(obs_xy), p, float(radius), _ptr(offsets), _ptr(idx), idx.numel(),
+             byref(total))
+    return offsets, idx[: total.value]
+
+
+def select_geo(col_lat: torch.Tensor, col_lon: torch.Tensor, obs_lat: torch.Tensor, obs_lon: torch.Tensor,
+               radius_km: float, cap: int | None = None) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+    """Local obs lists for every query column (haversine <= radius_km)."""
+    for t, nm in ((col_lat, "col_lat"), (col_lon, "col_lon"), (obs_lat, "obs_lat"), (obs_lon, "obs_lon")):
+        _need(t, torch.float64, nm)
+    dev = col_lat.device
+    ctx = context(dev.index)
+    ncol = col_lat.shape[0]
+    p = obs_lat.shape[0]
+    offsets = torch.empty(ncol + 1, dtype=torch.int64, device=dev)
+    total = c_int64(0)
+    if cap is None:
+        rc = ctx.lib.mg_select_geo(ctx.handle, _ptr(col_lat), _ptr(col_lon), ncol, _ptr(obs_lat), _ptr(obs_lon),
+                                   p, float(radius_km), _ptr(offsets), c_void_p(0), c_void_p(0), 0, byref(total))
+        if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
+            ctx.check(rc)
+        cap = total.value
+    idx = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+    dist = torch.empty(max(cap, 1), dtype=torch.float64, device=dev)
+    ctx.call("mg_select_geo", _ptr(col_lat), _ptr(col_lon), ncol, _ptr(obs_lat), _ptr(obs_lon), p,
+             float(radius_km), _ptr(offsets), _ptr(idx), _ptr(dist), idx.numel(), byref(total))
+    return offsets, idx[: total.value], dist[: total.value]
+
+
+def etkf(X: torch.Tensor, HX: torch.Tensor, yo: torch.Tensor, rvar: torch.Tensor, rho: float,
+         flags: int = _lib.MG_COMPAT, precision: int = _lib.MG_PREC_FP64) -> torch.Tensor:
+    """Global ETKF in place on X (k x n); returns the background mean."""
+    _need(X, torch.float64, "X")
+    k, n = X.shape
+    p = HX.shape[0]
+    mean = torch.empty(n, dtype=torch.float64, device=X.device)
+    context(X.device.index).call("mg_etkf", _ptr(X), n, k, n, _ptr(HX), _ptr(yo), _ptr(rvar), p, float(rho),
+                                 int(flags), int(precision), _ptr(mean))
+    return mean
+
+
+def letkf_compat_grid(X: torch.Tensor, nx: int, ny: int, obs_xy: torch.Tensor, yo: torch.Tensor,
+                      radius: float, rho: float, valid: torch.Tensor | None = None) -> torch.Tensor:
+    """Reference-order LETKF in place on X; returns the recomputed mean."""
+    _need(X, torch.float64, "X")
+    k, n = X.shape
+    mean = torch.empty(n, dtype=torch.float64, device=X.device)
+    context(X.device.index).call("mg_letkf_compat_grid", _ptr(X), k, n, nx, ny, _ptr(obs_xy), _ptr(valid),
+                                 _ptr(yo), obs_xy.shape[0], float(radius), float(rho), _ptr(mean))
+    return mean
+
+
+def letkf_batched(X: torch.Tensor, *, col_base: torch.Tensor, nlev: int, n_var: int, lev_stride: int,
+                  var_stride: int, HX: torch.Tensor, yo: torch.Tensor, rvar: torch.Tensor,
+                  loc_off: torch.Tensor, loc_idx: torch.Tensor, loc_dist: torch.Tensor | None = None,
+                  obs_lev: torch.Tensor | None = None, hsupport: float = 0.0, vsupport: float = 0.0,
+                  rho: float = 1.0, flags: int = 0, precision: int = _lib.MG_PREC_FP64,
+                  want_mean: bool = True) -> tuple[torch.Tensor | None, LetkfStats]:
+    """Batched LETKF in place on X (k x n)."""
+    _need(X, torch.float64, "X")
+    k, n = X.shape
+    mean = torch.empty(n, dtype=torch.float64, device=X.device) if want_mean else None
+    d = LetkfDesc()
+    d.X = X.data_ptr()
+    d.n = n
+    d.ld = n
+    d.k = k
+    d.n_var = n_var
+    d.nlev = nlev
+    d.precision = precision
+    d.ncol = col_base.shape[0]
+    d.col_base = _ptr(col_base).value
+    d.lev_stride = lev_stride
+    d.var_stride = var_stride
+    d.p = HX.shape[0]
+    d.HX = _ptr(HX).value
+    d.yo = _ptr(yo).value
+    d.rvar = _ptr(rvar).value
+    d.obs_lev = _ptr(obs_lev).value
+    d.loc_off = _ptr(loc_off).value
+    d.loc_idx = _ptr(loc_idx).value if loc_idx.numel() else None
+    d.loc_dist = _ptr(loc_dist).value if (loc_dist is not None and loc_dist.numel()) else None
+    d.hsupport = hsupport
+    d.vsupport = vsupport
+    d.rho = rho
+    d.flags = flags
+    d.mean_out = _ptr(mean).value
+    ctx = context(X.device.index)
+    ctx.call("mg_letkf_batched", ctypes.byref(d))
+    st = LetkfStats()
+    ctx.call("mg_letkf_last_stats", ctypes.byref(st))
+    return mean, st

@@ -1,0 +1,215 @@
+// Reference harness: runs the reference's OWN analysis headers
+// (src/framework/algorithms/ETKF.hpp, LETKF.hpp over the Simple backend,
+// GridObservation and IdentityObsOperator) unmodified, to pin the oracle.
+//
+// TEST INFRASTRUCTURE ONLY.  Built by oracle/build_ref.sh from the reference
+// tree in place (nothing of it is copied here), against the Eigen subset in
+// oracle/eigen_subset and a map-backed configuration backend written here
+// (the reference's YAML backend needs yaml-cpp, which is not installed).
+// Output goes to oracle/_ref/ and is never shipped.
+//
+// usage: ref_harness etkf|letkf NX NY K ENS_PREFIX OBS_FILE ERROR INFLATION
+//                    RADIUS OUT_DIR
+//   reads ENS_PREFIX<i>.txt (i = 1..K, SimpleState text) and OBS_FILE
+//   (GridObservation text format, grid coordinates); writes the analysed
+//   members as raw little-endian doubles to OUT_DIR/member_<i>.bin
+//   (i = 0..K-1) and Ensemble::Mean() to OUT_DIR/mean.bin.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "ConfigValue.hpp"
+
+namespace harness {
+
+namespace fw = metada::framework;
+
+// Configuration backend over an in-memory ConfigMap (dotted keys allowed).
+class MapConfig {
+ public:
+  MapConfig() = delete;
+  MapConfig(const MapConfig&) = delete;
+  MapConfig& operator=(const MapConfig&) = delete;
+  MapConfig(MapConfig&&) noexcept = default;
+  MapConfig& operator=(MapConfig&&) noexcept = default;
+  ~MapConfig() = default;
+
+  explicit MapConfig(const std::string& filename) {
+    throw std::runtime_error("MapConfig cannot load files: " + filename);
+  }
+  explicit MapConfig(const fw::ConfigMap& map) : root_(map) {}
+
+  bool LoadFromFile(const std::string&) { return false; }
+  bool LoadFromString(const std::string&) { return false; }
+
+  fw::ConfigValue Get(const std::string& key) const {
+    fw::ConfigValue cur(root_);
+    std::stringstream ss(key);
+    std::string part;
+    while (std::getline(ss, part, '.')) {
+      if (!cur.hasKey(part)) throw std::runtime_error("missing config key: " + key);
+      cur = cur.get(part);
+    }
+    return cur;
+  }
+  void Set(const std::string& key, const fw::ConfigValue& value) { root_[key] = value; }
+  bool HasKey(const std::string& key) const {
+    try {
+      Get(key);
+      return true;
+    } catch (...) {
+      return false;
+    }
+  }
+  bool SaveToFile(const std::string&) const { return false; }
+  std::string ToString() const { return "MapConfig"; }
+  void Clear() { root_.clear(); }
+  MapConfig CreateSubsection(const std::string& key) const { return MapConfig(Get(key).asMap()); }
+
+ private:
+  fw::ConfigMap root_;
+};
+
+}  // namespace harness
+
+#include "BackendTraits.hpp"
+#include "ConsoleLogger.hpp"
+#include "GridObservation.hpp"
+#include "IdentityObsOperator.hpp"
+#include "SimpleBackgroundErrorCovariance.hpp"
+#include "SimpleGeometry.hpp"
+#include "SimpleGeometryIterator.hpp"
+#include "SimpleIncrement.hpp"
+#include "SimpleModel.hpp"
+#include "SimpleState.hpp"
+
+namespace harness {
+struct HarnessBackendTag {};
+}  // namespace harness
+
+namespace metada::traits {
+template <>
+struct BackendTraits<harness::HarnessBackendTag> {
+  using ConfigBackend = harness::MapConfig;
+  using LoggerBackend = backends::logger::ConsoleLogger<ConfigBackend>;
+  using GeometryBackend = backends::simple::SimpleGeometry;
+  using GeometryIteratorBackend =
+      backends::simple::SimpleGeometryIterator<typename GeometryBackend::const_iterator>;
+  using StateBackend = backends::simple::SimpleState;
+  using IncrementBackend = backends::simple::SimpleIncrement;
+  using ControlVariableBackend = backends::simple::SimpleIncrement;
+  using ObservationBackend = backends::common::observation::GridObservation;
+  using ObservationIteratorBackend = backends::common::observation::GridObservationIterator;
+  using ObsOperatorBackend =
+      backends::common::obsoperator::IdentityObsOperator<StateBackend, ObservationBackend,
+                                                         ControlVariableBackend>;
+  using ModelBackend = backends::simple::SimpleModel;
+  using BackgroundErrorCovarianceBackend = backends::simple::SimpleBackgroundErrorCovariance;
+};
+}  // namespace metada::traits
+
+#include "Config.hpp"
+#include "ETKF.hpp"
+#include "Ensemble.hpp"
+#include "Geometry.hpp"
+#include "IdentityControlVariableBackend.hpp"
+#include "LETKF.hpp"
+#include "Logger.hpp"
+#include "ObsOperator.hpp"
+#include "Observation.hpp"
+
+namespace fw = metada::framework;
+using Tag = harness::HarnessBackendTag;
+
+static void dump(const std::string& path, const double* p, size_t n) {
+  std::ofstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("cannot write " + path);
+  f.write(reinterpret_cast<const char*>(p), (std::streamsize)(n * sizeof(double)));
+}
+
+int main(int argc, char** argv) {
+  try {
+    if (argc != 11) {
+      std::cerr << "usage: ref_harness etkf|letkf NX NY K ENS_PREFIX OBS_FILE ERROR INFLATION "
+                   "RADIUS OUT_DIR\n";
+      return 2;
+    }
+    const std::string algo = argv[1];
+    const int nx = std::atoi(argv[2]), ny = std::atoi(argv[3]), k = std::atoi(argv[4]);
+    const std::string ens_prefix = argv[5], obs_file = argv[6];
+    const float error = std::strtof(argv[7], nullptr);
+    const float inflation = std::strtof(argv[8], nullptr);
+    const float radius = std::strtof(argv[9], nullptr);
+    const std::string out = argv[10];
+
+    fw::ConfigMap logger_cfg{{"app_name", fw::ConfigValue("ref_harness")},
+                             {"level", fw::ConfigValue("error")},
+                             {"color", fw::ConfigValue(false)},
+                             {"show_timestamp", fw::ConfigValue(false)},
+                             {"console", fw::ConfigValue(true)}};
+    std::vector<fw::ConfigValue> members;
+    for (int i = 1; i <= k; ++i) {
+      fw::ConfigMap st{{"variables", fw::ConfigValue("simple")},
+                       {"file", fw::ConfigValue(ens_prefix + std::to_string(i) + ".txt")}};
+      members.emplace_back(fw::ConfigMap{{"state", fw::ConfigValue(st)}});
+    }
+    fw::ConfigMap var_cfg{{"if_use", fw::ConfigValue(true)},
+                          {"error", fw::ConfigValue(error)},
+                          {"missing_value", fw::ConfigValue(-999.0f)}};
+    std::vector<fw::ConfigValue> vars{fw::ConfigValue(fw::ConfigMap{{"simple", var_cfg}})};
+    fw::ConfigMap type_cfg{{"if_use", fw::ConfigValue(true)},
+                           {"file", fw::ConfigValue(obs_file)},
+                           {"coordinate", fw::ConfigValue("grid")},
+                           {"variables", fw::ConfigValue(vars)}};
+    std::vector<fw::ConfigValue> types{fw::ConfigValue(fw::ConfigMap{{"obs_A", type_cfg}})};
+    fw::ConfigMap analysis{{"algorithm", fw::ConfigValue(algo)},
+                           {"inflation", fw::ConfigValue(inflation)},
+                           {"localization_radius", fw::ConfigValue(radius)},
+                           {"format", fw::ConfigValue("txt")},
+                           {"output_base_file", fw::ConfigValue(out + "/analysis")}};
+    fw::ConfigMap root{
+        {"logger", fw::ConfigValue(logger_cfg)},
+        {"geometry",
+         fw::ConfigValue(fw::ConfigMap{{"x_dim", fw::ConfigValue(nx)}, {"y_dim", fw::ConfigValue(ny)}})},
+        {"ensemble", fw::ConfigValue(fw::ConfigMap{{"members", fw::ConfigValue(members)}})},
+        {"observations", fw::ConfigValue(fw::ConfigMap{{"types", fw::ConfigValue(types)}})},
+        {"obs_operator", fw::ConfigValue(fw::ConfigMap{})},
+        {"analysis", fw::ConfigValue(analysis)}};
+
+    fw::Config<Tag> config(root);
+    fw::Config<Tag> log_config(logger_cfg);
+    fw::Logger<Tag>::Init(log_config);
+
+    fw::Geometry<Tag> geometry(config.GetSubsection("geometry"));
+    fw::Config<Tag> ens_cfg = config.GetSubsection("ensemble");
+    fw::Ensemble<Tag> ensemble(ens_cfg, geometry);
+    fw::Observation<Tag> observations(config.GetSubsection("observations"));
+    auto control = std::make_shared<fw::IdentityControlVariableBackend<Tag>>();
+    fw::ObsOperator<Tag> obs_operator(config.GetSubsection("obs_operator"), *control);
+
+    if (algo == "etkf") {
+      fw::ETKF<Tag> etkf(ensemble, observations, obs_operator, config.GetSubsection("analysis"));
+      etkf.Analyse();
+    } else if (algo == "letkf") {
+      fw::LETKF<Tag> letkf(ensemble, observations, obs_operator, config.GetSubsection("analysis"));
+      letkf.Analyse();
+    } else {
+      throw std::runtime_error("unknown algorithm " + algo);
+    }
+    const size_t n = ensemble.GetMember(0).size();
+    for (int i = 0; i < k; ++i)
+      dump(out + "/member_" + std::to_string(i) + ".bin",
+           ensemble.GetMember(i).template getDataPtr<double>(), n);
+    dump(out + "/mean.bin", ensemble.Mean().template getDataPtr<double>(), n);
+    return 0;
+  } catch (const std::exception& e) {
+    std::cerr << "ref_harness failed: " << e.what() << std::endl;
+    return 1;
+  }
+}

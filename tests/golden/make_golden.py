@@ -1,0 +1,145 @@
+"""Generates the golden fixtures in this directory by running the reference's
+own analysis headers (oracle/_ref/ref_harness, built by oracle/build_ref.sh
+from the reference tree) on:
+
+  * the reference tutorial data (src/backends/simple/tutorial: 9 members on
+    a 36 x 18 grid, 28 grid observations, error 0.1), ETKF and LETKF
+    (radius 10) with inflation 1.0 as in etkf.yaml / letkf.yaml, and the
+    LETKF again with inflation 1.1;
+  * the seeded 64 x 64, 32-member, 1024-observation global ETKF case
+    (inflation 1.05, error 0.5);
+  * two seeded small-grid LETKF cases (some grid points without local
+    observations).
+
+Run from the repository root, in a checkout that has the reference tree:
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+The fixtures are small .npz files holding inputs and reference outputs.
+"""
+from __future__ import annotations
+
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from metada_gb300 import synthetic as syn  # noqa: E402
+from metada_gb300.build import build_reference_harness  # noqa: E402
+
+HARNESS = ROOT / "oracle" / "_ref" / "ref_harness"
+
+
+def read_simple_state(path: Path) -> np.ndarray:
+    return np.array([float(v) for v in path.read_text().split()], dtype=np.float64)
+
+
+def read_grid_obs(path: Path, missing: float = -999.0):
+    """Parses the GridObservation text format (GridObservation.hpp:416-469)."""
+    xy, vals = [], []
+    header = started = False
+    for line in path.read_text().splitlines():
+        if not line:
+            continue
+        if "Time" in line and "XLONG_U" in line:
+            header = True
+            continue
+        if "---" in line and not line.strip("- \t"):
+            if header:
+                started = True
+            continue
+        if not started:
+            continue
+        parts = line.split()
+        if len(parts) < 8:
+            continue
+        x, y = int(parts[3]), int(parts[2])
+        v = float(parts[7])
+        if v != missing:
+            xy.append((x, y))
+            vals.append(v)
+    return np.array(xy, dtype=np.int32), np.array(vals, dtype=np.float64)
+
+
+def run_harness(algo: str, nx: int, ny: int, k: int, ens_prefix: str, obs_file: str, error: float,
+                rho: float, radius: float, out: Path) -> tuple[np.ndarray, np.ndarray]:
+    out.mkdir(parents=True, exist_ok=True)
+    cmd = [str(HARNESS), algo, str(nx), str(ny), str(k), ens_prefix, obs_file, repr(error), repr(rho),
+           repr(radius), str(out)]
+    subprocess.run(cmd, check=True)
+    n = nx * ny
+    members = np.stack([np.fromfile(out / f"member_{i}.bin", dtype="<f8", count=n) for i in range(k)])
+    mean = np.fromfile(out / "mean.bin", dtype="<f8", count=n)
+    return members, mean
+
+
+def grid_case_to_files(case: syn.GridCase, tmp: Path) -> tuple[str, str]:
+    k = case.X.shape[0]
+    for i in range(k):
+        syn.write_simple_state(tmp / f"ens_{i + 1}.txt", case.X[i], case.nx, case.ny)
+    syn.write_grid_obs(tmp / "obs.txt", case.obs_xy, case.yo)
+    return str(tmp / "ens_"), str(tmp / "obs.txt")
+
+
+def main(ref_root: str | None = None) -> None:
+    import os
+
+    if ref_root:
+        os.environ["METADA_REFERENCE"] = ref_root
+    if build_reference_harness() is None:
+        raise SystemExit("reference tree not found; cannot regenerate the golden fixtures")
+    ref = Path(os.environ.get("METADA_REFERENCE", "/root/reference"))
+    tut = ref / "src" / "backends" / "simple" / "tutorial"
+    with tempfile.TemporaryDirectory() as td:
+        tmp = Path(td)
+        # --- tutorial ---
+        nx, ny, k = 36, 18, 9
+        X = np.stack([read_simple_state(tut / f"ens_{i}.txt") for i in range(1, k + 1)])
+        obs_xy, yo = read_grid_obs(tut / "obs_format.txt")
+        sigma = syn.float_config(0.1)
+        outs = {}
+        for name, algo, rho, radius in (("etkf", "etkf", 1.0, 0.0), ("letkf", "letkf", 1.0, 10.0),
+                                        ("letkf_rho11", "letkf", 1.1, 10.0)):
+            m, mu = run_harness(algo, nx, ny, k, str(tut / "ens_"), str(tut / "obs_format.txt"), 0.1, rho,
+                                radius, tmp / name)
+            outs[f"{name}_members"] = m
+            outs[f"{name}_mean"] = mu
+        np.savez_compressed(HERE / "tutorial.npz", X=X, obs_xy=obs_xy, yo=yo, sigma=sigma, nx=nx, ny=ny,
+                            radius=syn.float_config(10.0), rho=1.0, rho11=syn.float_config(1.1), **outs)
+        print("tutorial.npz", {k2: v.shape for k2, v in outs.items()})
+
+        # --- seeded 64 x 64 global ETKF ---
+        c = syn.global_etkf_grid()
+        d = tmp / "c1"
+        d.mkdir()
+        ens, obsf = grid_case_to_files(c, d)
+        m, mu = run_harness("etkf", c.nx, c.ny, c.X.shape[0], ens, obsf, 0.5, 1.05, 0.0, d / "out")
+        # inputs are re-read from text by the harness: store exactly what it read
+        Xr = np.stack([read_simple_state(d / f"ens_{i + 1}.txt") for i in range(c.X.shape[0])])
+        _, yor = read_grid_obs(Path(obsf))
+        np.savez_compressed(HERE / "etkf_grid64.npz", X=Xr, obs_xy=c.obs_xy, yo=yor, sigma=c.sigma_o,
+                            rho=c.rho, nx=c.nx, ny=c.ny, members=m, mean=mu)
+        print("etkf_grid64.npz", m.shape)
+
+        # --- seeded small LETKF grids ---
+        for name, args in (("letkf_grid24", dict(nx=24, ny=16, k=8, p=60, radius=5.0, rho=1.05, case=11)),
+                           ("letkf_grid20", dict(nx=20, ny=12, k=12, p=30, radius=3.0, rho=1.2, case=12))):
+            c = syn.grid_letkf_case(**args)
+            d = tmp / name
+            d.mkdir()
+            ens, obsf = grid_case_to_files(c, d)
+            m, mu = run_harness("letkf", c.nx, c.ny, c.X.shape[0], ens, obsf, 0.5, args["rho"], args["radius"],
+                                d / "out")
+            Xr = np.stack([read_simple_state(d / f"ens_{i + 1}.txt") for i in range(c.X.shape[0])])
+            _, yor = read_grid_obs(Path(obsf))
+            np.savez_compressed(HERE / f"{name}.npz", X=Xr, obs_xy=c.obs_xy, yo=yor, sigma=c.sigma_o, rho=c.rho,
+                                radius=c.radius, nx=c.nx, ny=c.ny, members=m, mean=mu)
+            print(f"{name}.npz", m.shape)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

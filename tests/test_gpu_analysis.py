@@ -1,0 +1,185 @@
+"""GPU parity of the analyses: global ETKF and LETKF (reference order and
+batched), FP64 against the reference golden vectors and the oracle at
+1e-10 relative, mixed precision at 1e-5 relative."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN, rel_err
+from helpers import point_lists
+
+import oracle.bind as ob
+from metada_gb300 import _lib
+from metada_gb300 import kernels as K
+from metada_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+MIXED_TOL = 1e-5
+
+
+def T(a, dev):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+# ------------------------------------------------------------ global ETKF --
+@pytest.mark.parametrize("name", ["tutorial", "etkf_grid64"])
+def test_etkf_reference_semantics_match_golden(dev, name):
+    g = np.load(GOLDEN / f"{name}.npz")
+    if name == "tutorial":
+        X, nx, ny, want, wmean, rho = g["X"], int(g["nx"]), int(g["ny"]), g["etkf_members"], g["etkf_mean"], 1.0
+    else:
+        X, nx, ny, want, wmean, rho = g["X"], 64, 64, g["members"], g["mean"], float(g["rho"])
+    s = float(g["sigma"])
+    Xd = T(X, dev)
+    HX = K.hx_idw4(Xd, nx, ny, T(g["obs_xy"], dev))
+    yo = T(g["yo"], dev)
+    mean = K.etkf(Xd, HX, yo, torch.full_like(yo, s * s), rho, flags=_lib.MG_COMPAT, precision=_lib.MG_PREC_FP64)
+    assert rel_err(Xd.cpu().numpy(), want) <= FP64_TOL
+    assert np.array_equal(mean.cpu().numpy(), wmean)
+
+
+def _global_oracle_hunt(X, HX, yo, rvar, rho, pts):
+    p = HX.shape[0]
+    npt = len(pts)
+    off = np.arange(npt + 1, dtype=np.int64) * p
+    idx = np.tile(np.arange(p, dtype=np.int32), npt)
+    return ob.letkf_points(X, pts, 1, 0, HX, yo, rvar, off, idx, None, rho, 0)[:, 0, :].T
+
+
+@pytest.mark.parametrize("k", [9, 32, 64, 100])
+@pytest.mark.parametrize("precision", [_lib.MG_PREC_FP64, _lib.MG_PREC_MIXED])
+def test_etkf_hunt_matches_oracle(dev, k, precision):
+    c = syn.global_etkf_grid(48, 40, k, 700, case=21)
+    Xd = T(c.X, dev)
+    HX = K.hx_idw4(Xd, c.nx, c.ny, T(c.obs_xy, dev))
+    yo = T(c.yo, dev)
+    rvar = torch.full_like(yo, c.sigma_o ** 2)
+    K.etkf(Xd, HX, yo, rvar, c.rho, flags=0, precision=precision)
+    pts = np.random.default_rng(k).choice(c.nx * c.ny, 64, replace=False)
+    want = _global_oracle_hunt(c.X, HX.cpu().numpy(), c.yo, c.rvar, c.rho, pts)
+    got = Xd.cpu().numpy()[:, pts]
+    tol = FP64_TOL if precision == _lib.MG_PREC_FP64 else MIXED_TOL
+    assert rel_err(got, want) <= tol
+
+
+def test_etkf_reference_semantics_mixed(dev):
+    g = np.load(GOLDEN / "etkf_grid64.npz")
+    Xd = T(g["X"], dev)
+    HX = K.hx_idw4(Xd, 64, 64, T(g["obs_xy"], dev))
+    yo = T(g["yo"], dev)
+    K.etkf(Xd, HX, yo, torch.full_like(yo, float(g["sigma"]) ** 2), float(g["rho"]), flags=_lib.MG_COMPAT,
+           precision=_lib.MG_PREC_MIXED)
+    assert rel_err(Xd.cpu().numpy(), g["members"]) <= MIXED_TOL
+
+
+# ----------------------------------------------------- reference-order LETKF --
+@pytest.mark.parametrize("name,rho_key", [("tutorial", "rho"), ("tutorial", "rho11"), ("letkf_grid24", "rho"),
+                                          ("letkf_grid20", "rho")])
+def test_letkf_reference_order_matches_golden(dev, name, rho_key):
+    g = np.load(GOLDEN / f"{name}.npz")
+    if name == "tutorial":
+        suffix = "letkf" if rho_key == "rho" else "letkf_rho11"
+        want, wmean = g[f"{suffix}_members"], g[f"{suffix}_mean"]
+    else:
+        want, wmean = g["members"], g["mean"]
+    Xd = T(g["X"], dev)
+    mean = K.letkf_compat_grid(Xd, int(g["nx"]), int(g["ny"]), T(g["obs_xy"], dev), T(g["yo"], dev),
+                               float(g["radius"]), float(g[rho_key]))
+    assert rel_err(Xd.cpu().numpy(), want) <= FP64_TOL
+    assert rel_err(mean.cpu().numpy(), wmean) <= FP64_TOL
+
+
+# ------------------------------------------------------------ batched LETKF --
+def _grid_batched(dev, g, rho, flags, precision):
+    nx, ny = int(g["nx"]), int(g["ny"])
+    X = g["X"]
+    s = float(g["sigma"])
+    Xd = T(X, dev)
+    xy = T(g["obs_xy"], dev)
+    HX = K.hx_idw4(Xd, nx, ny, xy)
+    yo = T(g["yo"], dev)
+    rvar = torch.full_like(yo, s * s)
+    off, idx = K.select_grid(nx, ny, xy, float(g["radius"]))
+    K.letkf_batched(Xd, col_base=torch.arange(nx * ny, dtype=torch.int64, device=dev), nlev=1, n_var=1,
+                    lev_stride=0, var_stride=0, HX=HX, yo=yo, rvar=rvar, loc_off=off, loc_idx=idx, rho=rho,
+                    flags=flags, precision=precision)
+    offc, idxc = ob.select_grid(nx, ny, g["obs_xy"], float(g["radius"]))
+    want = ob.letkf_points(X, np.arange(nx * ny), 1, 0, HX.cpu().numpy(), g["yo"], np.full(len(g["yo"]), s * s),
+                           offc, idxc, None, rho, flags)[:, 0, :].T
+    return Xd.cpu().numpy(), want
+
+
+@pytest.mark.parametrize("name", ["tutorial", "letkf_grid24", "letkf_grid20"])
+@pytest.mark.parametrize("flags", [_lib.MG_COMPAT, 0, _lib.MG_RTPS])
+@pytest.mark.parametrize("precision", [_lib.MG_PREC_FP64, _lib.MG_PREC_MIXED])
+def test_letkf_batched_grid_matches_oracle(dev, name, flags, precision):
+    g = np.load(GOLDEN / f"{name}.npz")
+    rho = 0.5 if flags == _lib.MG_RTPS else float(g["rho"]) if name != "tutorial" else 1.1
+    got, want = _grid_batched(dev, g, rho, flags, precision)
+    tol = FP64_TOL if precision == _lib.MG_PREC_FP64 else MIXED_TOL
+    assert rel_err(got, want) <= tol
+
+
+def _latlon_case(nlon, nlat, nlev, nvar, k, p, T_, case):
+    return syn.latlon_letkf_case(nlon=nlon, nlat=nlat, nlev=nlev, nvar=nvar, k=k, p=p, T=T_, case=case)
+
+
+def _run_latlon(dev, c, precision, flags=0, sample=None):
+    Xd = T(c.X, dev)
+    olat, olon, olev = T(c.obs_lat, dev), T(c.obs_lon, dev), T(c.obs_lev, dev)
+    HX = K.hx_latlon(Xd, c.nlon, c.nlat, c.nlev, olat, olon, olev, T(c.obs_var, dev))
+    clat, clon = c.col_lat_lon()
+    off, idx, dist = K.select_geo(T(clat, dev), T(clon, dev), olat, olon, c.hsupport_km)
+    yo = T(c.yo, dev)
+    rvar = torch.full_like(yo, c.sigma_o ** 2)
+    _, st = K.letkf_batched(Xd, col_base=T(c.col_base(), dev), nlev=c.nlev, n_var=c.nvar,
+                            lev_stride=c.lev_stride, var_stride=c.var_stride, HX=HX, yo=yo, rvar=rvar,
+                            loc_off=off, loc_idx=idx, loc_dist=dist, obs_lev=olev, hsupport=c.hsupport_km,
+                            vsupport=c.vsupport, rho=c.rho, flags=flags, precision=precision, want_mean=False)
+    return Xd, HX, off.cpu().numpy(), idx.cpu().numpy(), dist.cpu().numpy(), st
+
+
+def _oracle_latlon(c, HX, off, idx, dist, cols, flags=0):
+    pts, poff, pidx, pw = point_lists(cols, c.nlev, off, idx, dist, c.obs_lev, c.hsupport_km, c.vsupport,
+                                      compat=bool(flags & ob.ORC_R_IDENTITY))
+    base = c.col_base()[pts[:, 0]] + pts[:, 1] * c.lev_stride
+    out = ob.letkf_points(c.X, base, c.nvar, c.var_stride, HX, c.yo, c.rvar, poff, pidx, pw, c.rho, flags)
+    return base, out
+
+
+@pytest.mark.parametrize("precision", [_lib.MG_PREC_FP64, _lib.MG_PREC_MIXED])
+@pytest.mark.parametrize("k", [16, 64])
+def test_letkf_latlon_small_matches_oracle(dev, precision, k):
+    c = _latlon_case(72, 36, 5, 2, k, 20_000, 20, case=31)
+    Xd, HX, off, idx, dist, st = _run_latlon(dev, c, precision)
+    cols = np.arange(c.nlat * c.nlon)
+    base, want = _oracle_latlon(c, HX.cpu().numpy(), off, idx, dist, cols)
+    got = Xd.cpu().numpy()
+    gv = np.stack([got[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)  # npt x nvar x k
+    tol = FP64_TOL if precision == _lib.MG_PREC_FP64 else MIXED_TOL
+    assert rel_err(gv, want) <= tol
+    assert st.n_points == c.nlat * c.nlon * c.nlev
+    assert st.total_local > 0 and st.max_local > 0
+
+
+@pytest.mark.slow
+def test_letkf_latlon_full_size_sampled(dev):
+    """The 360 x 180 x 10 x 4, 64-member, 500k-obs configuration: FP64 and
+    mixed on the GPU, checked against the oracle on a sample of columns, and
+    mixed against FP64 everywhere (rel err <= 1e-5)."""
+    c = syn.latlon_letkf_case()
+    X64, HX, off, idx, dist, st64 = _run_latlon(dev, c, _lib.MG_PREC_FP64)
+    Xmx, _, _, _, _, stmx = _run_latlon(dev, c, _lib.MG_PREC_MIXED)
+    a64 = X64.cpu().numpy()
+    amx = Xmx.cpu().numpy()
+    # mean and perturbation errors of the mixed path against FP64
+    m64, mmx = a64.mean(0), amx.mean(0)
+    assert rel_err(mmx, m64) <= MIXED_TOL
+    assert rel_err(amx - mmx, a64 - m64) <= MIXED_TOL
+    cols = np.random.default_rng(7).choice(c.nlat * c.nlon, 40, replace=False)
+    base, want = _oracle_latlon(c, HX.cpu().numpy(), off, idx, dist, cols)
+    gv = np.stack([a64[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)
+    assert rel_err(gv, want) <= FP64_TOL
+    assert st64.total_local == stmx.total_local
