@@ -1,0 +1,402 @@
+"""Benchmark: batched LETKF on the 360 x 180 x 10-level x 4-variable lat-lon
+configuration with 64 members and 500k observations (Gaspari-Cohn support
+500 km / 2 levels), mixed precision against the FP64 path on one GB300.
+
+A step is one full analysis cycle of the hot path on inputs resident in HBM:
+restore the background ensemble (device copy), H(X) for every member,
+the spatial-hash local search, and the 648,000 local analyses (perturbations,
+obs-space prior, Gram, eigen-solve, update, write-back).  The metric is local
+analyses per second; the mixed path is the headline, the FP64 path is timed
+beside it, and the mixed analysis is checked against FP64 (max relative
+error of mean and perturbations <= 1e-5).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 (torchrun, one rank per GPU) runs independent replicas: the analysis
+has no exchange step on one GPU per problem, so there is no collective on the
+data path; barrier and max-over-ranks timing only.
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle restatement, OpenMP on all host cores) on a bounded sample of the same
+workload's local analyses; rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "local ETKF analyses/s @k=64: mixed vs FP64 on 1 GB300, rel err ≤1e-5"
+UNIT = "analyses/s"
+WORKLOAD = "batched LETKF, lat-lon 360x180x10 levels x4 vars (2.59M values), k=64, 500k obs, GC 500 km / 2 levels"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-points", type=int, default=1200, help="local analyses in the CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------- plumbing ----
+def dist_setup(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if _cuda_ok() else "gloo")
+    return rank, world, local
+
+
+def _cuda_ok() -> bool:
+    import torch
+
+    return torch.cuda.is_available()
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if _cuda_ok() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return None
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the analysis kernel from the committed ncu
+    summary (profiles/letkf_batched_kernel_latlon.md), if present."""
+    f = ROOT / "profiles" / "letkf_batched_kernel_latlon.md"
+    if not f.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
+    return float(m.group(1)) if m else None
+
+
+# ------------------------------------------------------------- workload ----
+def make_case():
+    from metada_gb300 import synthetic as syn
+
+    return syn.latlon_letkf_case()
+
+
+class Workload:
+    def __init__(self, case, device):
+        import torch
+
+        from metada_gb300 import kernels as K
+
+        self.c = case
+        self.K = K
+        T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)  # noqa: E731
+        c = case
+        self.X0 = T(c.X)
+        self.X = torch.empty_like(self.X0)
+        self.olat, self.olon, self.olev = T(c.obs_lat), T(c.obs_lon), T(c.obs_lev)
+        self.ovar = T(c.obs_var)
+        self.yo = T(c.yo)
+        self.rvar = torch.full_like(self.yo, c.sigma_o ** 2)
+        la, lo = c.col_lat_lon()
+        self.clat, self.clon = T(la), T(lo)
+        self.col_base = T(c.col_base())
+        self.npoints = c.nlat * c.nlon * c.nlev
+
+    def step(self, precision):
+        c, K = self.c, self.K
+        self.X.copy_(self.X0)
+        HX = K.hx_latlon(self.X, c.nlon, c.nlat, c.nlev, self.olat, self.olon, self.olev, self.ovar)
+        off, idx, dist = K.select_geo(self.clat, self.clon, self.olat, self.olon, c.hsupport_km)
+        _, st = K.letkf_batched(self.X, col_base=self.col_base, nlev=c.nlev, n_var=c.nvar, lev_stride=c.lev_stride,
+                                var_stride=c.var_stride, HX=HX, yo=self.yo, rvar=self.rvar, loc_off=off,
+                                loc_idx=idx, loc_dist=dist, obs_lev=self.olev, hsupport=c.hsupport_km,
+                                vsupport=c.vsupport, rho=c.rho, flags=0, precision=precision, want_mean=False)
+        return st
+
+
+def timed(fn, steps, world):
+    import torch
+
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    out = [fn() for _ in range(steps)]
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    return e0.elapsed_time(e1) / 1e3, out
+
+
+def flops_per_step(st, k, n_var):
+    """Algorithmic FLOPs of the local analyses: Gram 2k^2 p_loc, Y'^T R^-1 d
+    2k p_loc, update 2 n_var k^2 and the eigen-solve counted as 9k^3 per
+    analysis (Golub-Van Loan symmetric QR with vectors, a fixed convention)."""
+    return (2.0 * k * k + 2.0 * k) * st.total_local + (st.n_points - st.n_empty) * (2.0 * n_var * k * k + 9.0 * k ** 3)
+
+
+# ---------------------------------------------------------- CPU baseline ----
+def cpu_baseline(case, npoints: int, seed: int = 0):
+    """The oracle (the reference algorithm restated in C++, OpenMP, all host
+    threads) on a seeded sample of the workload's local analyses."""
+    import oracle.bind as ob
+    from oracle.lists import point_lists
+
+    c = case
+    la, lo = c.col_lat_lon()
+    rng = np.random.default_rng(seed)
+    ncols = max(1, npoints // c.nlev)
+    cols = rng.choice(c.nlat * c.nlon, ncols, replace=False)
+    # the sample's local search (oracle restatement of LETKF.hpp:159-165)
+    off, idx, dist = ob.select_geo(la[cols], lo[cols], c.obs_lat, c.obs_lon, c.hsupport_km)
+    pts, poff, pidx, pw = point_lists(np.arange(ncols), c.nlev, off, idx, dist, c.obs_lev, c.hsupport_km, c.vsupport)
+    # obs-space prior of the needed obs only
+    need = np.unique(pidx)
+    HXs = ob.hx_latlon(c.X, c.nlon, c.nlat, c.nlev, c.obs_lat[need], c.obs_lon[need], c.obs_lev[need],
+                       c.obs_var[need])
+    remap = np.full(c.yo.shape[0], -1, dtype=np.int64)
+    remap[need] = np.arange(need.size)
+    base = cols[pts[:, 0]] + pts[:, 1] * c.lev_stride
+    t0 = time.perf_counter()
+    ob.letkf_points(c.X, base, c.nvar, c.var_stride, HXs, c.yo[need], c.rvar[need], poff,
+                    remap[pidx].astype(np.int32), pw, c.rho, 0)
+    el = time.perf_counter() - t0
+    return {"value": len(base) / el, "unit": UNIT, "cores": ob.num_threads(), "kind": "port",
+            "sample": f"{len(base)} local analyses ({ncols} seeded columns x {c.nlev} levels) of the same workload, "
+                      f"{el:.1f} s of CPU work"}
+
+
+# ------------------------------------------------------------------ main ----
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    case = make_case()
+    import oracle.bind as ob
+
+    steps = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(case, max(100, args.cpu_points // 2), seed=i)
+        if i >= args.warmup:
+            steps.append(cb)
+    v = statistics.median(s["value"] for s in steps)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * case.nlat * case.nlon * case.nlev / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": steps[-1]["sample"]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": ob.num_threads(), "kind": "port",
+                             "sample": steps[-1]["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+
+    from metada_gb300 import _lib
+    from metada_gb300 import algorithms as A
+    from metada_gb300 import kernels as K
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    case = make_case()
+    w = Workload(case, dev)
+    c = case
+    k = c.X.shape[0]
+
+    # warm-up (mixed and FP64 once each)
+    for _ in range(args.warmup):
+        w.step(_lib.MG_PREC_MIXED)
+    w.step(_lib.MG_PREC_FP64)
+    ctx = K.context(local)
+    l0 = ctx.launches()
+    with ClockSampler(local) as clk:
+        t_mixed, sts = timed(lambda: w.step(_lib.MG_PREC_MIXED), args.steps, world)
+    launches = (ctx.launches() - l0) // max(1, args.steps)
+    clocks = clk.summary()
+    Xmixed = w.X.clone()
+    t_mixed = max_over_ranks(t_mixed, world)
+    t64, sts64 = timed(lambda: w.step(_lib.MG_PREC_FP64), args.fp64_steps, world)
+    t64 = max_over_ranks(t64, world)
+    X64 = w.X.clone()
+
+    # accuracy of the mixed path against FP64 (analysis mean and perturbations)
+    m64 = X64.mean(0)
+    mmx = Xmixed.mean(0)
+    err_mean = float((mmx - m64).abs().max() / m64.abs().max())
+    err_pert = float(((Xmixed - mmx) - (X64 - m64)).abs().max() / (X64 - m64).abs().max())
+    del X64, Xmixed
+
+    npts = w.npoints
+    value = world * npts * args.steps / t_mixed
+    v64 = world * npts * args.fp64_steps / t64
+    st = sts[-1]
+    ms_an = statistics.mean(s.ms_analysis for s in sts)
+    fl = flops_per_step(st, k, c.nvar)
+    peaks = {}
+    pf = ROOT / "MEASURED_PEAKS.json"
+    if pf.exists():
+        peaks = json.loads(pf.read_text())
+    peak_tf = peaks.get("bf16_tflops", 1900.0)
+    achieved_tf = fl / (ms_an / 1e3) / 1e12
+    traffic = profile_traffic()
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        Xh = torch.from_numpy(c.X).pin_memory()
+        out = torch.empty_like(Xh).pin_memory()
+        geom = A.LatLonGeometry(c.nlon, c.nlat, c.nlev, c.nvar)
+        cfg = {"inflation": c.rho, "localization_radius": c.hsupport_km, "vertical_radius": c.vsupport,
+               "precision": "mixed", "semantics": "hunt"}
+        obs_host = dict(values=c.yo, error=c.sigma_o, lat=c.obs_lat, lon=c.obs_lon, lev=c.obs_lev, var=c.obs_var)
+
+        def e2e_step():
+            ens = A.Ensemble(Xh, geom, device=dev)
+            obs = A.Observation(device=dev, **obs_host)
+            A.LETKF(ens, obs, A.ObsOperator(), cfg).Analyse()
+            out.copy_(ens.X, non_blocking=True)
+            return out
+
+        e2e_step()
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        te, _ = timed(e2e_step, args.e2e_steps, world)
+        te = max(te, (time.perf_counter() - t0))
+        te = max_over_ranks(te, world)
+        h2d = Xh.numel() * 8 + c.yo.size * (8 * 5 + 4)
+        e2e = {"value": world * npts * args.e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(out.numel() * 8)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(case, args.cpu_points)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 means, innovations, outputs)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "members": k, "obs": int(c.yo.size), "analyses_per_step": npts,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (1.33 GB FP64 ensemble)",
+                       "step": "restore background, H(X), spatial-hash local search, batched local analyses"},
+            "fp64": {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * t64 / args.fp64_steps,
+                     "ms_analysis_kernel": sts64[-1].ms_analysis},
+            "mixed_over_fp64": value / v64,
+            "rel_err_vs_fp64": {"mean": err_mean, "perturbations": err_pert},
+            "local_obs": {"mean": st.total_local / st.n_points, "max": st.max_local, "empty_points": st.n_empty},
+            "roofline": {"kernel": "letkf_batched_kernel<float,64>", "bound": "tensor", "achieved": achieved_tf,
+                         "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
+                         "traffic": traffic, "ms_per_launch": ms_an,
+                         "basis": f"{fl:.4g} algorithmic FLOP per launch (Gram 2k^2 p_loc + 2k p_loc + update "
+                                  f"2 n_var k^2 + eigen 9k^3); peak = measured bf16 dense"},
+            "clocks": clocks,
+            "gpu_launches": int(launches),
+        }
+        if e2e:
+            line["e2e"] = e2e
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,4 +1,5 @@
-"""Test helpers: expand per-column candidate lists into the per-point,
+"""Oracle-side helper (test infrastructure): expands per-column candidate
+lists into the per-point,
 weighted lists the oracle's LETKF takes (the library does this expansion
 inside its kernel)."""
 from __future__ import annotations

@@ -6,7 +6,7 @@ import pytest
 import torch
 
 from conftest import GOLDEN, rel_err
-from helpers import point_lists
+from oracle.lists import point_lists
 
 import oracle.bind as ob
 from metada_gb300 import _lib
