@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--cpu-points", type=int, default=1200, help="local analyses in the CPU sample")
+    ap.add_argument("--cpu-points", type=int, default=40000, help="local analyses in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 

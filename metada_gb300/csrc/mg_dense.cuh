@@ -31,7 +31,7 @@ __device__ bool cta_cholesky(T* A, int k, int lda, int* sflag) {
   for (int j = 0; j < k; ++j) {
     if (threadIdx.x == 0) {
       const T d = A[j * lda + j];
-      if (!(d > T(0)) || !isfinite((double)d)) *sflag = 0;
+      if (!(d > T(0)) || !(d < T(3.0e38))) *sflag = 0;
       A[j * lda + j] = dsqrt<T>(d > T(0) ? d : T(1));
     }
     __syncthreads();
@@ -83,14 +83,23 @@ __device__ void cta_gram_of_lower(const T* Li, T* Ainv, int k, int lda) {
 
 // Parallel cyclic Jacobi: A (kp x kp, kp even, symmetric) is diagonalised in
 // place, V receives the eigenvectors as columns (A_in = V diag(A_out) V^T).
-// A rotation of pair (p, q) is skipped when |a_pq| <= tol sqrt(|a_pp a_qq|).
-// Scratch: rot (4 * kp/2 values of T), pair (kp ints).  Returns sweeps run
-// (max_sweeps + 1 if it had not converged).
+// Round-robin (circle method) ordering: each round rotates kp/2 disjoint
+// pairs at once.  Because the pairs partition the indices, J^T A J splits
+// into independent 2 x 2 blocks (rows of pair b) x (columns of pair c): one
+// thread updates a whole block from its four inputs, so a round is one
+// rotation phase and one block phase (two barriers).  Diagonal blocks are
+// written in closed form (a_pp - t a_pq, a_qq + t a_pq, 0).  A rotation is
+// skipped when |a_pq| <= tol sqrt(|a_pp a_qq|).  init_v = false continues
+// from the basis already in V.  Scratch: rot (4 per pair), pair (2 per pair).
+// Returns the sweeps run (max_sweeps + 1 if it had not converged).
 template <typename T>
-__device__ int cta_jacobi(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T* rot, int* pair) {
-  for (int e = threadIdx.x; e < kp * kp; e += blockDim.x) {
-    const int i = e / kp, j = e % kp;
-    V[i * lda + j] = (i == j) ? T(1) : T(0);
+__device__ int cta_jacobi(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T* rot, int* pair,
+                          bool init_v = true) {
+  if (init_v) {
+    for (int e = threadIdx.x; e < kp * kp; e += blockDim.x) {
+      const int i = e / kp, j = e % kp;
+      V[i * lda + j] = (i == j) ? T(1) : T(0);
+    }
   }
   __syncthreads();
   const int h = kp >> 1, m = kp - 1;
@@ -110,7 +119,8 @@ __device__ int cta_jacobi(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T*
         if (p > q) { const int t = p; p = q; q = t; }
         const T app = A[p * lda + p], aqq = A[q * lda + q], apq = A[p * lda + q];
         T c = T(1), s = T(0), t = T(0);
-        if (apq != T(0) && fabs((double)apq) > (double)tol * sqrt(fabs((double)app * (double)aqq))) {
+        // Threshold test in the working precision (no FP64 on the FP32 path).
+        if (apq != T(0) && fabs(apq) > tol * dsqrt<T>(fabs(app) * fabs(aqq))) {
           const T theta = (aqq - app) / (T(2) * apq);
           t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + dsqrt<T>(theta * theta + T(1)));
           c = T(1) / dsqrt<T>(t * t + T(1));
@@ -125,39 +135,40 @@ __device__ int cta_jacobi(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T*
         rot[4 * i + 3] = aqq + t * apq;  // new a_qq
       }
       __syncthreads();
-      // Rows p, q.
-      for (int e = threadIdx.x; e < h * kp; e += blockDim.x) {
-        const int i = e / kp, j = e % kp;
-        const T s = rot[4 * i + 1];
-        if (s == T(0)) continue;
-        const T c = rot[4 * i + 0];
-        const int p = pair[2 * i], q = pair[2 * i + 1];
-        const T a = A[p * lda + j], b = A[q * lda + j];
-        A[p * lda + j] = c * a - s * b;
-        A[q * lda + j] = s * a + c * b;
-      }
-      __syncthreads();
-      // Columns p, q of A (2 x 2 block in closed form) and of V.
-      for (int e = threadIdx.x; e < h * kp; e += blockDim.x) {
-        const int i = e / kp, j = e % kp;
-        const T s = rot[4 * i + 1];
-        if (s == T(0)) continue;
-        const T c = rot[4 * i + 0];
-        const int p = pair[2 * i], q = pair[2 * i + 1];
-        if (j == p) {
-          A[p * lda + p] = rot[4 * i + 2];
-          A[p * lda + q] = T(0);
-        } else if (j == q) {
-          A[q * lda + p] = T(0);
-          A[q * lda + q] = rot[4 * i + 3];
-        } else {
-          const T a = A[j * lda + p], b = A[j * lda + q];
-          A[j * lda + p] = c * a - s * b;
-          A[j * lda + q] = s * a + c * b;
+      // 2 x 2 blocks of A: rows (p_b, q_b) x columns (p_c, q_c).
+      for (int e = threadIdx.x; e < h * h; e += blockDim.x) {
+        const int b = e / h, c2 = e - b * h;
+        const T sb = rot[4 * b + 1], sc = rot[4 * c2 + 1];
+        if (sb == T(0) && sc == T(0)) continue;
+        const int pb = pair[2 * b], qb = pair[2 * b + 1];
+        const int pc = pair[2 * c2], qc = pair[2 * c2 + 1];
+        if (b == c2) {
+          A[pb * lda + pb] = rot[4 * b + 2];
+          A[qb * lda + qb] = rot[4 * b + 3];
+          A[pb * lda + qb] = T(0);
+          A[qb * lda + pb] = T(0);
+          continue;
         }
-        const T va = V[j * lda + p], vb = V[j * lda + q];
-        V[j * lda + p] = c * va - s * vb;
-        V[j * lda + q] = s * va + c * vb;
+        const T cb = rot[4 * b + 0], cc = rot[4 * c2 + 0];
+        const T a00 = A[pb * lda + pc], a01 = A[pb * lda + qc];
+        const T a10 = A[qb * lda + pc], a11 = A[qb * lda + qc];
+        const T m00 = cb * a00 - sb * a10, m01 = cb * a01 - sb * a11;  // rows: J_b^T A
+        const T m10 = sb * a00 + cb * a10, m11 = sb * a01 + cb * a11;
+        A[pb * lda + pc] = cc * m00 - sc * m01;  // columns: (.) J_c
+        A[pb * lda + qc] = sc * m00 + cc * m01;
+        A[qb * lda + pc] = cc * m10 - sc * m11;
+        A[qb * lda + qc] = sc * m10 + cc * m11;
+      }
+      // Columns (p_c, q_c) of V.
+      for (int e = threadIdx.x; e < kp * h; e += blockDim.x) {
+        const int row = e / h, c2 = e - row * h;
+        const T sc = rot[4 * c2 + 1];
+        if (sc == T(0)) continue;
+        const T cc = rot[4 * c2 + 0];
+        const int pc = pair[2 * c2], qc = pair[2 * c2 + 1];
+        const T va = V[row * lda + pc], vb = V[row * lda + qc];
+        V[row * lda + pc] = cc * va - sc * vb;
+        V[row * lda + qc] = sc * va + cc * vb;
       }
       __syncthreads();
     }
@@ -209,7 +220,7 @@ __device__ bool solve_transform(T* A, T* V, const T* bvec, T* wa, T* lam, T* uve
   for (int i = tid; i < k; i += nt) {
     const T l = A[i * lda + i];
     lam[i] = l;
-    if (!(l > T(0)) || !isfinite((double)l)) misc[1] = 1;
+    if (!(l > T(0)) || !(l < T(3.0e38))) misc[1] = 1;
   }
   __syncthreads();
   ok = misc[1] == 0;

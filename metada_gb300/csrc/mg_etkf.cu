@@ -10,6 +10,10 @@
 //      transform T (T_ji = rho (wa_j + W_ji) for the reference, whose
 //      perturbations carry the inflation, ETKF.hpp:125);
 //   5. Xa_i = xm + sum_j X'_j T_ji, streamed over state tiles.
+// The Gram, its reduction and the k x k solve are FP64 on both paths (one
+// system per analysis, negligible cost; the small eigenvalues of
+// (k-1)I + Y'^T R^-1 Y' need it); the mixed path stores X' in FP32 and runs
+// the O(n k^2) update in FP32.
 // The reference never recomputes the ensemble mean after the update
 // (ETKF.hpp:190-191); mean_out receives that background mean.
 #include <algorithm>
@@ -132,14 +136,14 @@ __global__ void __launch_bounds__(kThreads) etkf_solve_kernel(const double* __re
 template <typename TE>
 __global__ void __launch_bounds__(kThreads) etkf_update_kernel(const TE* __restrict__ Xp, int64_t ldp,
                                                                const double* __restrict__ mean,
-                                                               const TE* __restrict__ T, int64_t n,
+                                                               const double* __restrict__ T, int64_t n,
                                                                int k, double* __restrict__ X,
                                                                int64_t ld) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TE* Ts = reinterpret_cast<TE*>(smem_raw);  // k x k
   TE* Xt = Ts + k * k;                       // 32 x (k + 1)
   const int64_t s0 = (int64_t)blockIdx.x * 32;
-  for (int e = threadIdx.x; e < k * k; e += kThreads) Ts[e] = T[e];
+  for (int e = threadIdx.x; e < k * k; e += kThreads) Ts[e] = (TE)T[e];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int j = warp; j < k; j += kThreads / 32) {
     const int64_t s = s0 + lane;
@@ -174,42 +178,40 @@ int run_etkf(mg_context* ctx, double* X, int64_t n, int k, int64_t ld, const dou
   mg::Carver cv;
   cv.reserve<double>(n);
   cv.reserve<TE>((size_t)n * k);
-  cv.reserve<TE>((size_t)(p + 1) * k);
+  cv.reserve<double>((size_t)(p + 1) * k);
   cv.reserve<double>(p + 1);
   cv.reserve<double>(p + 1);
   cv.reserve<double>((size_t)nblk * k * k);
   cv.reserve<double>((size_t)nblk * k);
-  cv.reserve<TE>((size_t)k * k);
+  cv.reserve<double>((size_t)k * k);
   cv.reserve<int>(4);
   void* ws = mg::workspace(ctx, cv.off);
   if (!ws) return MG_ERR_NOMEM;
   cv = mg::Carver{static_cast<char*>(ws), 0};
   double* mean = cv.take<double>(n);
   TE* Xp = cv.take<TE>((size_t)n * k);
-  TE* Y = cv.take<TE>((size_t)(p + 1) * k);
+  double* Y = cv.take<double>((size_t)(p + 1) * k);
   double* dinn = cv.take<double>(p + 1);
   double* rinv = cv.take<double>(p + 1);
   double* Gpart = cv.take<double>((size_t)nblk * k * k);
   double* bpart = cv.take<double>((size_t)nblk * k);
-  TE* T = cv.take<TE>((size_t)k * k);
+  double* T = cv.take<double>((size_t)k * k);
   int* status = cv.take<int>(4);
   cudaStream_t s = ctx->stream;
   const bool f64 = sizeof(TE) == 8;
   MG_TRY_CUDA(mg::launch_mean_pert_members(X, n, k, ld, mean, f64 ? (double*)Xp : nullptr,
                                            f64 ? nullptr : (float*)Xp, n, s));
-  MG_TRY_CUDA(mg::launch_obs_prior(HX, yo, rvar, p, k, f64 ? (double*)Y : nullptr,
-                                   f64 ? nullptr : (float*)Y, dinn, rinv, s));
-  if (k <= 32) MG_TRY_CUDA((launch_gram<TE, 32>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s)));
-  else if (k <= 64) MG_TRY_CUDA((launch_gram<TE, 64>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s)));
-  else MG_TRY_CUDA((launch_gram<TE, 128>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s)));
+  MG_TRY_CUDA(mg::launch_obs_prior(HX, yo, rvar, p, k, Y, nullptr, dinn, rinv, s));
+  if (k <= 32) MG_TRY_CUDA((launch_gram<double, 32>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s)));
+  else if (k <= 64) MG_TRY_CUDA((launch_gram<double, 64>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s)));
+  else MG_TRY_CUDA((launch_gram<double, 128>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s)));
   MG_TRY_CUDA(cudaMemsetAsync(status, 0, sizeof(int) * 4, s));
   const int kp = k + (k & 1);
-  const size_t smem = sizeof(TE) * (2 * (size_t)kp * (kp + 1) + 6 * (size_t)kp) + sizeof(int) * (kp + 8) + 64;
-  if (smem > 227 * 1024) return mg::fail(ctx, MG_ERR_ARG, "mg_etkf: k too large for this precision");
-  MG_TRY_CUDA(cudaFuncSetAttribute(etkf_solve_kernel<TE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const size_t smem = sizeof(double) * (2 * (size_t)kp * (kp + 1) + 6 * (size_t)kp) + sizeof(int) * (kp + 8) + 64;
+  if (smem > 227 * 1024) return mg::fail(ctx, MG_ERR_ARG, "mg_etkf: k too large");
+  MG_TRY_CUDA(cudaFuncSetAttribute(etkf_solve_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
-  etkf_solve_kernel<TE><<<1, kThreads, smem, s>>>(Gpart, bpart, nblk, k, flags, rho,
-                                                  f64 ? 1e-14 : 1e-6, f64 ? 30 : 20, T, status);
+  etkf_solve_kernel<double><<<1, kThreads, smem, s>>>(Gpart, bpart, nblk, k, flags, rho, 1e-14, 30, T, status);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   const size_t usmem = sizeof(TE) * ((size_t)k * k + 32 * (size_t)(k + 1));
@@ -233,12 +235,10 @@ extern "C" int mg_etkf(mg_context* ctx, double* X, int64_t n, int32_t k, int64_t
                        const double* HX, const double* yo, const double* rvar, int64_t p,
                        double rho, int32_t flags, int32_t precision, double* mean_out) {
   if (!ctx) return MG_ERR_ARG;
-  MG_CHECK_ARG(X && n > 0 && k >= 2 && k <= 128 && ld >= n && p >= 1 && HX && yo && rvar && rho > 0.0,
+  MG_CHECK_ARG(X && n > 0 && k >= 2 && ld >= n && p >= 1 && HX && yo && rvar && rho > 0.0,
                "mg_etkf: bad arguments (k must be 2..128, p >= 1)");
   MG_CHECK_ARG(precision == MG_PREC_FP64 || precision == MG_PREC_MIXED, "mg_etkf: bad precision");
-  if (precision == MG_PREC_FP64) {
-    MG_CHECK_ARG(k <= 112, "mg_etkf: FP64 path supports k <= 112");
-    return run_etkf<double>(ctx, X, n, k, ld, HX, yo, rvar, p, rho, flags, mean_out);
-  }
+  MG_CHECK_ARG(k <= 112, "mg_etkf: k must be <= 112 (FP64 k x k solve in shared memory)");
+  if (precision == MG_PREC_FP64) return run_etkf<double>(ctx, X, n, k, ld, HX, yo, rvar, p, rho, flags, mean_out);
   return run_etkf<float>(ctx, X, n, k, ld, HX, yo, rvar, p, rho, flags, mean_out);
 }

@@ -59,40 +59,134 @@ struct LetkfParams {
   int sweep_cap;
 };
 
-__device__ __forceinline__ double gaspari_cohn(double z) {
+template <typename T>
+__device__ __forceinline__ T gaspari_cohn(T z) {
   z = fabs(z);
-  if (z >= 2.0) return 0.0;
-  if (z <= 1.0) return (((-0.25 * z + 0.5) * z + 0.625) * z - 5.0 / 3.0) * z * z + 1.0;
-  return ((((z / 12.0 - 0.5) * z + 0.625) * z + 5.0 / 3.0) * z - 5.0) * z + 4.0 - 2.0 / (3.0 * z);
+  if (z >= T(2)) return T(0);
+  if (z <= T(1))
+    return (((T(-0.25) * z + T(0.5)) * z + T(0.625)) * z - T(5.0 / 3.0)) * z * z + T(1);
+  return ((((z / T(12) - T(0.5)) * z + T(0.625)) * z + T(5.0 / 3.0)) * z - T(5)) * z + T(4) -
+         T(2) / (T(3) * z);
 }
 
+// Shared-memory plan of one CTA.  The FP32 (mixed) path with k <= 96 runs a
+// two-stage eigen-solve and needs a second k x k basis (V2) and a chunk of
+// rotated rows (Bc); the other paths do not.
 template <typename TE, int KMAX>
-struct Smem {
+struct Plan {
+  static constexpr bool TWO_STAGE = sizeof(TE) == 4 && KMAX <= 96;
   static constexpr int LDA = KMAX + 1;
-  static constexpr int CH = (sizeof(TE) == 8 && KMAX > 64) ? 32 : 64;  // Gram chunk rows
+  static constexpr int CH = (sizeof(TE) == 8 && KMAX > 64) ? 32 : 64;  // list chunk rows
+  static constexpr int NMAT = TWO_STAGE ? 3 : 2;                       // A, V (, V2)
+  static constexpr int NCHUNK = TWO_STAGE ? 2 : 1;                     // Ys (, Bc)
+  static constexpr size_t te_count() {
+    return (size_t)NMAT * KMAX * LDA + (size_t)NCHUNK * CH * KMAX + 2 * CH + 4 * KMAX + 2 * KMAX +
+           kNVarMax * KMAX;
+  }
   static constexpr size_t bytes() {
-    return sizeof(TE) * (2 * (size_t)KMAX * LDA + (size_t)CH * KMAX + 3 * CH + 4 * KMAX +
-                         2 * KMAX + kNVarMax * KMAX) +
-           sizeof(double) * (2 * kNVarMax) + sizeof(int) * (CH + KMAX + 16) + 64;
+    return sizeof(TE) * te_count() + sizeof(double) * (2 * kNVarMax) + sizeof(int) * (CH + KMAX + 16) + 64;
   }
 };
 
+// Walks the candidate list of column `col` for analysis level `lev` in
+// chunks of CH entries: filters by vertical support, weights (Gaspari-Cohn x
+// 1/sigma^2, or 1 for R = I), compacts the kept entries and gathers their Y'
+// rows into Ys (zero-padded to KMAX columns); then calls body(cnt) with the
+// chunk ready in shared memory.  Returns the number of local obs.
+template <typename TE, int KMAX, int CH, typename Body>
+__device__ int for_each_chunk(const LetkfParams& prm, int64_t e0, int64_t e1, int lev, TE* Ys, int* sel_o,
+                              TE* sel_r, TE* sel_d, int* wcnt, Body&& body) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int k = prm.k;
+  const TE* Y = static_cast<const TE*>(prm.Y);
+  const bool r_identity = prm.flags & MG_R_IDENTITY;
+  const TE hc = (TE)(0.5 * prm.hsupport), vc = (TE)(0.5 * prm.vsupport), vs = (TE)prm.vsupport;
+  int nloc = 0;
+  for (int64_t c0 = e0; c0 < e1; c0 += CH) {
+    bool keep = false;
+    int o = 0;
+    TE rw = TE(0), dd = TE(0);
+    if (tid < CH && c0 + tid < e1) {
+      const int64_t e = c0 + tid;
+      o = prm.loc_idx[e];
+      TE w = TE(1);
+      keep = true;
+      if (prm.obs_lev) {
+        const TE dl = fabs((TE)lev - (TE)prm.obs_lev[o]);
+        if (dl > vs) keep = false;
+        else if (!r_identity) w *= gaspari_cohn<TE>(dl / vc);
+      }
+      if (keep && !r_identity) {
+        if (prm.loc_dist) w *= gaspari_cohn<TE>((TE)prm.loc_dist[e] / hc);
+        w *= (TE)prm.rinv[o];
+        if (!(w > TE(0))) keep = false;
+      }
+      rw = w;
+      dd = (TE)prm.dinn[o];
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) wcnt[warp] = __popc(bal);
+    __syncthreads();
+    int wbase = 0, cnt = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+      if (w < warp) wbase += wcnt[w];
+      cnt += wcnt[w];
+    }
+    if (keep) {
+      const int pos = wbase + __popc(bal & ((1u << lane) - 1u));
+      sel_o[pos] = o;
+      sel_r[pos] = rw;
+      sel_d[pos] = dd;
+    }
+    __syncthreads();
+    for (int e = tid; e < cnt * KMAX; e += kThreads) {
+      const int r = e / KMAX, j = e - r * KMAX;
+      Ys[e] = (j < k) ? Y[(int64_t)sel_o[r] * k + j] : TE(0);
+    }
+    __syncthreads();
+    body(cnt);
+    nloc += cnt;
+    __syncthreads();
+  }
+  return nloc;
+}
+
+// acc += sum_r w_r * M[r, ti*R..] (x) M[r, tj*R..] over the rows of a chunk.
+template <typename TE, int KMAX, int R>
+__device__ __forceinline__ void gram_rows(TE (&acc)[R][R], const TE* M, const TE* w, int cnt, int ti, int tj) {
+  for (int r = 0; r < cnt; ++r) {
+    const TE wr = w ? w[r] : TE(1);
+    TE av[R], bv[R];
+#pragma unroll
+    for (int a = 0; a < R; ++a) av[a] = M[r * KMAX + ti * R + a] * wr;
+#pragma unroll
+    for (int b = 0; b < R; ++b) bv[b] = M[r * KMAX + tj * R + b];
+#pragma unroll
+    for (int a = 0; a < R; ++a)
+#pragma unroll
+      for (int b = 0; b < R; ++b) acc[a][b] += av[a] * bv[b];
+  }
+}
+
 template <typename TE, int KMAX>
 __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm) {
-  using S = Smem<TE, KMAX>;
-  constexpr int LDA = S::LDA, CH = S::CH, R = KMAX / 16;
+  using P = Plan<TE, KMAX>;
+  constexpr int LDA = P::LDA, CH = P::CH, R = KMAX / 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TE* A = reinterpret_cast<TE*>(smem_raw);
   TE* V = A + KMAX * LDA;
-  TE* Ys = V + KMAX * LDA;        // CH x KMAX
-  TE* sel_r = Ys + CH * KMAX;     // CH
-  TE* sel_d = sel_r + CH;         // CH
-  TE* bvec = sel_d + CH;          // KMAX
-  TE* wa = bvec + KMAX;           // KMAX
-  TE* uvec = wa + KMAX;           // KMAX
-  TE* lam = uvec + KMAX;          // KMAX
-  TE* rot = lam + KMAX;           // 2*KMAX (4 per pair)
-  TE* Xs = rot + 2 * KMAX;        // kNVarMax x KMAX
+  TE* V2 = V + KMAX * LDA;                   // two-stage only
+  TE* Ys = V + (P::NMAT - 1) * KMAX * LDA;   // CH x KMAX
+  TE* Bc = Ys + CH * KMAX;                   // two-stage only: CH x KMAX
+  TE* sel_r = Ys + P::NCHUNK * CH * KMAX;    // CH
+  TE* sel_d = sel_r + CH;                    // CH
+  TE* bvec = sel_d + CH;                     // KMAX
+  TE* wa = bvec + KMAX;                      // KMAX
+  TE* uvec = wa + KMAX;                      // KMAX
+  TE* lam = uvec + KMAX;                     // KMAX
+  TE* rot = lam + KMAX;                      // 2*KMAX (4 per pair)
+  TE* Xs = rot + 2 * KMAX;                   // kNVarMax x KMAX
   double* xm = reinterpret_cast<double*>(Xs + kNVarMax * KMAX);  // kNVarMax
   double* red = xm + kNVarMax;                                   // kNVarMax
   int* sel_o = reinterpret_cast<int*>(red + kNVarMax);           // CH
@@ -101,17 +195,15 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
   __shared__ long long s_item;
   __shared__ int wcnt[kThreads / 32];
 
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const int k = prm.k, kp = prm.kp;
-  const TE* Y = static_cast<const TE*>(prm.Y);
   const TE* Xp = static_cast<const TE*>(prm.Xp);
   const int ti = tid / 16, tj = tid % 16;
-  const bool r_identity = prm.flags & MG_R_IDENTITY;
   const bool use_chol = prm.flags & MG_SQRT_CHOLESKY;
   const bool infl_compat = prm.flags & MG_INFL_COMPAT;
   const bool upd_compat = prm.flags & MG_UPDATE_COMPAT;
   const bool rtps = prm.flags & MG_RTPS;
-  const double hc = 0.5 * prm.hsupport, vc = 0.5 * prm.vsupport;
+  const bool two_stage = P::TWO_STAGE && !use_chol;
 
   for (;;) {
     if (tid == 0) s_item = (long long)atomicAdd(prm.next, 1ull);
@@ -124,74 +216,18 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
     const int64_t base = prm.col_base[col] + (int64_t)lev * prm.lev_stride;
     const int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
 
-    // ---- Gram and b accumulation over the local list, chunk by chunk ----
+    // ---- Gram G = Y'^T R^-1 Y' and b = Y'^T R^-1 d ----
     TE acc[R][R];
 #pragma unroll
     for (int a = 0; a < R; ++a)
 #pragma unroll
       for (int b = 0; b < R; ++b) acc[a][b] = TE(0);
     TE bacc = TE(0);
-    int nloc = 0;
-    for (int64_t c0 = e0; c0 < e1; c0 += CH) {
-      bool keep = false;
-      int o = 0;
-      TE rw = TE(0), dd = TE(0);
-      if (tid < CH && c0 + tid < e1) {
-        const int64_t e = c0 + tid;
-        o = prm.loc_idx[e];
-        double w = 1.0;
-        keep = true;
-        if (prm.obs_lev) {
-          const double dl = fabs((double)lev - prm.obs_lev[o]);
-          if (dl > prm.vsupport) keep = false;
-          else if (!r_identity) w *= gaspari_cohn(dl / vc);
-        }
-        if (keep && !r_identity) {
-          if (prm.loc_dist) w *= gaspari_cohn(prm.loc_dist[e] / hc);
-          w *= prm.rinv[o];
-          if (!(w > 0.0)) keep = false;
-        }
-        rw = (TE)w;
-        dd = (TE)prm.dinn[o];
-      }
-      const unsigned bal = __ballot_sync(0xffffffffu, keep);
-      if (lane == 0) wcnt[warp] = __popc(bal);
-      __syncthreads();
-      int wbase = 0, cnt = 0;
-#pragma unroll
-      for (int w = 0; w < kThreads / 32; ++w) {
-        if (w < warp) wbase += wcnt[w];
-        cnt += wcnt[w];
-      }
-      if (keep) {
-        const int pos = wbase + __popc(bal & ((1u << lane) - 1u));
-        sel_o[pos] = o;
-        sel_r[pos] = rw;
-        sel_d[pos] = dd;
-      }
-      __syncthreads();
-      for (int e = tid; e < cnt * KMAX; e += kThreads) {
-        const int r = e / KMAX, j = e - r * KMAX;
-        Ys[e] = (j < k) ? Y[(int64_t)sel_o[r] * k + j] : TE(0);
-      }
-      __syncthreads();
-      for (int r = 0; r < cnt; ++r) {
-        const TE w = sel_r[r];
-        TE av[R], bv[R];
-#pragma unroll
-        for (int a = 0; a < R; ++a) av[a] = Ys[r * KMAX + ti * R + a] * w;
-#pragma unroll
-        for (int b = 0; b < R; ++b) bv[b] = Ys[r * KMAX + tj * R + b];
-#pragma unroll
-        for (int a = 0; a < R; ++a)
-#pragma unroll
-          for (int b = 0; b < R; ++b) acc[a][b] += av[a] * bv[b];
-      }
+    const int nloc = for_each_chunk<TE, KMAX, CH>(prm, e0, e1, lev, Ys, sel_o, sel_r, sel_d, wcnt, [&](int cnt) {
+      gram_rows<TE, KMAX, R>(acc, Ys, sel_r, cnt, ti, tj);
       if (tid < k)
         for (int r = 0; r < cnt; ++r) bacc += (Ys[r * KMAX + tid] * sel_r[r]) * sel_d[r];
-      nloc += cnt;
-      __syncthreads();
-    }
+    });
 
     // Load this point's perturbations and means (all variables).
     for (int e = tid; e < prm.n_var * k; e += kThreads) {
@@ -230,9 +266,88 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
     __syncthreads();
 
     int sweeps = 0;
-    const bool ok = mg::solve_transform<TE>(A, V, bvec, wa, lam, uvec, rot, pairbuf, misc, k, kp,
-                                            LDA, use_chol, infl_compat, prm.rho, (TE)prm.tol,
-                                            prm.sweep_cap, &sweeps);
+    bool ok = true;
+    if (!two_stage) {
+      ok = mg::solve_transform<TE>(A, V, bvec, wa, lam, uvec, rot, pairbuf, misc, k, kp, LDA, use_chol,
+                                   infl_compat, prm.rho, (TE)prm.tol, prm.sweep_cap, &sweeps);
+    } else {
+      // Stage 1: loose Jacobi on A = diag I + G gives a basis V1 in which A
+      // is nearly diagonal.
+      sweeps = mg::cta_jacobi<TE>(A, V, kp, LDA, TE(1e-4), prm.sweep_cap, rot, pairbuf);
+      // Stage 2: rebuild A2 = V1^T A V1 from the factor, diag I + B^T B with
+      // B = R^-1/2 Y' V1, chunk by chunk.  Entries of B^T B carry errors
+      // relative to the column norms of B, so the small eigenvalues keep
+      // their relative accuracy (no eps * cond(A) loss from rounding A).
+#pragma unroll
+      for (int a = 0; a < R; ++a)
+#pragma unroll
+        for (int b = 0; b < R; ++b) acc[a][b] = TE(0);
+      for_each_chunk<TE, KMAX, CH>(prm, e0, e1, lev, Ys, sel_o, sel_r, sel_d, wcnt, [&](int cnt) {
+        for (int e = tid; e < cnt * KMAX; e += kThreads) {
+          const int r = e / KMAX, j = e - r * KMAX;
+          TE s = TE(0);
+          if (j < k) {
+            for (int m = 0; m < k; ++m) s += Ys[r * KMAX + m] * V[m * LDA + j];
+            s *= sqrt(sel_r[r]);
+          }
+          Bc[e] = s;
+        }
+        __syncthreads();
+        gram_rows<TE, KMAX, R>(acc, Bc, nullptr, cnt, ti, tj);
+      });
+#pragma unroll
+      for (int a = 0; a < R; ++a)
+#pragma unroll
+        for (int b = 0; b < R; ++b) {
+          const int i = ti * R + a, j = tj * R + b;
+          if (i < kp && j < kp) {
+            TE v = (i < k && j < k) ? acc[a][b] : TE(0);
+            if (i == j) v += (i < k) ? diag : TE(1);
+            A[i * LDA + j] = v;
+          }
+        }
+      __syncthreads();
+      // Stage 3: tight Jacobi on A2 (nearly diagonal, well scaled).
+      sweeps += mg::cta_jacobi<TE>(A, V2, kp, LDA, (TE)prm.tol, prm.sweep_cap, rot, pairbuf);
+      for (int i = tid; i < k; i += kThreads) {
+        const TE l = A[i * LDA + i];
+        lam[i] = l;
+        if (!(l > TE(0)) || !(l < TE(3.0e38))) atomicExch(prm.status, 1);
+      }
+      __syncthreads();
+      // V = V1 V2 into A (A2 is no longer needed), then copy back to V.
+      for (int e = tid; e < k * k; e += kThreads) {
+        const int i = e / k, j = e - i * k;
+        TE s = TE(0);
+        for (int m = 0; m < k; ++m) s += V[i * LDA + m] * V2[m * LDA + j];
+        A[i * LDA + j] = s;
+      }
+      __syncthreads();
+      for (int e = tid; e < k * k; e += kThreads) V[(e / k) * LDA + e % k] = A[(e / k) * LDA + e % k];
+      const TE sc = infl_compat ? (TE)prm.rho : TE(1);
+      __syncthreads();
+      for (int i = tid; i < k; i += kThreads) {  // u = diag(sc / lam) V^T b
+        TE s = TE(0);
+        for (int j = 0; j < k; ++j) s += V[j * LDA + i] * bvec[j];
+        uvec[i] = s * sc / lam[i];
+      }
+      __syncthreads();
+      for (int i = tid; i < k; i += kThreads) {  // wa = V u
+        TE s = TE(0);
+        for (int m = 0; m < k; ++m) s += V[i * LDA + m] * uvec[m];
+        wa[i] = s;
+      }
+      __syncthreads();
+      for (int i = tid; i < k; i += kThreads) uvec[i] = mg::dsqrt<TE>(TE(k - 1) * sc / lam[i]);
+      __syncthreads();
+      for (int e = tid; e < k * k; e += kThreads) {  // W = V diag(sqrt((k-1) sc / lam)) V^T
+        const int i = e / k, j = e - i * k;
+        TE s = TE(0);
+        for (int m = 0; m < k; ++m) s += V[i * LDA + m] * uvec[m] * V[j * LDA + m];
+        A[i * LDA + j] = s;
+      }
+      __syncthreads();
+    }
     if (!ok && tid == 0) atomicExch(prm.status, 1);
 
     // ---- update every variable of the point ----
@@ -297,7 +412,7 @@ __global__ void list_len_kernel(const int64_t* __restrict__ off, int64_t ncol,
 
 template <typename TE, int KMAX>
 int launch_batched(mg_context* ctx, LetkfParams& prm) {
-  const size_t smem = Smem<TE, KMAX>::bytes();
+  const size_t smem = Plan<TE, KMAX>::bytes();
   if (smem > 227 * 1024) return mg::fail(ctx, MG_ERR_ARG, "mg_letkf_batched: k too large for this precision");
   MG_TRY_CUDA(cudaFuncSetAttribute(letkf_batched_kernel<TE, KMAX>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
