@@ -50,6 +50,9 @@ extern "C" {
 #define MG_UPDATE_COMPAT 8
 #define MG_COMPAT 15
 #define MG_RTPS 16 /* relaxation to prior spread with alpha = rho (no multiplicative inflation) */
+#define MG_COLD_START 32 /* batched LETKF: every eigen-solve from the identity (default: the
+                            levels of a column run in sequence, each warm-started from the
+                            previous level's eigenvectors) */
 
 /* Arithmetic of the analysis. */
 #define MG_PREC_FP64 0  /* every step in IEEE double */
@@ -187,6 +190,7 @@ typedef struct mg_letkf_stats {
   double ms_prepare;     /* device time: perturbations, obs prior, ordering */
   double ms_analysis;    /* device time of the local-analysis kernel */
   double ms_writeback;   /* device time: write-back to members and mean */
+  int64_t total_sweeps;  /* Jacobi sweeps summed over all analyses */
 } mg_letkf_stats;
 int mg_letkf_last_stats(const mg_context* ctx, mg_letkf_stats* stats);
 

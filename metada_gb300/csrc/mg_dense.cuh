@@ -177,6 +177,37 @@ __device__ int cta_jacobi(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T*
   return sweep + 1;
 }
 
+// A <- V^T A V in place (k x k), using tmp (at least rows x lda values of T,
+// rows >= 1) as a staging buffer: first A <- A V row block by row block, then
+// A <- V^T A column block by column block.
+template <typename T>
+__device__ void cta_similarity(T* A, const T* V, int k, int lda, T* tmp, int rows) {
+  for (int r0 = 0; r0 < k; r0 += rows) {
+    const int nr = (k - r0 < rows) ? k - r0 : rows;
+    for (int e = threadIdx.x; e < nr * k; e += blockDim.x) tmp[(e / k) * lda + e % k] = A[(r0 + e / k) * lda + e % k];
+    __syncthreads();
+    for (int e = threadIdx.x; e < nr * k; e += blockDim.x) {
+      const int r = e / k, j = e - r * k;
+      T s = T(0);
+      for (int m = 0; m < k; ++m) s += tmp[r * lda + m] * V[m * lda + j];
+      A[(r0 + r) * lda + j] = s;
+    }
+    __syncthreads();
+  }
+  for (int c0 = 0; c0 < k; c0 += rows) {
+    const int nc = (k - c0 < rows) ? k - c0 : rows;
+    for (int e = threadIdx.x; e < nc * k; e += blockDim.x) tmp[(e / k) * lda + e % k] = A[(e % k) * lda + c0 + e / k];
+    __syncthreads();
+    for (int e = threadIdx.x; e < nc * k; e += blockDim.x) {
+      const int c = e % nc, i = e / nc;
+      T s = T(0);
+      for (int m = 0; m < k; ++m) s += V[m * lda + i] * tmp[c * lda + m];
+      A[i * lda + c0 + c] = s;
+    }
+    __syncthreads();
+  }
+}
+
 // The k x k part of one ensemble-space analysis.  On entry A holds
 // diag * I + Y'^T R^-1 Y' (k x k, padded to kp with a decoupled unit
 // diagonal when k is odd) and b = Y'^T R^-1 d.  On exit A holds W (k x k) and
@@ -191,7 +222,8 @@ __device__ int cta_jacobi(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T*
 template <typename T>
 __device__ bool solve_transform(T* A, T* V, const T* bvec, T* wa, T* lam, T* uvec, T* rot,
                                 int* pairbuf, int* misc, int k, int kp, int lda, bool use_chol,
-                                bool infl_compat, double rho, T tol, int sweep_cap, int* sweeps) {
+                                bool infl_compat, double rho, T tol, int sweep_cap, int* sweeps,
+                                bool warm = false, T* tmp = nullptr, int tmp_rows = 0) {
   const int tid = threadIdx.x, nt = blockDim.x;
   bool ok = true;
   *sweeps = 0;
@@ -215,7 +247,10 @@ __device__ bool solve_transform(T* A, T* V, const T* bvec, T* wa, T* lam, T* uve
     return ok;
   }
   if (tid == 0) misc[1] = 0;
-  *sweeps = cta_jacobi<T>(A, V, kp, lda, tol, sweep_cap, rot, pairbuf);
+  // Warm start: V holds the eigenvectors of a nearby system; rotate A into
+  // that basis and let the sweeps continue from it.
+  if (warm) cta_similarity<T>(A, V, kp, lda, tmp, tmp_rows);
+  *sweeps = cta_jacobi<T>(A, V, kp, lda, tol, sweep_cap, rot, pairbuf, !warm);
   const T sc = infl_compat ? (T)rho : T(1);
   for (int i = tid; i < k; i += nt) {
     const T l = A[i * lda + i];

@@ -52,11 +52,13 @@ struct LetkfParams {
   unsigned long long* next;
   unsigned long long* n_empty;
   unsigned long long* total_local;
+  unsigned long long* total_sweeps;
   int* max_local;
   int* max_sweeps;
   int* status;
   double tol;
   int sweep_cap;
+  int warm_start;  // levels of a column run in sequence, each Jacobi warm-started
 };
 
 template <typename T>
@@ -205,14 +207,27 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
   const bool rtps = prm.flags & MG_RTPS;
   const bool two_stage = P::TWO_STAGE && !use_chol;
 
+  // Cold: one work item per (column, level).  Warm start: one item per
+  // column, its levels analysed in sequence by this CTA, each eigen-solve
+  // starting from the previous level's eigenvectors (kept in V).
+  const bool warm_mode = prm.warm_start != 0 && !use_chol;
+  const long long nitems = warm_mode ? prm.ncol : prm.npoints;
+  long long item = 0;
+  int lev = prm.nlev;
+  bool have_basis = false;
   for (;;) {
-    if (tid == 0) s_item = (long long)atomicAdd(prm.next, 1ull);
-    __syncthreads();
-    const long long item = s_item;
-    __syncthreads();
-    if (item >= prm.npoints) break;
-    const int64_t col = prm.order[item / prm.nlev];
-    const int lev = (int)(item % prm.nlev);
+    if (!warm_mode || lev + 1 >= prm.nlev) {
+      if (tid == 0) s_item = (long long)atomicAdd(prm.next, 1ull);
+      __syncthreads();
+      item = s_item;
+      __syncthreads();
+      if (item >= nitems) break;
+      lev = warm_mode ? 0 : (int)(item % prm.nlev);
+      have_basis = false;
+    } else {
+      ++lev;
+    }
+    const int64_t col = warm_mode ? prm.order[item] : prm.order[item / prm.nlev];
     const int64_t base = prm.col_base[col] + (int64_t)lev * prm.lev_stride;
     const int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
 
@@ -269,11 +284,15 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
     bool ok = true;
     if (!two_stage) {
       ok = mg::solve_transform<TE>(A, V, bvec, wa, lam, uvec, rot, pairbuf, misc, k, kp, LDA, use_chol,
-                                   infl_compat, prm.rho, (TE)prm.tol, prm.sweep_cap, &sweeps);
+                                   infl_compat, prm.rho, (TE)prm.tol, prm.sweep_cap, &sweeps,
+                                   warm_mode && have_basis, Ys, CH - 1);
+      have_basis = !use_chol;
     } else {
       // Stage 1: loose Jacobi on A = diag I + G gives a basis V1 in which A
       // is nearly diagonal.
-      sweeps = mg::cta_jacobi<TE>(A, V, kp, LDA, TE(1e-4), prm.sweep_cap, rot, pairbuf);
+      const bool warm = warm_mode && have_basis;
+      if (warm) mg::cta_similarity<TE>(A, V, kp, LDA, Ys, CH - 1);
+      sweeps = mg::cta_jacobi<TE>(A, V, kp, LDA, TE(1e-4), prm.sweep_cap, rot, pairbuf, !warm);
       // Stage 2: rebuild A2 = V1^T A V1 from the factor, diag I + B^T B with
       // B = R^-1/2 Y' V1, chunk by chunk.  Entries of B^T B carry errors
       // relative to the column norms of B, so the small eigenvalues keep
@@ -324,6 +343,7 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
       }
       __syncthreads();
       for (int e = tid; e < k * k; e += kThreads) V[(e / k) * LDA + e % k] = A[(e / k) * LDA + e % k];
+      have_basis = true;
       const TE sc = infl_compat ? (TE)prm.rho : TE(1);
       __syncthreads();
       for (int i = tid; i < k; i += kThreads) {  // u = diag(sc / lam) V^T b
@@ -392,6 +412,7 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
     }
     if (tid == 0) {
       atomicAdd(prm.total_local, (unsigned long long)nloc);
+      atomicAdd(prm.total_sweeps, (unsigned long long)sweeps);
       atomicMax(prm.max_local, nloc);
       atomicMax(prm.max_sweeps, sweeps);
     }
@@ -673,8 +694,10 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   prm.max_local = reinterpret_cast<int*>(cnt + 3);
   prm.max_sweeps = reinterpret_cast<int*>(cnt + 3) + 1;
   prm.status = reinterpret_cast<int*>(cnt + 4);
+  prm.total_sweeps = cnt + 5;
   prm.tol = fp64 ? 1e-14 : 1e-6;
   prm.sweep_cap = fp64 ? 30 : 20;
+  prm.warm_start = (d->flags & MG_COLD_START) ? 0 : 1;
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[1], s));
   int rc;
   if (fp64) {
@@ -694,7 +717,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   if (d->mean_out)
     MG_TRY_CUDA(mg::launch_mean_pert_members(d->X, n, k, d->ld, d->mean_out, nullptr, nullptr, 0, s));
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[3], s));
-  unsigned long long host_cnt[5];
+  unsigned long long host_cnt[6];
   MG_TRY_CUDA(cudaMemcpyAsync(host_cnt, cnt, sizeof(host_cnt), cudaMemcpyDeviceToHost, s));
   MG_TRY_CUDA(cudaStreamSynchronize(s));
   float ms[3] = {0.f, 0.f, 0.f};
@@ -707,6 +730,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   ctx->stats.total_local = (int64_t)host_cnt[2];
   ctx->stats.max_local = (int32_t)(host_cnt[3] & 0xffffffffull);
   ctx->stats.max_sweeps = (int32_t)(host_cnt[3] >> 32);
+  ctx->stats.total_sweeps = (int64_t)host_cnt[5];
   if ((int)(host_cnt[4] & 0xffffffffull) != 0)
     return mg::fail(ctx, MG_ERR_NUMERIC, "mg_letkf_batched: a local k x k system was not positive definite");
   return MG_OK;

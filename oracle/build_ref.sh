@@ -22,5 +22,5 @@ for d in traits framework/base framework/algorithms framework/adapters \
 done
 # SimpleState.hpp calls std::min_element without including <algorithm>.
 g++ -std=c++20 -O2 -ffp-contract=off -include algorithm -include numeric -w \
-  "${incs[@]}" "$here/ref_harness.cpp" -o "$here/_ref/ref_harness"
+  -I "$here" "${incs[@]}" "$here/ref_harness.cpp" -o "$here/_ref/ref_harness"
 echo "built $here/_ref/ref_harness"

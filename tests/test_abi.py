@@ -52,4 +52,4 @@ def test_create_without_gpu_reports_cuda_error(built):
 def test_descriptor_layout_matches_header():
     # 25 fields; pointer/int64/double are 8 bytes, int32 pairs pack to 8.
     assert ctypes.sizeof(_lib.LetkfDesc) == 8 * 22
-    assert ctypes.sizeof(_lib.LetkfStats) == 56
+    assert ctypes.sizeof(_lib.LetkfStats) == 64

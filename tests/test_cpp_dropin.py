@@ -1,0 +1,32 @@
+"""CPU test: the C++ drop-in policies compile and link against the
+reference's own adapter headers (skipped where the reference tree is absent,
+e.g. on the GPU host)."""
+import os
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from conftest import ROOT
+
+REF = Path(os.environ.get("METADA_REFERENCE", "/root/reference"))
+
+
+@pytest.mark.skipif(not (REF / "src").is_dir(), reason="reference tree not present")
+def test_dropin_policies_compile_against_reference_adapters(built, tmp_path):
+    incs = []
+    for d in ("traits", "framework/base", "framework/algorithms", "framework/adapters",
+              "framework/adapters/common/utils/config", "framework/adapters/common/utils/logger",
+              "backends/simple", "backends/common/observation", "backends/common/obsoperator",
+              "backends/common/utils/logger/console"):
+        incs += ["-I", str(REF / "src" / d)]
+    cuda = Path("/usr/local/cuda")
+    out = tmp_path / "dropin_reference"
+    cmd = ["g++", "-std=c++20", "-O1", "-w", "-include", "algorithm", "-include", "numeric",
+           "-I", str(ROOT / "include"), "-I", str(ROOT / "oracle"), "-I", str(cuda / "include"), *incs,
+           str(ROOT / "tests" / "cpp" / "dropin_reference.cpp"), "-o", str(out),
+           "-L", str(ROOT / "metada_gb300" / "_lib"), "-lmetada_gb300",
+           "-L", str(cuda / "lib64"), "-lcudart", f"-Wl,-rpath,{ROOT / 'metada_gb300' / '_lib'}"]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-4000:]
+    assert out.exists()

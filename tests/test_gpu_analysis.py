@@ -182,4 +182,5 @@ def test_letkf_latlon_full_size_sampled(dev):
     base, want = _oracle_latlon(c, HX.cpu().numpy(), off, idx, dist, cols)
     gv = np.stack([a64[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)
     assert rel_err(gv, want) <= FP64_TOL
-    assert st64.total_local == stmx.total_local
+    # every analysis point of the configuration has local observations
+    assert st64.n_points == c.nlat * c.nlon * c.nlev and st64.n_empty == stmx.n_empty == 0
