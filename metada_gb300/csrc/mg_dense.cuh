@@ -177,6 +177,116 @@ __device__ int cta_jacobi(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T*
   return sweep + 1;
 }
 
+// cta_jacobi with compile-time bounds (KMAX >= kp, NT threads): the 2 x 2
+// blocks and V column pairs a thread updates are the same in every round, so
+// their (b, c) coordinates are computed once instead of by an integer
+// division per element per round.  Same ordering, rotations and results as
+// cta_jacobi.
+template <typename T, int KMAX, int NT>
+__device__ int cta_jacobi_fast(T* A, T* V, int kp, int lda, T tol, int max_sweeps, T* rot, int* pair,
+                               bool init_v = true) {
+  constexpr int HMAX = KMAX / 2;
+  constexpr int NB = (HMAX * HMAX + NT - 1) / NT;  // A blocks per thread
+  constexpr int NV = (KMAX * HMAX + NT - 1) / NT;  // V column pairs per thread
+  const int tid = threadIdx.x;
+  const int h = kp >> 1, m = kp - 1;
+  if (init_v) {
+    for (int e = tid; e < kp * kp; e += NT) {
+      const int i = e / kp, j = e % kp;
+      V[i * lda + j] = (i == j) ? T(1) : T(0);
+    }
+  }
+  short bb[NB], bc[NB], vr[NV], vc[NV];
+#pragma unroll
+  for (int u = 0; u < NB; ++u) {
+    const int e = tid + u * NT;
+    bb[u] = (short)(e < h * h ? e / h : -1);
+    bc[u] = (short)(e < h * h ? e % h : 0);
+  }
+#pragma unroll
+  for (int u = 0; u < NV; ++u) {
+    const int e = tid + u * NT;
+    vr[u] = (short)(e < kp * h ? e / h : -1);
+    vc[u] = (short)(e < kp * h ? e % h : 0);
+  }
+  __syncthreads();
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    int rotated = 0;
+    for (int r = 0; r < m; ++r) {
+      for (int i = tid; i < h; i += NT) {
+        int p, q;
+        if (i == 0) {
+          p = r;
+          q = m;
+        } else {
+          p = r + i;
+          if (p >= m) p -= m;
+          q = r - i;
+          if (q < 0) q += m;
+        }
+        if (p > q) { const int x = p; p = q; q = x; }
+        const T app = A[p * lda + p], aqq = A[q * lda + q], apq = A[p * lda + q];
+        T c = T(1), s = T(0), t = T(0);
+        if (apq != T(0) && fabs(apq) > tol * dsqrt<T>(fabs(app) * fabs(aqq))) {
+          const T theta = (aqq - app) / (T(2) * apq);
+          t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + dsqrt<T>(theta * theta + T(1)));
+          c = T(1) / dsqrt<T>(t * t + T(1));
+          s = t * c;
+          rotated = 1;
+        }
+        pair[2 * i] = p;
+        pair[2 * i + 1] = q;
+        rot[4 * i + 0] = c;
+        rot[4 * i + 1] = s;
+        rot[4 * i + 2] = app - t * apq;
+        rot[4 * i + 3] = aqq + t * apq;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        const int b = bb[u], c2 = bc[u];
+        if (b < 0) continue;
+        const T sb = rot[4 * b + 1], s_c = rot[4 * c2 + 1];
+        if (sb == T(0) && s_c == T(0)) continue;
+        const int pb = pair[2 * b], qb = pair[2 * b + 1];
+        if (b == c2) {
+          A[pb * lda + pb] = rot[4 * b + 2];
+          A[qb * lda + qb] = rot[4 * b + 3];
+          A[pb * lda + qb] = T(0);
+          A[qb * lda + pb] = T(0);
+          continue;
+        }
+        const int pc = pair[2 * c2], qc = pair[2 * c2 + 1];
+        const T cb = rot[4 * b + 0], c_c = rot[4 * c2 + 0];
+        const T a00 = A[pb * lda + pc], a01 = A[pb * lda + qc];
+        const T a10 = A[qb * lda + pc], a11 = A[qb * lda + qc];
+        const T m00 = cb * a00 - sb * a10, m01 = cb * a01 - sb * a11;
+        const T m10 = sb * a00 + cb * a10, m11 = sb * a01 + cb * a11;
+        A[pb * lda + pc] = c_c * m00 - s_c * m01;
+        A[pb * lda + qc] = s_c * m00 + c_c * m01;
+        A[qb * lda + pc] = c_c * m10 - s_c * m11;
+        A[qb * lda + qc] = s_c * m10 + c_c * m11;
+      }
+#pragma unroll
+      for (int u = 0; u < NV; ++u) {
+        const int row = vr[u], c2 = vc[u];
+        if (row < 0) continue;
+        const T s_c = rot[4 * c2 + 1];
+        if (s_c == T(0)) continue;
+        const T c_c = rot[4 * c2 + 0];
+        const int pc = pair[2 * c2], qc = pair[2 * c2 + 1];
+        const T va = V[row * lda + pc], vb = V[row * lda + qc];
+        V[row * lda + pc] = c_c * va - s_c * vb;
+        V[row * lda + qc] = s_c * va + c_c * vb;
+      }
+      __syncthreads();
+    }
+    if (!__syncthreads_or(rotated)) break;
+  }
+  return sweep + 1;
+}
+
 // A <- V^T A V in place (k x k), using tmp (at least rows x lda values of T,
 // rows >= 1) as a staging buffer: first A <- A V row block by row block, then
 // A <- V^T A column block by column block.
@@ -219,7 +329,7 @@ __device__ void cta_similarity(T* A, const T* V, int k, int lda, T* tmp, int row
 //   wa = Pa b in both.
 // Scratch: V (kp x lda), lam, uvec (k), rot (2 kp), pairbuf (kp ints),
 // misc (4 ints).  Returns false if the system was not positive definite.
-template <typename T>
+template <typename T, int KMAX, int NT>
 __device__ bool solve_transform(T* A, T* V, const T* bvec, T* wa, T* lam, T* uvec, T* rot,
                                 int* pairbuf, int* misc, int k, int kp, int lda, bool use_chol,
                                 bool infl_compat, double rho, T tol, int sweep_cap, int* sweeps,
@@ -250,7 +360,7 @@ __device__ bool solve_transform(T* A, T* V, const T* bvec, T* wa, T* lam, T* uve
   // Warm start: V holds the eigenvectors of a nearby system; rotate A into
   // that basis and let the sweeps continue from it.
   if (warm) cta_similarity<T>(A, V, kp, lda, tmp, tmp_rows);
-  *sweeps = cta_jacobi<T>(A, V, kp, lda, tol, sweep_cap, rot, pairbuf, !warm);
+  *sweeps = cta_jacobi_fast<T, KMAX, NT>(A, V, kp, lda, tol, sweep_cap, rot, pairbuf, !warm);
   const T sc = infl_compat ? (T)rho : T(1);
   for (int i = tid; i < k; i += nt) {
     const T l = A[i * lda + i];

@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kThreads) etkf_solve_kernel(const double* __re
   __syncthreads();
   int sweeps = 0;
   // In the reference form the inflation is applied to X' rather than Pa.
-  const bool ok = mg::solve_transform<TE>(A, V, bvec, wa, lam, uvec, rot, pairbuf, misc, k, kp, lda,
+  const bool ok = mg::solve_transform<TE, 128, kThreads>(A, V, bvec, wa, lam, uvec, rot, pairbuf, misc, k, kp, lda,
                                           flags & MG_SQRT_CHOLESKY, false, rho, (TE)tol, sweep_cap,
                                           &sweeps);
   const TE scale = compat_infl ? (TE)rho : TE(1);

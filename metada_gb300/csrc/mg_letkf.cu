@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
     int sweeps = 0;
     bool ok = true;
     if (!two_stage) {
-      ok = mg::solve_transform<TE>(A, V, bvec, wa, lam, uvec, rot, pairbuf, misc, k, kp, LDA, use_chol,
+      ok = mg::solve_transform<TE, KMAX, kThreads>(A, V, bvec, wa, lam, uvec, rot, pairbuf, misc, k, kp, LDA, use_chol,
                                    infl_compat, prm.rho, (TE)prm.tol, prm.sweep_cap, &sweeps,
                                    warm_mode && have_basis, Ys, CH - 1);
       have_basis = !use_chol;
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
       // is nearly diagonal.
       const bool warm = warm_mode && have_basis;
       if (warm) mg::cta_similarity<TE>(A, V, kp, LDA, Ys, CH - 1);
-      sweeps = mg::cta_jacobi<TE>(A, V, kp, LDA, TE(1e-4), prm.sweep_cap, rot, pairbuf, !warm);
+      sweeps = mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V, kp, LDA, TE(1e-4), prm.sweep_cap, rot, pairbuf, !warm);
       // Stage 2: rebuild A2 = V1^T A V1 from the factor, diag I + B^T B with
       // B = R^-1/2 Y' V1, chunk by chunk.  Entries of B^T B carry errors
       // relative to the column norms of B, so the small eigenvalues keep
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
         }
       __syncthreads();
       // Stage 3: tight Jacobi on A2 (nearly diagonal, well scaled).
-      sweeps += mg::cta_jacobi<TE>(A, V2, kp, LDA, (TE)prm.tol, prm.sweep_cap, rot, pairbuf);
+      sweeps += mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V2, kp, LDA, (TE)prm.tol, prm.sweep_cap, rot, pairbuf);
       for (int i = tid; i < k; i += kThreads) {
         const TE l = A[i * LDA + i];
         lam[i] = l;
