@@ -50,9 +50,9 @@ extern "C" {
 #define MG_UPDATE_COMPAT 8
 #define MG_COMPAT 15
 #define MG_RTPS 16 /* relaxation to prior spread with alpha = rho (no multiplicative inflation) */
-#define MG_COLD_START 32 /* batched LETKF: every eigen-solve from the identity (default: the
-                            levels of a column run in sequence, each warm-started from the
-                            previous level's eigenvectors) */
+#define MG_WARM_START 32 /* batched LETKF: the levels of a column run in sequence, each
+                            eigen-solve warm-started from the previous level's eigenvectors
+                            (default: every eigen-solve starts from the identity) */
 
 /* Arithmetic of the analysis. */
 #define MG_PREC_FP64 0  /* every step in IEEE double */

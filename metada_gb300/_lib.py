@@ -24,7 +24,7 @@ MG_INFL_COMPAT = 4
 MG_UPDATE_COMPAT = 8
 MG_COMPAT = 15
 MG_RTPS = 16
-MG_COLD_START = 32
+MG_WARM_START = 32
 
 MG_PREC_FP64 = 0
 MG_PREC_MIXED = 1

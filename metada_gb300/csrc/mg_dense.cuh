@@ -204,10 +204,10 @@ __device__ int cta_jacobi_fast(T* A, T* V, int kp, int lda, T tol, int max_sweep
     bc[u] = (short)(e < h * h ? e % h : 0);
   }
 #pragma unroll
-  for (int u = 0; u < NV; ++u) {
+  for (int u = 0; u < NV; ++u) {  // rows fastest: a warp touches 32 consecutive rows (distinct banks)
     const int e = tid + u * NT;
-    vr[u] = (short)(e < kp * h ? e / h : -1);
-    vc[u] = (short)(e < kp * h ? e % h : 0);
+    vr[u] = (short)(e < kp * h ? e % kp : -1);
+    vc[u] = (short)(e < kp * h ? e / kp : 0);
   }
   __syncthreads();
   int sweep = 0;

@@ -242,3 +242,4 @@ extern "C" int mg_etkf(mg_context* ctx, double* X, int64_t n, int32_t k, int64_t
   if (precision == MG_PREC_FP64) return run_etkf<double>(ctx, X, n, k, ld, HX, yo, rvar, p, rho, flags, mean_out);
   return run_etkf<float>(ctx, X, n, k, ld, HX, yo, rvar, p, rho, flags, mean_out);
 }
+

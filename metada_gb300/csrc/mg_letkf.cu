@@ -71,18 +71,18 @@ __device__ __forceinline__ T gaspari_cohn(T z) {
          T(2) / (T(3) * z);
 }
 
-// Shared-memory plan of one CTA.  The FP32 (mixed) path with k <= 96 runs a
-// two-stage eigen-solve and needs a second k x k basis (V2) and a chunk of
-// rotated rows (Bc); the other paths do not.
+// Shared-memory plan of one CTA: A and V (k x k, padded rows), one chunk of
+// gathered Y' rows (Ys) and, for the FP32 two-stage eigen-solve (k <= 96),
+// one chunk of rotated rows (Bc); 32-row chunks keep the FP32 plan near
+// 54 KB so four CTAs share an SM.
 template <typename TE, int KMAX>
 struct Plan {
   static constexpr bool TWO_STAGE = sizeof(TE) == 4 && KMAX <= 96;
   static constexpr int LDA = KMAX + 1;
-  static constexpr int CH = (sizeof(TE) == 8 && KMAX > 64) ? 32 : 64;  // list chunk rows
-  static constexpr int NMAT = TWO_STAGE ? 3 : 2;                       // A, V (, V2)
-  static constexpr int NCHUNK = TWO_STAGE ? 2 : 1;                     // Ys (, Bc)
+  static constexpr int CH = 32;                    // list chunk rows
+  static constexpr int NCHUNK = TWO_STAGE ? 2 : 1;  // Ys (, Bc)
   static constexpr size_t te_count() {
-    return (size_t)NMAT * KMAX * LDA + (size_t)NCHUNK * CH * KMAX + 2 * CH + 4 * KMAX + 2 * KMAX +
+    return (size_t)2 * KMAX * LDA + (size_t)NCHUNK * CH * KMAX + 2 * CH + 4 * KMAX + 2 * KMAX +
            kNVarMax * KMAX;
   }
   static constexpr size_t bytes() {
@@ -178,8 +178,7 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TE* A = reinterpret_cast<TE*>(smem_raw);
   TE* V = A + KMAX * LDA;
-  TE* V2 = V + KMAX * LDA;                   // two-stage only
-  TE* Ys = V + (P::NMAT - 1) * KMAX * LDA;   // CH x KMAX
+  TE* Ys = V + KMAX * LDA;                   // CH x KMAX
   TE* Bc = Ys + CH * KMAX;                   // two-stage only: CH x KMAX
   TE* sel_r = Ys + P::NCHUNK * CH * KMAX;    // CH
   TE* sel_d = sel_r + CH;                    // CH
@@ -326,23 +325,17 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
           }
         }
       __syncthreads();
-      // Stage 3: tight Jacobi on A2 (nearly diagonal, well scaled).
-      sweeps += mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V2, kp, LDA, (TE)prm.tol, prm.sweep_cap, rot, pairbuf);
+      // Stage 3: tight Jacobi on A2 (nearly diagonal, well scaled); its
+      // rotations are applied to V1 in place, so V ends as V1 V2 without a
+      // product (and stays orthogonal to rounding).
+      sweeps += mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V, kp, LDA, (TE)prm.tol, prm.sweep_cap, rot, pairbuf,
+                                                        false);
       for (int i = tid; i < k; i += kThreads) {
         const TE l = A[i * LDA + i];
         lam[i] = l;
         if (!(l > TE(0)) || !(l < TE(3.0e38))) atomicExch(prm.status, 1);
       }
       __syncthreads();
-      // V = V1 V2 into A (A2 is no longer needed), then copy back to V.
-      for (int e = tid; e < k * k; e += kThreads) {
-        const int i = e / k, j = e - i * k;
-        TE s = TE(0);
-        for (int m = 0; m < k; ++m) s += V[i * LDA + m] * V2[m * LDA + j];
-        A[i * LDA + j] = s;
-      }
-      __syncthreads();
-      for (int e = tid; e < k * k; e += kThreads) V[(e / k) * LDA + e % k] = A[(e / k) * LDA + e % k];
       have_basis = true;
       const TE sc = infl_compat ? (TE)prm.rho : TE(1);
       __syncthreads();
@@ -697,7 +690,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   prm.total_sweeps = cnt + 5;
   prm.tol = fp64 ? 1e-14 : 1e-6;
   prm.sweep_cap = fp64 ? 30 : 20;
-  prm.warm_start = (d->flags & MG_COLD_START) ? 0 : 1;
+  prm.warm_start = (d->flags & MG_WARM_START) ? 1 : 0;
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[1], s));
   int rc;
   if (fp64) {

@@ -184,3 +184,14 @@ def test_letkf_latlon_full_size_sampled(dev):
     assert rel_err(gv, want) <= FP64_TOL
     # every analysis point of the configuration has local observations
     assert st64.n_points == c.nlat * c.nlon * c.nlev and st64.n_empty == stmx.n_empty == 0
+
+
+def test_letkf_latlon_warm_start_fp64_matches_oracle(dev):
+    """Levels of a column in sequence, each Jacobi warm-started from the
+    previous level's eigenvectors: same analysis to 1e-10."""
+    c = _latlon_case(72, 36, 5, 2, 32, 20_000, 20, case=32)
+    Xd, HX, off, idx, dist, st = _run_latlon(dev, c, _lib.MG_PREC_FP64, flags=_lib.MG_WARM_START)
+    base, want = _oracle_latlon(c, HX.cpu().numpy(), off, idx, dist, np.arange(c.nlat * c.nlon))
+    got = Xd.cpu().numpy()
+    gv = np.stack([got[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)
+    assert rel_err(gv, want) <= FP64_TOL
