@@ -142,6 +142,32 @@ int mg_letkf_compat_grid(mg_context* ctx, double* X, int32_t k, int64_t ld, int3
                          const double* yo, int64_t p, double radius, double rho,
                          double* mean_out);
 
+/* Allocation-free variant of mg_etkf, for callers that cannot allocate device
+ * memory when they run the analysis: code running while its stream is being
+ * captured into a CUDA graph (allocation is not allowed there), real-time
+ * loops whose memory is fixed at start-up, and host frameworks that own every
+ * device allocation through their own pool.  No counterpart in the reference
+ * (its analysis is host code).
+ *  - Same arguments and results as mg_etkf, but no context: work goes on
+ *    `cuda_stream` (a cudaStream_t, NULL = default stream) of the current
+ *    device, and only a status code is returned.
+ *  - Scratch comes from one fixed 32 MiB array that the library reserves on
+ *    every GPU it is loaded on, until the process exits; the call performs no
+ *    cudaMalloc, cudaFree or other allocating call.  A problem needs about
+ *    8*n + s*n*k + 8*(p+1)*(k+2) + 8*B*k*(k+1) + 8*k*k bytes (s = 8 for FP64,
+ *    4 for mixed; B = min(ceil(p/256), 2 x SM count)); larger problems return
+ *    MG_ERR_CAPACITY before any GPU work.
+ *  - The first call on a device looks up the array's device address (once
+ *    per device, with that device current); make that first call before any
+ *    stream capture begins.
+ *  - Every call shares the one array, which keeps the last call's contents:
+ *    calls that overlap on the GPU (other streams, other host threads) race
+ *    and must be serialised by the caller.
+ *  - k <= 112. */
+int mg_etkf_noalloc(void* cuda_stream, double* X, int64_t n, int32_t k, int64_t ld,
+                    const double* HX, const double* yo, const double* rvar, int64_t p,
+                    double rho, int32_t flags, int32_t precision, double* mean_out);
+
 /* Batched LETKF over columns x levels with the obs-space prior of the
  * background (all local analyses independent). */
 typedef struct mg_letkf_desc {

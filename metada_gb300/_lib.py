@@ -116,6 +116,8 @@ _SIGNATURES = {
     "mg_letkf_batched": [c_void_p, POINTER(LetkfDesc)],
     "mg_letkf_last_stats": [c_void_p, POINTER(LetkfStats)],
     "mg_kernel_launches": [c_void_p],
+    "mg_etkf_noalloc": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
+                        c_double, c_int32, c_int32, c_void_p],
 }
 _RESTYPES = {"mg_destroy": None, "mg_last_error": c_char_p, "mg_version": c_char_p, "mg_kernel_launches": c_int64}
 

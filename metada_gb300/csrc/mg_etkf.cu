@@ -17,6 +17,7 @@
 // The reference never recomputes the ensemble mean after the update
 // (ETKF.hpp:190-191); mean_out receives that background mean.
 #include <algorithm>
+#include <mutex>
 
 #include "mg_dense.cuh"
 #include "mg_internal.h"
@@ -243,3 +244,141 @@ extern "C" int mg_etkf(mg_context* ctx, double* X, int64_t n, int32_t k, int64_t
   return run_etkf<float>(ctx, X, n, k, ld, HX, yo, rvar, p, rho, flags, mean_out);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free global ETKF.
+//
+// Some callers cannot allocate device memory at the point where they run the
+// analysis: code executing while a CUDA stream is being captured into a graph
+// (a cudaMalloc there is illegal), real-time loops whose memory budget is
+// fixed at start-up, and host frameworks that own every device allocation
+// through their own pool.  mg_etkf_noalloc serves them: it runs the same
+// kernels as mg_etkf, but its scratch lives in one file-scope device array
+// of fixed size, so the call itself performs no cudaMalloc/cudaFree and no
+// allocating library call.  The array is part of this library's module:
+// every GPU that loads the library keeps kStaticScratchBytes reserved until
+// the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kStaticScratchBytes = size_t(32) << 20;  // 32 MiB
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+struct StaticSetup {
+  std::mutex mu;
+  void* addr[kMaxDevices] = {};
+  int sms[kMaxDevices] = {};
+};
+StaticSetup& static_setup() {
+  static StaticSetup s;
+  return s;
+}
+
+// Device address of g_static_scratch on the current device (and its SM
+// count), looked up once per device.  In host code the array's name is only
+// a host-side stand-in, never a device address.
+cudaError_t static_scratch_for_current_device(void** addr, int* sms) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  StaticSetup& st = static_setup();
+  std::lock_guard<std::mutex> lock(st.mu);
+  if (!st.addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return e;
+    int n = 0;
+    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    st.addr[dev] = p;
+    st.sms[dev] = n;
+  }
+  *addr = st.addr[dev];
+  *sms = st.sms[dev];
+  return cudaSuccess;
+}
+
+template <typename TE>
+int run_etkf_static(cudaStream_t s, double* X, int64_t n, int k, int64_t ld, const double* HX,
+                    const double* yo, const double* rvar, int64_t p, double rho, int flags,
+                    double* mean_out) {
+  void* base = nullptr;
+  int num_sms = 0;
+  if (static_scratch_for_current_device(&base, &num_sms) != cudaSuccess) {
+    cudaGetLastError();
+    return MG_ERR_CUDA;
+  }
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>((p + 255) / 256, 2 * num_sms));
+  const int64_t per_block = (p + nblk - 1) / nblk;
+  mg::Carver cv;
+  cv.reserve<double>(n);
+  cv.reserve<TE>((size_t)n * k);
+  cv.reserve<double>((size_t)(p + 1) * k);
+  cv.reserve<double>(p + 1);
+  cv.reserve<double>(p + 1);
+  cv.reserve<double>((size_t)nblk * k * k);
+  cv.reserve<double>((size_t)nblk * k);
+  cv.reserve<double>((size_t)k * k);
+  cv.reserve<int>(4);
+  if (cv.off > kStaticScratchBytes) return MG_ERR_CAPACITY;
+  cv = mg::Carver{static_cast<char*>(base), 0};
+  double* mean = cv.take<double>(n);
+  TE* Xp = cv.take<TE>((size_t)n * k);
+  double* Y = cv.take<double>((size_t)(p + 1) * k);
+  double* dinn = cv.take<double>(p + 1);
+  double* rinv = cv.take<double>(p + 1);
+  double* Gpart = cv.take<double>((size_t)nblk * k * k);
+  double* bpart = cv.take<double>((size_t)nblk * k);
+  double* T = cv.take<double>((size_t)k * k);
+  int* status = cv.take<int>(4);
+  const bool f64 = sizeof(TE) == 8;
+  auto cuda = [](cudaError_t e) { return e == cudaSuccess ? MG_OK : (cudaGetLastError(), MG_ERR_CUDA); };
+  int rc;
+  if ((rc = cuda(mg::launch_mean_pert_members(X, n, k, ld, mean, f64 ? (double*)Xp : nullptr,
+                                              f64 ? nullptr : (float*)Xp, n, s))) != MG_OK) return rc;
+  if ((rc = cuda(mg::launch_obs_prior(HX, yo, rvar, p, k, Y, nullptr, dinn, rinv, s))) != MG_OK) return rc;
+  cudaError_t e;
+  if (k <= 32) e = launch_gram<double, 32>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s);
+  else if (k <= 64) e = launch_gram<double, 64>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s);
+  else e = launch_gram<double, 128>(Y, rinv, dinn, p, k, nblk, per_block, Gpart, bpart, s);
+  if ((rc = cuda(e)) != MG_OK) return rc;
+  // The status word carries the previous call's value: clear it.
+  if ((rc = cuda(cudaMemsetAsync(status, 0, sizeof(int) * 4, s))) != MG_OK) return rc;
+  const int kp = k + (k & 1);
+  const size_t smem = sizeof(double) * (2 * (size_t)kp * (kp + 1) + 6 * (size_t)kp) + sizeof(int) * (kp + 8) + 64;
+  if (smem > 227 * 1024) return MG_ERR_ARG;
+  if ((rc = cuda(cudaFuncSetAttribute(etkf_solve_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem))) != MG_OK) return rc;
+  etkf_solve_kernel<double><<<1, kThreads, smem, s>>>(Gpart, bpart, nblk, k, flags, rho, 1e-14, 30, T, status);
+  MG_COUNT_LAUNCH();
+  if ((rc = cuda(cudaGetLastError())) != MG_OK) return rc;
+  const size_t usmem = sizeof(TE) * ((size_t)k * k + 32 * (size_t)(k + 1));
+  if ((rc = cuda(cudaFuncSetAttribute(etkf_update_kernel<TE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)usmem))) != MG_OK) return rc;
+  etkf_update_kernel<TE><<<(unsigned)((n + 31) / 32), kThreads, usmem, s>>>(Xp, n, mean, T, n, k, X, ld);
+  MG_COUNT_LAUNCH();
+  if ((rc = cuda(cudaGetLastError())) != MG_OK) return rc;
+  if (mean_out &&
+      (rc = cuda(cudaMemcpyAsync(mean_out, mean, sizeof(double) * n, cudaMemcpyDeviceToDevice, s))) != MG_OK)
+    return rc;
+  int hs = 0;
+  if ((rc = cuda(cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, s))) != MG_OK) return rc;
+  if ((rc = cuda(cudaStreamSynchronize(s))) != MG_OK) return rc;
+  return hs ? MG_ERR_NUMERIC : MG_OK;
+}
+
+}  // namespace
+
+extern "C" int mg_etkf_noalloc(void* stream, double* X, int64_t n, int32_t k, int64_t ld, const double* HX,
+                               const double* yo, const double* rvar, int64_t p, double rho, int32_t flags,
+                               int32_t precision, double* mean_out) {
+  if (!(X && n > 0 && k >= 2 && k <= 112 && ld >= n && p >= 1 && HX && yo && rvar && rho > 0.0))
+    return MG_ERR_ARG;
+  if (precision != MG_PREC_FP64 && precision != MG_PREC_MIXED) return MG_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (precision == MG_PREC_FP64)
+    return run_etkf_static<double>(s, X, n, k, ld, HX, yo, rvar, p, rho, flags, mean_out);
+  return run_etkf_static<float>(s, X, n, k, ld, HX, yo, rvar, p, rho, flags, mean_out);
+}
