@@ -53,6 +53,12 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-points", type=int, default=40000, help="local analyses in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", choices=["latlon", "uneven"], default="latlon",
+                    help="latlon: the headline LETKF configuration; uneven: 512 global-ETKF cases of "
+                         "uneven sizes in one captured graph (reports analyses/s and p50/p99 latency)")
+    ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
+                    help="run one batched LETKF on the reduced 180x90x10x4 case (125k obs) and exit; "
+                         "the case ncu captures of the analysis kernel use")
     return ap.parse_args()
 
 
@@ -274,8 +280,94 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def profile_case(precision_name: str) -> None:
+    """One analysis of a reduced configuration (inputs ~170 MB, above L2; a
+    few hundred MB on the device) for profiler captures."""
+    import torch
+
+    from metada_gb300 import _lib
+    from metada_gb300 import synthetic as syn
+
+    c = syn.latlon_letkf_case(nlon=180, nlat=90, nlev=10, nvar=4, k=64, p=125_000, T=45, case=40)
+    w = Workload(c, torch.device("cuda", 0))
+    st = w.step(_lib.MG_PREC_MIXED if precision_name == "mixed" else _lib.MG_PREC_FP64)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": precision_name, "analyses": st.n_points, "ms_analysis": st.ms_analysis,
+                      "mean_local": st.total_local / st.n_points, "mean_sweeps": st.total_sweeps / st.n_points}))
+
+
+def run_uneven(args) -> None:
+    """512 independent global ETKF analyses (n log-uniform 1k-200k, k in
+    {20,32,48,64,100}, p log-uniform 100-50k, identity interpolation), one
+    autotuned plan replayed as a CUDA graph."""
+    import torch
+
+    from metada_gb300 import _lib
+    from metada_gb300 import kernels as K
+    from metada_gb300 import synthetic as syn
+
+    dev = torch.device("cuda", 0)
+    cases = syn.uneven_batch()
+    out = {}
+    for prec_name, prec in (("mixed", _lib.MG_PREC_MIXED), ("fp64", _lib.MG_PREC_FP64)):
+        dc = []
+        for c in cases:
+            dc.append({"X": torch.tensor(c.X, device=dev), "obs_node": torch.tensor(c.obs_node, device=dev),
+                       "yo": torch.tensor(c.yo, device=dev),
+                       "rvar": torch.full((len(c.yo),), c.sigma_o ** 2, dtype=torch.float64, device=dev),
+                       "rho": c.rho})
+        X0 = [d["X"].clone() for d in dc]
+        b = K.EtkfBatch(dc, flags=0, precision=prec)
+        chunk, mode = b.autotune()
+        times, lat = [], None
+        for it in range(args.warmup + args.steps):
+            for d, x0 in zip(dc, X0):
+                d["X"].copy_(x0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            b.run(graph=True)
+            e1.record()
+            lat = b.finish()
+            if it >= args.warmup:
+                times.append(e0.elapsed_time(e1) / 1e3)
+        t = statistics.mean(times)
+        out[prec_name] = {"analyses_per_s": len(cases) / t, "ms_per_batch": 1e3 * t,
+                          "case_latency_ms_p50": float(np.percentile(lat, 50)),
+                          "case_latency_ms_p99": float(np.percentile(lat, 99)),
+                          "autotuned": {"gram_obs_chunk": chunk, "bucket_mode": mode}}
+        if prec_name == "mixed":
+            Xmx = [d["X"].clone() for d in dc]
+        else:
+            err = 0.0
+            for a, w in zip(Xmx, [d["X"] for d in dc]):
+                ma, mw = a.mean(0), w.mean(0)
+                err = max(err, float(((a - ma) - (w - mw)).abs().max() / (w - mw).abs().max()),
+                          float((ma - mw).abs().max() / mw.abs().max()))
+            out["max_rel_err_mixed_vs_fp64"] = err
+        b.close()
+        del dc, X0
+        torch.cuda.empty_cache()
+    line = {"metric": "uneven-batch global ETKF analyses/s (512 cases, one captured graph)",
+            "value": out["mixed"]["analyses_per_s"], "unit": "analyses/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["mixed"]["ms_per_batch"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 update (FP64 Gram and solve)",
+            "data": "synthetic",
+            "config": {"workload": "512 cases: n log-uniform 1k-200k, k in {20,32,48,64,100}, p log-uniform "
+                                   "100-50k, identity interpolation, sigma_o = 1",
+                       "total_state_values": int(sum(c.X.size for c in cases))},
+            **out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
+    if args.workload == "uneven":
+        run_uneven(args)
+        return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)

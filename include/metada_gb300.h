@@ -91,7 +91,8 @@ int mg_hx_idw4(mg_context* ctx, const double* X, int32_t k, int64_t ld, int32_t 
                double* HX);
 
 /* Bilinear-horizontal / linear-vertical H on a cell-centred lat-lon grid
- * (lon_i = i+0.5 deg, lat_j = -89.5+j deg, integer levels), state layout
+ * (lon_i = (i+0.5) 360/nlon deg, lat_j = -90 + (j+0.5) 180/nlat deg, integer
+ * levels), state layout
  * ((v*nlev + l)*nlat + j)*nlon + i.  No reference counterpart (the reference
  * has only IDW4); used for the lat-lon configurations.  Bit-exact with the
  * oracle's fixed operation order. */
@@ -205,6 +206,44 @@ typedef struct mg_letkf_desc {
  * arithmetic; without them, the Hunt et al. (2007) LETKF with Gaspari-Cohn
  * R-localisation.  Points are scheduled longest-list first. */
 int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* desc);
+
+/* One case of an uneven batch of global ETKF analyses (see mg_etkf_batch_*). */
+typedef struct mg_etkf_case {
+  double* X;               /* members, member-major, updated in place */
+  int64_t n;               /* state values per member */
+  int64_t ld;              /* member stride (>= n) */
+  int32_t k;               /* members, 2..112 */
+  int32_t reserved;
+  const double* HX;        /* p x k obs-space ensemble of the raw members, or NULL */
+  const int64_t* obs_node; /* identity interpolation: state index of each obs (used when HX is NULL) */
+  const double* yo;        /* p */
+  const double* rvar;      /* p */
+  int64_t p;               /* observations */
+  double rho;              /* inflation */
+  double* mean_out;        /* n (background mean) or NULL */
+} mg_etkf_case;
+
+typedef struct mg_etkf_batch mg_etkf_batch;
+
+/* Many independent ETKF::Analyse calls (ETKF.hpp:100-179) of uneven sizes
+ * in one pass.  create() flattens the cases (host array; device pointers
+ * inside) into work-item tables and a workspace; run() only enqueues kernels
+ * (no allocation, no host synchronisation: capturable); launch_graph()
+ * captures run() once into a CUDA graph and replays it; finish() waits,
+ * checks the status and returns each case's completion time after the batch
+ * start in ms (case_ms: host array of ncases, or NULL).  autotune() times
+ * candidate obs chunks for the Gram items and member-count bucket boundaries
+ * on this batch (restoring the members between trials) and keeps the fastest;
+ * it reports the choice (either pointer may be NULL).  flags / precision as
+ * for mg_etkf; cases are analysed in place. */
+int mg_etkf_batch_create(mg_context* ctx, const mg_etkf_case* cases, int32_t ncases, int32_t flags,
+                         int32_t precision, mg_etkf_batch** batch);
+int mg_etkf_batch_autotune(mg_context* ctx, mg_etkf_batch* batch, int32_t* gram_chunk,
+                           int32_t* bucket_mode);
+int mg_etkf_batch_run(mg_context* ctx, mg_etkf_batch* batch);
+int mg_etkf_batch_launch_graph(mg_context* ctx, mg_etkf_batch* batch);
+int mg_etkf_batch_finish(mg_context* ctx, mg_etkf_batch* batch, double* case_ms);
+void mg_etkf_batch_destroy(mg_etkf_batch* batch);
 
 /* Statistics of the last mg_letkf_batched call (host). */
 typedef struct mg_letkf_stats {

@@ -77,6 +77,23 @@ class LetkfDesc(Structure):
     ]
 
 
+class EtkfCase(Structure):
+    _fields_ = [
+        ("X", c_void_p),
+        ("n", c_int64),
+        ("ld", c_int64),
+        ("k", c_int32),
+        ("reserved", c_int32),
+        ("HX", c_void_p),
+        ("obs_node", c_void_p),
+        ("yo", c_void_p),
+        ("rvar", c_void_p),
+        ("p", c_int64),
+        ("rho", c_double),
+        ("mean_out", c_void_p),
+    ]
+
+
 class LetkfStats(Structure):
     _fields_ = [
         ("n_points", c_int64),
@@ -116,10 +133,16 @@ _SIGNATURES = {
     "mg_letkf_batched": [c_void_p, POINTER(LetkfDesc)],
     "mg_letkf_last_stats": [c_void_p, POINTER(LetkfStats)],
     "mg_kernel_launches": [c_void_p],
+    "mg_etkf_batch_create": [c_void_p, c_void_p, c_int32, c_int32, c_int32, POINTER(c_void_p)],
+    "mg_etkf_batch_autotune": [c_void_p, c_void_p, POINTER(c_int32), POINTER(c_int32)],
+    "mg_etkf_batch_run": [c_void_p, c_void_p],
+    "mg_etkf_batch_launch_graph": [c_void_p, c_void_p],
+    "mg_etkf_batch_finish": [c_void_p, c_void_p, c_void_p],
+    "mg_etkf_batch_destroy": [c_void_p],
     "mg_etkf_noalloc": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
                         c_double, c_int32, c_int32, c_void_p],
 }
-_RESTYPES = {"mg_destroy": None, "mg_last_error": c_char_p, "mg_version": c_char_p, "mg_kernel_launches": c_int64}
+_RESTYPES = {"mg_destroy": None, "mg_etkf_batch_destroy": None, "mg_last_error": c_char_p, "mg_version": c_char_p, "mg_kernel_launches": c_int64}
 
 # Entry points the header declares; the CPU tests check every one is exported.
 EXPORTED = tuple(_SIGNATURES)

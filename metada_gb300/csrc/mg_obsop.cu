@@ -61,13 +61,15 @@ __global__ void hx_latlon_kernel(const double* __restrict__ X, int k, int64_t ld
       HX[e] = __longlong_as_double(0x7ff8000000000000LL);
       continue;
     }
-    const double gx = __dsub_rn(olon[o], 0.5);
+    // Fractional grid indices: lon_i = (i + 0.5) dlon, lat_j = -90 + (j + 0.5) dlat.
+    const double dlon = 360.0 / (double)nlon, dlat = 180.0 / (double)nlat;
+    const double gx = __dsub_rn(__ddiv_rn(olon[o], dlon), 0.5);
     const double fxl = floor(gx);
     const double fx = __dsub_rn(gx, fxl);
     long long i0 = (long long)fxl % nlon;
     if (i0 < 0) i0 += nlon;
     const long long i1 = (i0 + 1) % nlon;
-    double gy = __dadd_rn(olat[o], 89.5);
+    double gy = __dsub_rn(__ddiv_rn(__dadd_rn(olat[o], 90.0), dlat), 0.5);
     gy = fmax(0.0, fmin((double)(nlat - 1), gy));
     long long j0 = (long long)floor(gy);
     if (j0 > nlat - 2) j0 = nlat - 2;

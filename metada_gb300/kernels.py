@@ -193,3 +193,70 @@ def letkf_batched(X: torch.Tensor, *, col_base: torch.Tensor, nlev: int, n_var: 
     st = LetkfStats()
     ctx.call("mg_letkf_last_stats", ctypes.byref(st))
     return mean, st
+
+
+class EtkfBatch:
+    """An uneven batch of global ETKF analyses (mg_etkf_batch_*), in place on
+    the members.  `cases` is a list of dicts with keys X (k x n float64 CUDA
+    tensor), yo, rvar (p), and HX (p x k) or obs_node (p int64), rho."""
+
+    def __init__(self, cases, flags: int = _lib.MG_COMPAT, precision: int = _lib.MG_PREC_FP64,
+                 want_mean: bool = False):
+        import numpy as np
+
+        self.cases = cases
+        dev = cases[0]["X"].device
+        self.ctx = context(dev.index)
+        arr = (_lib.EtkfCase * len(cases))()
+        self.means = []
+        for i, c in enumerate(cases):
+            X = c["X"]
+            _need(X, torch.float64, "X")
+            k, n = X.shape
+            a = arr[i]
+            a.X = X.data_ptr()
+            a.n = n
+            a.ld = n
+            a.k = k
+            a.HX = _ptr(c.get("HX")).value
+            a.obs_node = _ptr(c.get("obs_node")).value
+            a.yo = _ptr(c["yo"]).value
+            a.rvar = _ptr(c["rvar"]).value
+            a.p = c["yo"].shape[0]
+            a.rho = float(c.get("rho", 1.0))
+            m = torch.empty(n, dtype=torch.float64, device=dev) if want_mean else None
+            self.means.append(m)
+            a.mean_out = _ptr(m).value
+        self._arr = arr
+        h = c_void_p()
+        self.ctx.call("mg_etkf_batch_create", ctypes.cast(arr, c_void_p), len(cases), int(flags), int(precision),
+                      byref(h))
+        self.handle = h
+        self.case_ms = np.zeros(len(cases))
+
+    def autotune(self) -> tuple[int, int]:
+        ch, mode = ctypes.c_int32(0), ctypes.c_int32(0)
+        self.ctx.call("mg_etkf_batch_autotune", self.handle, byref(ch), byref(mode))
+        return ch.value, mode.value
+
+    def run(self, graph: bool = True) -> None:
+        self.ctx.call("mg_etkf_batch_launch_graph" if graph else "mg_etkf_batch_run", self.handle)
+
+    def finish(self):
+        import numpy as np
+
+        buf = (ctypes.c_double * len(self.cases))()
+        self.ctx.call("mg_etkf_batch_finish", self.handle, ctypes.cast(buf, c_void_p))
+        self.case_ms = np.frombuffer(buf, dtype=np.float64).copy()
+        return self.case_ms
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx.lib.mg_etkf_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass

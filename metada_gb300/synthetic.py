@@ -172,8 +172,8 @@ class LatLonCase:
         return np.full(self.yo.shape[0], self.sigma_o * self.sigma_o)
 
     def col_lat_lon(self) -> tuple[np.ndarray, np.ndarray]:
-        lat = -89.5 + np.arange(self.nlat) * 180.0 / self.nlat
-        lon = 0.5 + np.arange(self.nlon) * 360.0 / self.nlon
+        lat = -90.0 + (np.arange(self.nlat) + 0.5) * 180.0 / self.nlat
+        lon = (np.arange(self.nlon) + 0.5) * 360.0 / self.nlon
         la, lo = np.meshgrid(lat, lon, indexing="ij")
         return la.reshape(-1).copy(), lo.reshape(-1).copy()
 
@@ -201,12 +201,13 @@ def _vertical_ar1(F: np.ndarray, alpha: float) -> np.ndarray:
 
 def trilinear_h(field: np.ndarray, nlon, nlat, nlev, lat, lon, lev, var) -> np.ndarray:
     """The lat-lon operator (same arithmetic as the library's) on one state."""
-    gx = lon - 0.5
+    dlon, dlat = 360.0 / nlon, 180.0 / nlat
+    gx = lon / dlon - 0.5
     fxl = np.floor(gx)
     fx = gx - fxl
     i0 = np.mod(fxl.astype(np.int64), nlon)
     i1 = (i0 + 1) % nlon
-    gy = np.clip(lat + 89.5, 0.0, nlat - 1.0)
+    gy = np.clip((lat + 90.0) / dlat - 0.5, 0.0, nlat - 1.0)
     j0 = np.minimum(np.floor(gy).astype(np.int64), nlat - 2)
     fy = gy - j0
     gz = np.clip(lev, 0.0, nlev - 1.0)
@@ -263,3 +264,33 @@ def write_grid_obs(path, obs_xy: np.ndarray, yo: np.ndarray) -> None:
         f.write("-" * 80 + "\n")
         for (x, y), v in zip(obs_xy, yo):
             f.write(f"0 1 {int(y)} {int(x)} 0.5 0.0 0.0 {v:.17g}\n")
+
+
+@dataclass
+class UnevenCase:
+    X: np.ndarray        # k x n (float32-representable values, stored float64)
+    obs_node: np.ndarray  # p int64 state indices (identity interpolation)
+    yo: np.ndarray
+    sigma_o: float
+    rho: float
+
+
+def uneven_batch(ncases: int = 512, n_range=(1_000, 200_000), k_choices=(20, 32, 48, 64, 100),
+                 p_range=(100, 50_000), sigma_o: float = 1.0, rho: float = 1.05, case: int = 5):
+    """The uneven-batch configuration: state sizes and obs counts log-uniform
+    in the given ranges, member counts uniform in k_choices, obs at seeded
+    state nodes (identity interpolation), sigma_o = 1.  Values are FP32
+    (rounded) stored as float64.  Returns a list of UnevenCase."""
+    g = rng(case, 0)
+    out = []
+    so = float_config(sigma_o)
+    for _ in range(ncases):
+        n = int(np.exp(g.uniform(np.log(n_range[0]), np.log(n_range[1]))))
+        k = int(g.choice(k_choices))
+        p = int(np.exp(g.uniform(np.log(p_range[0]), np.log(p_range[1]))))
+        truth = g.standard_normal(n).astype(np.float32)
+        X = (truth[None, :] + g.standard_normal((k, n)).astype(np.float32)).astype(np.float64)
+        nodes = g.choice(n, size=p, replace=p > n).astype(np.int64)
+        yo = truth[nodes].astype(np.float64) + so * g.standard_normal(p)
+        out.append(UnevenCase(X, nodes, yo, so, float_config(rho)))
+    return out

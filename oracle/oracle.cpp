@@ -201,13 +201,14 @@ void orc_hx_latlon(const double* X, int32_t k, int64_t ld, int32_t nlon, int32_t
 #pragma omp parallel for schedule(static)
   for (int64_t o = 0; o < p; ++o) {
     // Horizontal: periodic in longitude, clamped in latitude.
-    const double gx = obs_lon[o] - 0.5;
+    const double dlon = 360.0 / (double)nlon, dlat = 180.0 / (double)nlat;
+    const double gx = obs_lon[o] / dlon - 0.5;
     const double fxl = std::floor(gx);
     const double fx = gx - fxl;
     long i0 = (long)fxl % nlon;
     if (i0 < 0) i0 += nlon;
     const long i1 = (i0 + 1) % nlon;
-    double gy = obs_lat[o] + 89.5;
+    double gy = (obs_lat[o] + 90.0) / dlat - 0.5;
     gy = std::max(0.0, std::min((double)(nlat - 1), gy));
     long j0 = (long)std::floor(gy);
     if (j0 > nlat - 2) j0 = nlat - 2;

@@ -60,7 +60,8 @@ void orc_hx_idw4(const double* X, int32_t k, int64_t ld, int32_t nx,
                  int64_t p, double* HX);
 
 /* Bilinear-horizontal / linear-vertical interpolation on a regular lat-lon
- * grid with cell-centred nodes (lon_i = i+0.5 deg, lat_j = -89.5+j deg) and
+ * grid with cell-centred nodes (lon_i = (i+0.5) 360/nlon deg,
+ * lat_j = -90 + (j+0.5) 180/nlat deg) and
  * integer level coordinates.  State layout ((v*nlev + l)*nlat + j)*nlon + i.
  * This operator has no counterpart in the reference (it is the one the
  * lat-lon configurations name); it is fixed here so GPU and oracle agree

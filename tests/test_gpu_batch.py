@@ -1,0 +1,86 @@
+"""GPU: the uneven batch of global ETKF analyses (many cases of different
+sizes in one pass, CUDA-graph replay, autotuned chunking) against the
+single-case path and the oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_err
+
+import oracle.bind as ob
+from metada_gb300 import _lib
+from metada_gb300 import kernels as K
+from metada_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+
+def _device_cases(cases, dev, with_hx=False):
+    out = []
+    for c in cases:
+        X = torch.tensor(c.X, device=dev)
+        d = {"X": X, "yo": torch.tensor(c.yo, device=dev),
+             "rvar": torch.full((len(c.yo),), c.sigma_o ** 2, dtype=torch.float64, device=dev), "rho": c.rho}
+        if with_hx:
+            d["HX"] = X[:, torch.tensor(c.obs_node, device=dev)].T.contiguous()
+        else:
+            d["obs_node"] = torch.tensor(c.obs_node, device=dev)
+        out.append(d)
+    return out
+
+
+@pytest.fixture(scope="module")
+def cases():
+    return syn.uneven_batch(ncases=40, n_range=(1_000, 20_000), p_range=(100, 5_000), case=55)
+
+
+@pytest.mark.parametrize("flags", [_lib.MG_COMPAT, 0])
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_fp64_matches_single_case_path(dev, cases, flags, graph):
+    dc = _device_cases(cases, dev)
+    ref = []
+    for c in dc:  # single-case mg_etkf on a copy, HX by the same gather
+        X = c["X"].clone()
+        HX = X[:, c["obs_node"]].T.contiguous()
+        K.etkf(X, HX, c["yo"], c["rvar"], c["rho"], flags=flags, precision=_lib.MG_PREC_FP64)
+        ref.append(X.cpu().numpy())
+    b = K.EtkfBatch(dc, flags=flags, precision=_lib.MG_PREC_FP64)
+    b.run(graph=graph)
+    ms = b.finish()
+    for c, r in zip(dc, ref):
+        assert rel_err(c["X"].cpu().numpy(), r) <= 1e-10
+    assert np.all(ms > 0)
+
+
+def test_batch_reference_semantics_match_oracle(dev, cases):
+    sub = cases[:6]
+    dc = _device_cases(sub, dev, with_hx=True)
+    b = K.EtkfBatch(dc, flags=_lib.MG_COMPAT, precision=_lib.MG_PREC_FP64)
+    b.run(graph=False)
+    b.finish()
+    for c, d in zip(sub, dc):
+        HX = c.X[:, c.obs_node].T.copy()
+        want, _ = ob.etkf_compat(c.X, HX, c.yo, np.full(len(c.yo), c.sigma_o ** 2), c.rho)
+        assert rel_err(d["X"].cpu().numpy(), want) <= 1e-10
+
+
+def test_batch_mixed_within_tolerance_and_graph_replays(dev, cases):
+    d64 = _device_cases(cases, dev)
+    b64 = K.EtkfBatch(d64, flags=0, precision=_lib.MG_PREC_FP64)
+    b64.run(graph=False)
+    b64.finish()
+    dmx = _device_cases(cases, dev)
+    X0 = [c["X"].clone() for c in dmx]
+    bmx = K.EtkfBatch(dmx, flags=0, precision=_lib.MG_PREC_MIXED)
+    chunk, mode = bmx.autotune()
+    assert chunk in (128, 256, 512, 1024, 2048) and mode in (0, 1, 2)
+    for rep in range(2):  # replay the captured graph twice from the same background
+        for c, x0 in zip(dmx, X0):
+            c["X"].copy_(x0)
+        bmx.run(graph=True)
+        bmx.finish()
+        for c, r in zip(dmx, d64):
+            a, w = c["X"].cpu().numpy(), r["X"].cpu().numpy()
+            ma, mw = a.mean(0), w.mean(0)
+            assert rel_err(ma, mw) <= 1e-5
+            assert rel_err(a - ma, w - mw) <= 1e-5
