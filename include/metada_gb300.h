@@ -245,6 +245,51 @@ int mg_etkf_batch_launch_graph(mg_context* ctx, mg_etkf_batch* batch);
 int mg_etkf_batch_finish(mg_context* ctx, mg_etkf_batch* batch, double* case_ms);
 void mg_etkf_batch_destroy(mg_etkf_batch* batch);
 
+/* ---- Learned column observation operator (no reference counterpart) ----
+ * Plain operator: nlev-level columns of T (K) and q to nch channels,
+ *   y_c = sum_l w[c,l] exp(-tau_c sum_{m<=l} q_m) T_l^4 / 1e8   (nch <= 32).
+ * T, q: ncol x nlev row-major; w: nch x nlev; y: ncol x nch (all FP32). */
+int mg_column_op(mg_context* ctx, const float* T, const float* q, int64_t ncol, int32_t nlev,
+                 const float* w, const float* tau, int32_t nch, float* y);
+/* MLP input features of columns: [(T_l - 255)/30, (ln q_l + 9)/2.5, 0 pad]
+ * (ncol x nin, nin >= 2 nlev). */
+int mg_column_features(mg_context* ctx, const float* T, const float* q, int64_t ncol, int32_t nlev,
+                       int32_t nin, float* X);
+/* H of column observations on a member-major state laid out
+ * ((v*nlev + l)*ncol + col), v = 0: T (K), v = 1: ln q.  Obs o observes
+ * channel obs_ch[o] of column obs_col[o]; HX is p x k (FP64). */
+int mg_hx_column(mg_context* ctx, const double* X, int32_t k, int64_t ld, int64_t ncol, int32_t nlev,
+                 const int64_t* obs_col, const int32_t* obs_ch, int64_t p, const float* w,
+                 const float* tau, int32_t nch, double* HX);
+
+/* Surrogate MLP nin -> nh -> nh -> nout, SiLU, BF16 weights and FP32
+ * accumulation, FP32 master parameters trained by Adam on the mean squared
+ * error of standardised outputs ((y - out_shift)/out_scale).  Parameters are
+ * one FP32 vector [W1 (nh x nin), b1, W2 (nh x nh), b2, W3 (nout x nh), b3]. */
+typedef struct mg_mlp mg_mlp;
+int mg_mlp_create(mg_context* ctx, int32_t nin, int32_t nh, int32_t nout, mg_mlp** mlp);
+void mg_mlp_destroy(mg_mlp* mlp);
+int64_t mg_mlp_num_params(const mg_mlp* mlp);
+/* params (device, num_params); out_shift/out_scale (device, nout) or NULL.
+ * Resets the Adam state. */
+int mg_mlp_set_params(mg_context* ctx, mg_mlp* mlp, const float* params, const float* out_shift,
+                      const float* out_scale);
+/* FP32 master parameters, or (bf16_rounded != 0) the BF16 working copy. */
+int mg_mlp_get_params(mg_context* ctx, const mg_mlp* mlp, float* params, int32_t bf16_rounded);
+/* Y (B x nout, standardised) = MLP(X (B x nin)). */
+int mg_mlp_forward(mg_context* ctx, mg_mlp* mlp, const float* X, int64_t B, float* Y);
+/* Gradients of the loss for targets Yt (B x nout, physical units) into grad
+ * (device, num_params, may be NULL); *loss (host, may be NULL). */
+int mg_mlp_gradients(mg_context* ctx, mg_mlp* mlp, const float* X, const float* Yt, int64_t B,
+                     float* grad, float* loss);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on a batch; *loss as above. */
+int mg_mlp_train_step(mg_context* ctx, mg_mlp* mlp, const float* X, const float* Yt, int64_t B,
+                      float lr, float* loss);
+/* mg_hx_column with the surrogate in place of the plain operator. */
+int mg_hx_column_mlp(mg_context* ctx, mg_mlp* mlp, const double* X, int32_t k, int64_t ld,
+                     int64_t ncol, int32_t nlev, const int64_t* obs_col, const int32_t* obs_ch,
+                     int64_t p, double* HX);
+
 /* Statistics of the last mg_letkf_batched call (host). */
 typedef struct mg_letkf_stats {
   int64_t n_points;      /* local analyses run */

@@ -139,10 +139,25 @@ _SIGNATURES = {
     "mg_etkf_batch_launch_graph": [c_void_p, c_void_p],
     "mg_etkf_batch_finish": [c_void_p, c_void_p, c_void_p],
     "mg_etkf_batch_destroy": [c_void_p],
+    "mg_column_op": [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_int32, c_void_p],
+    "mg_column_features": [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_int32, c_void_p],
+    "mg_hx_column": [c_void_p, c_void_p, c_int32, c_int64, c_int64, c_int32, c_void_p, c_void_p, c_int64, c_void_p,
+                     c_void_p, c_int32, c_void_p],
+    "mg_mlp_create": [c_void_p, c_int32, c_int32, c_int32, POINTER(c_void_p)],
+    "mg_mlp_destroy": [c_void_p],
+    "mg_mlp_num_params": [c_void_p],
+    "mg_mlp_set_params": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "mg_mlp_get_params": [c_void_p, c_void_p, c_void_p, c_int32],
+    "mg_mlp_forward": [c_void_p, c_void_p, c_void_p, c_int64, c_void_p],
+    "mg_mlp_gradients": [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, POINTER(ctypes.c_float)],
+    "mg_mlp_train_step": [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, ctypes.c_float, POINTER(ctypes.c_float)],
+    "mg_hx_column_mlp": [c_void_p, c_void_p, c_void_p, c_int32, c_int64, c_int64, c_int32, c_void_p, c_void_p, c_int64,
+                         c_void_p],
     "mg_etkf_noalloc": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
                         c_double, c_int32, c_int32, c_void_p],
 }
-_RESTYPES = {"mg_destroy": None, "mg_etkf_batch_destroy": None, "mg_last_error": c_char_p, "mg_version": c_char_p, "mg_kernel_launches": c_int64}
+_RESTYPES = {"mg_destroy": None, "mg_etkf_batch_destroy": None, "mg_mlp_destroy": None,
+             "mg_mlp_num_params": c_int64, "mg_last_error": c_char_p, "mg_version": c_char_p, "mg_kernel_launches": c_int64}
 
 # Entry points the header declares; the CPU tests check every one is exported.
 EXPORTED = tuple(_SIGNATURES)

@@ -243,20 +243,13 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
         for (int r = 0; r < cnt; ++r) bacc += (Ys[r * KMAX + tid] * sel_r[r]) * sel_d[r];
     });
 
-    // Load this point's perturbations and means (all variables).
-    for (int e = tid; e < prm.n_var * k; e += kThreads) {
-      const int v = e / k, i = e - v * k;
-      Xs[v * KMAX + i] = Xp[(base + (int64_t)v * prm.var_stride) * k + i];
-    }
-    if (tid < prm.n_var) xm[tid] = prm.xmean[base + (int64_t)tid * prm.var_stride];
-
     if (nloc == 0) {
       // LETKF.hpp:167-190: no local obs, x' *= sqrt(rho) (RTPS: unchanged).
-      __syncthreads();
       const double sr = rtps ? 1.0 : sqrt(prm.rho);
       for (int e = tid; e < prm.n_var * k; e += kThreads) {
         const int v = e / k, i = e - v * k;
-        prm.Xa[(base + (int64_t)v * prm.var_stride) * k + i] = xm[v] + (double)Xs[v * KMAX + i] * sr;
+        const int64_t s = base + (int64_t)v * prm.var_stride;
+        prm.Xa[s * k + i] = prm.xmean[s] + (double)Xp[s * k + i] * sr;
       }
       if (tid == 0) atomicAdd(prm.n_empty, 1ull);
       __syncthreads();
@@ -363,8 +356,16 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
     }
     if (!ok && tid == 0) atomicExch(prm.status, 1);
 
-    // ---- update every variable of the point ----
-    for (int e = tid; e < prm.n_var * k; e += kThreads) {
+    // ---- update every variable of the point, kNVarMax at a time ----
+    for (int v0 = 0; v0 < prm.n_var; v0 += kNVarMax) {
+    const int nv = (prm.n_var - v0 < kNVarMax) ? prm.n_var - v0 : kNVarMax;
+    for (int e = tid; e < nv * k; e += kThreads) {
+      const int v = e / k, i = e - v * k;
+      Xs[v * KMAX + i] = Xp[(base + (int64_t)(v0 + v) * prm.var_stride) * k + i];
+    }
+    if (tid < nv) xm[tid] = prm.xmean[base + (int64_t)(v0 + tid) * prm.var_stride];
+    __syncthreads();
+    for (int e = tid; e < nv * k; e += kThreads) {
       const int v = e / k, i = e - v * k;
       const TE* x = Xs + v * KMAX;
       double out;
@@ -382,11 +383,11 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
         out = (xm[v] + (double)inc) + (double)s2;
         if (rtps) Ys[v * KMAX + i] = s2;  // analysis perturbation for the spread
       }
-      prm.Xa[(base + (int64_t)v * prm.var_stride) * k + i] = out;
+      prm.Xa[(base + (int64_t)(v0 + v) * prm.var_stride) * k + i] = out;
     }
     if (rtps && !upd_compat) {
       __syncthreads();
-      if (tid < prm.n_var) {
+      if (tid < nv) {
         double sb = 0.0, sa = 0.0;
         for (int i = 0; i < k; ++i) {
           const double xb = (double)Xs[tid * KMAX + i], xa = (double)Ys[tid * KMAX + i];
@@ -398,10 +399,12 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
         red[tid] = (sa > 0.0) ? prm.rho * (sb - sa) / sa : 0.0;  // factor - 1
       }
       __syncthreads();
-      for (int e = tid; e < prm.n_var * k; e += kThreads) {
+      for (int e = tid; e < nv * k; e += kThreads) {
         const int v = e / k, i = e - v * k;
-        prm.Xa[(base + (int64_t)v * prm.var_stride) * k + i] += red[v] * (double)Ys[v * KMAX + i];
+        prm.Xa[(base + (int64_t)(v0 + v) * prm.var_stride) * k + i] += red[v] * (double)Ys[v * KMAX + i];
       }
+    }
+    __syncthreads();
     }
     if (tid == 0) {
       atomicAdd(prm.total_local, (unsigned long long)nloc);
@@ -592,7 +595,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   if (!ctx) return MG_ERR_ARG;
   MG_CHECK_ARG(d != nullptr, "mg_letkf_batched: null descriptor");
   MG_CHECK_ARG(d->X && d->n > 0 && d->ld >= d->n && d->k >= 2 && d->k <= 128 && d->n_var >= 1 &&
-                   d->n_var <= kNVarMax && d->nlev >= 1 && d->ncol >= 1 && d->col_base &&
+                   d->nlev >= 1 && d->ncol >= 1 && d->col_base &&
                    d->p >= 0 && d->loc_off && (d->p == 0 || (d->HX && d->yo && d->rvar)) &&
                    d->rho > 0.0,
                "mg_letkf_batched: bad descriptor");

@@ -260,3 +260,107 @@ class EtkfBatch:
             self.close()
         except Exception:
             pass
+
+
+# ----------------------------------------------------- column operator ----
+def column_op(T: torch.Tensor, q: torch.Tensor, w: torch.Tensor, tau: torch.Tensor) -> torch.Tensor:
+    """Plain column operator: T, q (ncol x nlev float32) -> y (ncol x nch)."""
+    ncol, nlev = T.shape
+    nch = tau.shape[0]
+    y = torch.empty((ncol, nch), dtype=torch.float32, device=T.device)
+    context(T.device.index).call("mg_column_op", _ptr(T), _ptr(q), ncol, nlev, _ptr(w), _ptr(tau), nch, _ptr(y))
+    return y
+
+
+def column_features(T: torch.Tensor, q: torch.Tensor, nin: int = 64) -> torch.Tensor:
+    ncol, nlev = T.shape
+    X = torch.empty((ncol, nin), dtype=torch.float32, device=T.device)
+    context(T.device.index).call("mg_column_features", _ptr(T), _ptr(q), ncol, nlev, nin, _ptr(X))
+    return X
+
+
+def hx_column(X: torch.Tensor, ncol: int, nlev: int, obs_col: torch.Tensor, obs_ch: torch.Tensor, w: torch.Tensor,
+              tau: torch.Tensor) -> torch.Tensor:
+    """Plain H of column obs on a member-major (T, ln q) state; HX p x k."""
+    _need(X, torch.float64, "X")
+    k, n = X.shape
+    p = obs_col.shape[0]
+    HX = torch.empty((p, k), dtype=torch.float64, device=X.device)
+    context(X.device.index).call("mg_hx_column", _ptr(X), k, n, ncol, nlev, _ptr(obs_col), _ptr(obs_ch), p, _ptr(w),
+                                 _ptr(tau), tau.shape[0], _ptr(HX))
+    return HX
+
+
+class MLP:
+    """The surrogate network (mg_mlp_*): nin -> nh -> nh -> nout, SiLU, BF16
+    weights, FP32 accumulation and master parameters, Adam."""
+
+    def __init__(self, nin: int = 64, nh: int = 256, nout: int = 16, device: int = 0):
+        self.ctx = context(device)
+        self.nin, self.nh, self.nout = nin, nh, nout
+        h = c_void_p()
+        self.ctx.call("mg_mlp_create", nin, nh, nout, byref(h))
+        self.handle = h
+        self.nparam = int(self.ctx.lib.mg_mlp_num_params(h))
+        self.device = torch.device("cuda", device)
+
+    def init_params(self, seed: int = 0) -> torch.Tensor:
+        """Seeded uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights, zero biases."""
+        import numpy as np
+
+        g = np.random.Generator(np.random.PCG64(seed))
+        parts = []
+        for fan_out, fan_in in ((self.nh, self.nin), (self.nh, self.nh), (self.nout, self.nh)):
+            bound = 1.0 / np.sqrt(fan_in)
+            parts.append(g.uniform(-bound, bound, fan_out * fan_in))
+            parts.append(np.zeros(fan_out))
+        P = torch.tensor(np.concatenate(parts), dtype=torch.float32, device=self.device)
+        self.set_params(P)
+        return P
+
+    def set_params(self, P: torch.Tensor, out_shift: torch.Tensor | None = None,
+                   out_scale: torch.Tensor | None = None) -> None:
+        self.ctx.call("mg_mlp_set_params", self.handle, _ptr(P), _ptr(out_shift), _ptr(out_scale))
+
+    def params(self, bf16_rounded: bool = False) -> torch.Tensor:
+        P = torch.empty(self.nparam, dtype=torch.float32, device=self.device)
+        self.ctx.call("mg_mlp_get_params", self.handle, _ptr(P), int(bf16_rounded))
+        return P
+
+    def forward(self, X: torch.Tensor) -> torch.Tensor:
+        Y = torch.empty((X.shape[0], self.nout), dtype=torch.float32, device=X.device)
+        self.ctx.call("mg_mlp_forward", self.handle, _ptr(X), X.shape[0], _ptr(Y))
+        return Y
+
+    def gradients(self, X: torch.Tensor, Yt: torch.Tensor) -> tuple[torch.Tensor, float]:
+        G = torch.empty(self.nparam, dtype=torch.float32, device=X.device)
+        loss = ctypes.c_float(0.0)
+        self.ctx.call("mg_mlp_gradients", self.handle, _ptr(X), _ptr(Yt), X.shape[0], _ptr(G), byref(loss))
+        return G, loss.value
+
+    def train_step(self, X: torch.Tensor, Yt: torch.Tensor, lr: float, want_loss: bool = False) -> float:
+        loss = ctypes.c_float(0.0)
+        self.ctx.call("mg_mlp_train_step", self.handle, _ptr(X), _ptr(Yt), X.shape[0], ctypes.c_float(lr),
+                      byref(loss) if want_loss else None)
+        return loss.value
+
+    def hx_column(self, X: torch.Tensor, ncol: int, nlev: int, obs_col: torch.Tensor,
+                  obs_ch: torch.Tensor) -> torch.Tensor:
+        _need(X, torch.float64, "X")
+        k, n = X.shape
+        p = obs_col.shape[0]
+        HX = torch.empty((p, k), dtype=torch.float64, device=X.device)
+        self.ctx.call("mg_hx_column_mlp", self.handle, _ptr(X), k, n, ncol, nlev, _ptr(obs_col), _ptr(obs_ch), p,
+                      _ptr(HX))
+        return HX
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.ctx.lib.mg_mlp_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -294,3 +294,97 @@ def uneven_batch(ncases: int = 512, n_range=(1_000, 200_000), k_choices=(20, 32,
         yo = truth[nodes].astype(np.float64) + so * g.standard_normal(p)
         out.append(UnevenCase(X, nodes, yo, so, float_config(rho)))
     return out
+
+
+# --------------------------------------------------- column operator case ----
+@dataclass
+class ColumnOperator:
+    w: np.ndarray    # nch x nlev float32
+    tau: np.ndarray  # nch float32
+    nlev: int
+    nch: int
+
+
+def column_operator(nlev: int = 30, nch: int = 16, case: int = 4) -> ColumnOperator:
+    """Seeded weights w[c,l] ~ U(0, 1)/nlev and absorption tau_c log-uniform
+    in [1, 100] of the 16-channel, 30-level column operator."""
+    g = rng(case, 0)
+    w = (g.uniform(0.0, 1.0, (nch, nlev)) / nlev).astype(np.float32)
+    tau = np.exp(g.uniform(np.log(1.0), np.log(100.0), nch)).astype(np.float32)
+    return ColumnOperator(w, tau, nlev, nch)
+
+
+def random_columns(ncol: int, nlev: int = 30, case: int = 4, stream: int = 1):
+    """Independent levels: T ~ U(200, 310) K, q log-uniform in [1e-6, 2e-2]."""
+    g = rng(case, stream)
+    T = g.uniform(200.0, 310.0, (ncol, nlev)).astype(np.float32)
+    q = np.exp(g.uniform(np.log(1e-6), np.log(2e-2), (ncol, nlev))).astype(np.float32)
+    return T, q
+
+
+@dataclass
+class ColumnLetkfCase:
+    nlon: int
+    nlat: int
+    nlev: int
+    op: ColumnOperator
+    truth: np.ndarray      # n = 2 nlev ncol: ((v*nlev + l)*ncol + col), v = 0 T (K), v = 1 ln q
+    X: np.ndarray          # k x n
+    obs_col: np.ndarray    # p int64
+    obs_ch: np.ndarray     # p int32
+    yo: np.ndarray         # p
+    sigma_o: float
+    hsupport_km: float
+    rho: float
+
+    @property
+    def ncol(self) -> int:
+        return self.nlat * self.nlon
+
+    def col_lat_lon(self):
+        lat = -90.0 + (np.arange(self.nlat) + 0.5) * 180.0 / self.nlat
+        lon = (np.arange(self.nlon) + 0.5) * 360.0 / self.nlon
+        la, lo = np.meshgrid(lat, lon, indexing="ij")
+        return la.reshape(-1).copy(), lo.reshape(-1).copy()
+
+
+def column_state_to_Tq(x: np.ndarray, nlev: int, ncol: int):
+    """(T, ln q) state vector -> T, q columns (ncol x nlev float32)."""
+    T = x[: nlev * ncol].reshape(nlev, ncol).T
+    q = np.exp(x[nlev * ncol:].reshape(nlev, ncol).T)
+    return np.ascontiguousarray(T, dtype=np.float32), np.ascontiguousarray(q, dtype=np.float32)
+
+
+def column_letkf_case(nlon: int = 720, nlat: int = 360, nlev: int = 30, k: int = 64, p: int = 200_000,
+                      T_trunc: int = 60, sigma_o: float = 0.05, hsupport_km: float = 800.0, rho: float = 1.05,
+                      case: int = 4) -> ColumnLetkfCase:
+    """Column grid of the learned-operator configuration: (T, ln q) columns of
+    nlev levels on an nlon x nlat grid; truth and members from spherical-
+    harmonic fields (T: 255 K +- 15 K, member spread 2 K; ln q: ln 2e-3 +- 1,
+    spread 0.25), clipped to the operator's ranges; p column obs of seeded
+    channels at seeded columns, y = H(truth) + N(0, sigma_o^2)."""
+    op = column_operator(nlev, 16, case)
+    g = rng(case, 10)
+    F = sh_random_fields((k + 1) * 2 * nlev, nlat, nlon, T_trunc, -3.0, g).reshape(k + 1, 2, nlev, nlat * nlon)
+    F = _vertical_ar1(F.reshape(k + 1, 2, nlev, nlat, nlon), 0.8).reshape(k + 1, 2, nlev, nlat * nlon)
+    Tt = np.clip(255.0 + 15.0 * F[0, 0], 205.0, 305.0)
+    lqt = np.clip(np.log(2e-3) + 1.0 * F[0, 1], np.log(2e-6), np.log(1.5e-2))
+    truth = np.concatenate([Tt.reshape(-1), lqt.reshape(-1)])
+    Tm = np.clip(Tt[None] + 2.0 * F[1:, 0], 200.0, 310.0)
+    lqm = np.clip(lqt[None] + 0.25 * F[1:, 1], np.log(1e-6), np.log(2e-2))
+    X = np.concatenate([Tm.reshape(k, -1), lqm.reshape(k, -1)], axis=1)
+    ncol = nlat * nlon
+    g2 = rng(case, 11)
+    obs_col = g2.integers(0, ncol, p).astype(np.int64)
+    obs_ch = g2.integers(0, 16, p).astype(np.int32)
+    T, q = column_state_to_Tq(truth, nlev, ncol)
+    y = np.zeros(p)
+    cq = np.cumsum(q[obs_col].astype(np.float64), axis=1)
+    Tt4 = T[obs_col].astype(np.float64) ** 4 / 1e8
+    for c in range(16):
+        m = obs_ch == c
+        y[m] = np.sum(op.w[c].astype(np.float64) * np.exp(-float(op.tau[c]) * cq[m]) * Tt4[m], axis=1)
+    so = float_config(sigma_o)
+    yo = y + so * g2.standard_normal(p)
+    return ColumnLetkfCase(nlon, nlat, nlev, op, truth, np.ascontiguousarray(X), obs_col, obs_ch, yo, so,
+                           hsupport_km, float_config(rho))
