@@ -53,9 +53,12 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-points", type=int, default=40000, help="local analyses in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["latlon", "uneven"], default="latlon",
+    ap.add_argument("--workload", choices=["latlon", "uneven", "column"], default="latlon",
                     help="latlon: the headline LETKF configuration; uneven: 512 global-ETKF cases of "
-                         "uneven sizes in one captured graph (reports analyses/s and p50/p99 latency)")
+                         "uneven sizes in one captured graph (reports analyses/s and p50/p99 latency); "
+                         "column: the learned column operator (training, H(x) plain vs surrogate, LETKF)")
+    ap.add_argument("--train-steps", type=int, default=3000, help="column workload: Adam steps")
+    ap.add_argument("--train-batch", type=int, default=4096, help="column workload: columns per Adam step")
     ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
                     help="run one batched LETKF on the reduced 180x90x10x4 case (125k obs) and exit; "
                          "the case ncu captures of the analysis kernel use")
@@ -360,6 +363,124 @@ def run_uneven(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_column(args) -> None:
+    """Learned column operator on the 720 x 360 column grid (30 levels, T and
+    ln q, 64 members, 200k single-channel column obs): train the surrogate
+    (64-padded 60 -> 256 -> 256 -> 16, SiLU, BF16 weights) by Adam on 2M
+    operator-labelled columns, time H(x) of all 12.8M (obs, member) columns
+    through the plain operator and through the surrogate on the tensor cores,
+    and run the LETKF with each H(x)."""
+    import torch
+
+    from metada_gb300 import _lib
+    from metada_gb300 import kernels as K
+    from metada_gb300 import synthetic as syn
+
+    dev = torch.device("cuda", 0)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    op = syn.column_operator()
+    w, tau = torch.tensor(op.w, device=dev), torch.tensor(op.tau, device=dev)
+    # ---- training on 2M columns, shuffled once; one epoch = ncol / batch steps
+    T, q = syn.random_columns(2_000_000, stream=7)
+    Td, qd = torch.tensor(T, device=dev), torch.tensor(q, device=dev)
+    Y = K.column_op(Td, qd, w, tau)
+    Xf = K.column_features(Td, qd, 64)
+    shift, scale = Y.mean(0), Y.std(0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    perm = torch.randperm(Xf.shape[0], device=dev, generator=g)
+    Xs, Ys = Xf[perm].contiguous(), Y[perm].contiguous()
+    mlp = K.MLP(64, 256, 16)
+    mlp.set_params(mlp.init_params(seed=7), shift, scale)
+    B, S = args.train_batch, args.train_steps
+    per_epoch = Xs.shape[0] // B
+    first_loss = mlp.gradients(Xs[:B], Ys[:B])[1]
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    e0.record()
+    for st in range(S):
+        o = (st % per_epoch) * B
+        lr = 2e-3 * 0.5 * (1 + np.cos(np.pi * st / S)) + 1e-5
+        mlp.train_step(Xs[o:o + B], Ys[o:o + B], lr)
+    e1.record()
+    torch.cuda.synchronize()
+    t_train = e0.elapsed_time(e1) / 1e3
+    # held-out columns: surrogate against the plain operator
+    Th, qh = syn.random_columns(200_000, stream=99)
+    Thd, qhd = torch.tensor(Th, device=dev), torch.tensor(qh, device=dev)
+    yh = K.column_op(Thd, qhd, w, tau)
+    ynet = mlp.forward(K.column_features(Thd, qhd, 64)) * scale + shift
+    held_err = float(((ynet - yh).pow(2).mean() / yh.pow(2).mean()).sqrt())
+    # ---- H(x) of 200k obs x 64 members, plain vs surrogate
+    c = syn.column_letkf_case()
+    X0 = torch.tensor(c.X, device=dev)
+    oc, och = torch.tensor(c.obs_col, device=dev), torch.tensor(c.obs_ch, device=dev)
+    k = X0.shape[0]
+    ncols_eval = len(c.obs_col) * k
+
+    def time_it(fn, reps=5):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record()
+        for _ in range(reps):
+            out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b) / 1e3 / reps
+
+    HXp, t_plain = time_it(lambda: K.hx_column(X0, c.ncol, c.nlev, oc, och, w, tau))
+    HXs, t_sur = time_it(lambda: mlp.hx_column(X0, c.ncol, c.nlev, oc, och))
+    hx_err = float(((HXs - HXp).pow(2).mean() / HXp.pow(2).mean()).sqrt())
+    hx_err_sigma = float((HXs - HXp).pow(2).mean().sqrt()) / c.sigma_o
+    flop_col = 2 * (60 * 256 + 256 * 256 + 256 * 16)
+    # ---- the LETKF with each H(x)
+    la, lo = c.col_lat_lon()
+    off, idx, dist = K.select_geo(torch.tensor(la, device=dev), torch.tensor(lo, device=dev),
+                                  torch.tensor(la[c.obs_col], device=dev), torch.tensor(lo[c.obs_col], device=dev),
+                                  c.hsupport_km)
+    yo = torch.tensor(c.yo, device=dev)
+    rvar = torch.full_like(yo, c.sigma_o ** 2)
+    truth = torch.tensor(c.truth, device=dev)
+    nT = c.nlev * c.ncol
+    res = {}
+    for name, HX in (("plain", HXp), ("surrogate", HXs)):
+        X = X0.clone()
+        a, b = ev(), ev()
+        a.record()
+        K.letkf_batched(X, col_base=torch.arange(c.ncol, dtype=torch.int64, device=dev), nlev=1, n_var=2 * c.nlev,
+                        lev_stride=0, var_stride=c.ncol, HX=HX, yo=yo, rvar=rvar, loc_off=off, loc_idx=idx,
+                        loc_dist=dist, hsupport=c.hsupport_km, rho=c.rho, flags=0, precision=_lib.MG_PREC_MIXED,
+                        want_mean=False)
+        b.record()
+        torch.cuda.synchronize()
+        m = X.mean(0)
+        res[name] = {"ms_letkf": a.elapsed_time(b),
+                     "rmse_T_analysis_K": float((m[:nT] - truth[:nT]).pow(2).mean().sqrt()), "mean": m}
+        del X
+    rb = float((X0.mean(0)[:nT] - truth[:nT]).pow(2).mean().sqrt())
+    gain_kept = (rb - res["surrogate"]["rmse_T_analysis_K"]) / (rb - res["plain"]["rmse_T_analysis_K"])
+    line = {"metric": "learned column operator: surrogate H(x) columns/s on the tensor cores (plain beside)",
+            "value": ncols_eval / t_sur, "unit": "columns/s", "n_gpus": 1, "steps": 5, "warmup": 2,
+            "ms_per_step": 1e3 * t_sur, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 x bf16 -> f32 (surrogate); f32 (plain operator)", "data": "synthetic",
+            "config": {"workload": "720x360 column grid, 30 levels (T, ln q), k=64, 200k column obs, 16 channels; "
+                                   "MLP 60(64)->256->256->16 SiLU trained on 2M columns",
+                       "train_steps": S, "train_batch": B},
+            "training": {"s": t_train, "columns_per_s": S * B / t_train, "loss_first": first_loss,
+                         "loss_last": mlp.gradients(Xs[:B], Ys[:B])[1],
+                         "heldout_rel_rms_err": held_err},
+            "hx": {"plain_ms": 1e3 * t_plain, "surrogate_ms": 1e3 * t_sur, "columns": ncols_eval,
+                   "plain_columns_per_s": ncols_eval / t_plain, "surrogate_tflops": ncols_eval * flop_col / t_sur / 1e12,
+                   "surrogate_vs_plain_rel_rms": hx_err, "surrogate_vs_plain_rms_over_sigma_o": hx_err_sigma},
+            "letkf": {"background_rmse_T_K": rb,
+                      **{f"{n}_{key}": v for n, r in res.items() for key, v in r.items() if key != "mean"},
+                      "gain_kept_by_surrogate": gain_kept,
+                      "max_abs_diff_T_K": float((res["plain"]["mean"][:nT] - res["surrogate"]["mean"][:nT]).abs().max())}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.profile_case:
@@ -367,6 +488,9 @@ def main():
         return
     if args.workload == "uneven":
         run_uneven(args)
+        return
+    if args.workload == "column":
+        run_column(args)
         return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":

@@ -251,7 +251,7 @@ void mg_etkf_batch_destroy(mg_etkf_batch* batch);
  * T, q: ncol x nlev row-major; w: nch x nlev; y: ncol x nch (all FP32). */
 int mg_column_op(mg_context* ctx, const float* T, const float* q, int64_t ncol, int32_t nlev,
                  const float* w, const float* tau, int32_t nch, float* y);
-/* MLP input features of columns: [(T_l - 255)/30, (ln q_l + 9)/2.5, 0 pad]
+/* MLP input features of columns: [(T_l - 255)/30, 100 q_l, 0 pad]
  * (ncol x nin, nin >= 2 nlev). */
 int mg_column_features(mg_context* ctx, const float* T, const float* q, int64_t ncol, int32_t nlev,
                        int32_t nin, float* X);
@@ -289,6 +289,15 @@ int mg_mlp_train_step(mg_context* ctx, mg_mlp* mlp, const float* X, const float*
 int mg_hx_column_mlp(mg_context* ctx, mg_mlp* mlp, const double* X, int32_t k, int64_t ld,
                      int64_t ncol, int32_t nlev, const int64_t* obs_col, const int32_t* obs_ch,
                      int64_t p, double* HX);
+
+/* C (M x N, FP32, row-major) = A (M x K) B^T + bias, then SiLU if silu != 0;
+ * A and B are BF16 row-major (K contiguous) device arrays, 16-byte aligned,
+ * 1 <= N <= 256, K a multiple of 8; bias (N) may be NULL.  Runs on the
+ * tensor cores (tcgen05, TMA-staged tiles, FP32 accumulation in tensor
+ * memory); the surrogate's inference layers use the same kernel.  No
+ * counterpart in the reference. */
+int mg_gemm_bf16_tc(mg_context* ctx, const void* A, const void* B, int32_t M, int32_t N, int32_t K,
+                    const float* bias, int32_t silu, float* C);
 
 /* Statistics of the last mg_letkf_batched call (host). */
 typedef struct mg_letkf_stats {

@@ -153,6 +153,7 @@ _SIGNATURES = {
     "mg_mlp_train_step": [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, ctypes.c_float, POINTER(ctypes.c_float)],
     "mg_hx_column_mlp": [c_void_p, c_void_p, c_void_p, c_int32, c_int64, c_int64, c_int32, c_void_p, c_void_p, c_int64,
                          c_void_p],
+    "mg_gemm_bf16_tc": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p],
     "mg_etkf_noalloc": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
                         c_double, c_int32, c_int32, c_void_p],
 }

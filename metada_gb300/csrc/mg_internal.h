@@ -2,6 +2,7 @@
 // libmetada_gb300.so.  Not part of the C-ABI.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -71,6 +72,13 @@ cudaError_t launch_point_major_to_members(const double* P, int64_t n, int k, dou
 cudaError_t launch_obs_prior(const double* HX, const double* yo, const double* rvar, int64_t p,
                              int k, double* Y64, float* Y32, double* d, double* rinv,
                              cudaStream_t s);
+
+// Tensor-core GEMM (tcgen05): C = A B^T + bias, SiLU if act != 0; A (M x K)
+// and B (N x K) BF16 row-major, 16-byte aligned, 1 <= N <= 256, K % 8 == 0.
+// Writes C32 (FP32) and/or C16 (BF16) with leading dimension ldc; *err is
+// set to 1 (not cleared) if a bounded wait gave up.
+int tc_gemm_bf16(mg_context* ctx, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K,
+                 const float* bias, int act, float* C32, __nv_bfloat16* C16, int ldc, int* err);
 
 }  // namespace mg
 

@@ -10,7 +10,8 @@
 // and bias-gradient epilogues, the loss, and Adam.
 //
 // Column features for the MLP: [(T_l - 255)/30 for l < nlev,
-// (ln q_l + 9)/2.5 for l < nlev, 0 ... 0] padded to nin; outputs are
+// 100 q_l for l < nlev, 0 ... 0] padded to nin (the operator depends on q
+// through its running sum, so q enters linearly); outputs are
 // standardised per channel (y - out_shift)/out_scale.
 #include <cuda_bf16.h>
 
@@ -42,6 +43,13 @@ struct mg_mlp {
   float* dA = nullptr;  // nh-wide scratch
   float* dB = nullptr;
   float* loss = nullptr;
+  // BF16 activations of the tensor-core inference path, up to tc_cap rows,
+  // and its error flag (a bounded wait that gave up).
+  int64_t tc_cap = 0;
+  __nv_bfloat16* Xb = nullptr;
+  __nv_bfloat16* H1b = nullptr;
+  __nv_bfloat16* H2b = nullptr;
+  int* tc_err = nullptr;
   // parameter offsets: W1 (nh x nin), b1, W2 (nh x nh), b2, W3 (nout x nh), b3
   int64_t oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0;
 };
@@ -237,7 +245,7 @@ __global__ void column_features_kernel(const float* __restrict__ T, const float*
     const int f = (int)(e - c * nin);
     float v = 0.0f;
     if (f < nlev) v = (T[c * nlev + f] - 255.0f) / 30.0f;
-    else if (f < 2 * nlev) v = (logf(q[c * nlev + f - nlev]) + 9.0f) / 2.5f;
+    else if (f < 2 * nlev) v = 100.0f * q[c * nlev + f - nlev];
     X[e] = v;
   }
 }
@@ -249,7 +257,8 @@ __global__ void column_features_kernel(const float* __restrict__ T, const float*
 __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t ld, int64_t ncol, int nlev,
                                  const int64_t* __restrict__ obs_col, const int32_t* __restrict__ obs_ch,
                                  int64_t p, const float* __restrict__ w, const float* __restrict__ tau,
-                                 double* __restrict__ HX, float* __restrict__ feat, int nin) {
+                                 double* __restrict__ HX, float* __restrict__ feat, int nin,
+                                 __nv_bfloat16* __restrict__ featb = nullptr) {
   const int64_t total = p * k;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t o = e / k;
@@ -264,11 +273,18 @@ __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t l
         acc += w[ch * nlev + l] * expf(-tau[ch] * Q) * ((t * t) * (t * t) / 1e8f);
       }
       HX[e] = acc;
+    } else if (featb) {
+      __nv_bfloat16* f = featb + e * nin;
+      for (int l = 0; l < nlev; ++l) {
+        f[l] = __float2bfloat16_rn(((float)x[(int64_t)l * ncol] - 255.0f) / 30.0f);
+        f[nlev + l] = __float2bfloat16_rn(100.0f * expf((float)x[(int64_t)(nlev + l) * ncol]));
+      }
+      for (int j = 2 * nlev; j < nin; ++j) f[j] = __float2bfloat16_rn(0.0f);
     } else {
       float* f = feat + e * nin;
       for (int l = 0; l < nlev; ++l) {
         f[l] = ((float)x[(int64_t)l * ncol] - 255.0f) / 30.0f;
-        f[nlev + l] = ((float)x[(int64_t)(nlev + l) * ncol] + 9.0f) / 2.5f;
+        f[nlev + l] = 100.0f * expf((float)x[(int64_t)(nlev + l) * ncol]);
       }
       for (int j = 2 * nlev; j < nin; ++j) f[j] = 0.0f;
     }
@@ -325,6 +341,43 @@ int forward(mg_context* ctx, mg_mlp* m, const float* X, int64_t B) {
   MG_TRY_CUDA((gemm<false, false>(s, (int)B, nh, nh, m->H1, nh, W + m->oW2, nh, EpiBiasSilu{P + m->ob2, m->Z2, m->H2, nh})));
   MG_TRY_CUDA((gemm<false, false>(s, (int)B, no, nh, m->H2, nh, W + m->oW3, nh, EpiBias{P + m->ob3, m->Y, no})));
   return MG_OK;
+}
+
+// The tensor-core inference path needs K (nin, nh) a multiple of 8 and
+// N (nh, nout) at most 256; those sizes also keep every weight block of the
+// BF16 parameter vector 16-byte aligned.
+bool tc_shapes_ok(const mg_mlp* m) { return m->nin % 8 == 0 && m->nh % 8 == 0 && m->nh <= 256 && m->nout <= 256; }
+
+int ensure_tc_capacity(mg_context* ctx, mg_mlp* m, int64_t B) {
+  if (B <= m->tc_cap) return MG_OK;
+  void* old[] = {m->Xb, m->H1b, m->H2b};
+  for (void* p : old)
+    if (p) cudaFree(p);
+  m->Xb = m->H1b = m->H2b = nullptr;
+  m->tc_cap = 0;
+  if (cudaMalloc(&m->Xb, sizeof(__nv_bfloat16) * B * m->nin) != cudaSuccess ||
+      cudaMalloc(&m->H1b, sizeof(__nv_bfloat16) * B * m->nh) != cudaSuccess ||
+      cudaMalloc(&m->H2b, sizeof(__nv_bfloat16) * B * m->nh) != cudaSuccess ||
+      (!m->tc_err && cudaMalloc(&m->tc_err, sizeof(int)) != cudaSuccess)) {
+    cudaGetLastError();
+    return mg::fail(ctx, MG_ERR_NOMEM, "mg_mlp: activation allocation failed");
+  }
+  m->tc_cap = B;
+  return MG_OK;
+}
+
+// Inference on the tensor cores: m->Xb (B x nin, BF16) -> m->Y (B x nout,
+// standardised, FP32); hidden activations are rounded to BF16 between layers.
+int forward_tc(mg_context* ctx, mg_mlp* m, int64_t B) {
+  const __nv_bfloat16* W = m->wbf;
+  const float* P = m->master;
+  const int Bi = (int)B, nin = m->nin, nh = m->nh, no = m->nout;
+  int rc;
+  if ((rc = mg::tc_gemm_bf16(ctx, m->Xb, W + m->oW1, Bi, nh, nin, P + m->ob1, 1, nullptr, m->H1b, nh, m->tc_err)))
+    return rc;
+  if ((rc = mg::tc_gemm_bf16(ctx, m->H1b, W + m->oW2, Bi, nh, nh, P + m->ob2, 1, nullptr, m->H2b, nh, m->tc_err)))
+    return rc;
+  return mg::tc_gemm_bf16(ctx, m->H2b, W + m->oW3, Bi, no, nh, P + m->ob3, 0, m->Y, nullptr, no, m->tc_err);
 }
 
 // Gradients of the mean squared (standardised) error into m->grad.
@@ -433,7 +486,8 @@ int mg_mlp_create(mg_context* ctx, int32_t nin, int32_t nh, int32_t nout, mg_mlp
 void mg_mlp_destroy(mg_mlp* m) {
   if (!m) return;
   void* ps[] = {m->master, m->m1, m->m2, m->grad, m->wbf, m->out_shift, m->out_scale, m->loss,
-                m->Z1, m->H1, m->Z2, m->H2, m->Y, m->dY, m->dA, m->dB};
+                m->Z1, m->H1, m->Z2, m->H2, m->Y, m->dY, m->dA, m->dB,
+                m->Xb, m->H1b, m->H2b, m->tc_err};
   for (void* p : ps)
     if (p) cudaFree(p);
   delete m;
@@ -535,6 +589,27 @@ int mg_hx_column_mlp(mg_context* ctx, mg_mlp* m, const double* X, int32_t k, int
   // Columns are run through the network in slices so activations stay bounded.
   const int64_t total = p * k;
   const int64_t slice = std::min<int64_t>(total, (int64_t)1 << 20);
+  if (tc_shapes_ok(m)) {
+    int rc = ensure_capacity(ctx, m, slice);
+    if (rc != MG_OK || (rc = ensure_tc_capacity(ctx, m, slice)) != MG_OK) return rc;
+    MG_TRY_CUDA(cudaMemsetAsync(m->tc_err, 0, sizeof(int), ctx->stream));
+    for (int64_t o0 = 0; o0 < p; o0 += slice / k) {
+      const int64_t np = std::min<int64_t>(p - o0, slice / k);
+      hx_column_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(
+          X, k, ld, ncol, nlev, obs_col + o0, obs_ch + o0, np, nullptr, nullptr, nullptr, nullptr, m->nin, m->Xb);
+      MG_COUNT_LAUNCH();
+      if ((rc = forward_tc(ctx, m, np * k)) != MG_OK) return rc;
+      pick_channel_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(m->Y, np, k, m->nout, obs_ch + o0,
+                                                                          m->out_shift, m->out_scale, HX + o0 * k);
+      MG_COUNT_LAUNCH();
+      MG_TRY_CUDA(cudaGetLastError());
+    }
+    int h = 0;
+    MG_TRY_CUDA(cudaMemcpyAsync(&h, m->tc_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MG_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (h) return mg::fail(ctx, MG_ERR_TIMEOUT, "mg_hx_column_mlp: a tensor-core GEMM wait gave up");
+    return MG_OK;
+  }
   int rc = ensure_capacity(ctx, m, slice);
   if (rc != MG_OK) return rc;
   void* ws = mg::workspace(ctx, sizeof(float) * (size_t)slice * m->nin);

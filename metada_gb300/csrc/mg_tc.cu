@@ -1,0 +1,315 @@
+// Tensor-core GEMM for sm_103a: C = A B^T (+ bias, optional SiLU), A (M x K)
+// and B (N x K) BF16 K-major in global memory, FP32 accumulation in tensor
+// memory, written with inline PTX:
+//   * TMA (cp.async.bulk.tensor.2d) loads 128-row x 64-column tiles of A and
+//     B into shared memory with the 128-byte swizzle, completion tracked by
+//     an mbarrier (arrive.expect_tx / complete_tx);
+//   * one elected thread issues tcgen05.mma.cta_group::1.kind::f16
+//     (M = 128, N = BN, K = 16 per instruction, four per 64-wide K block),
+//     shared-memory descriptors in the SM100 format (SWIZZLE_128B K-major,
+//     SBO = 1024 B), accumulator in TMEM (BN columns allocated per CTA);
+//   * tcgen05.commit signals an mbarrier when the MMAs have drained; two
+//     smem stages let the TMA of block k+1 overlap the MMAs of block k;
+//   * the epilogue: each warp reads its 32 TMEM lanes (rows) with
+//     tcgen05.ld.32x32b, adds the bias, applies SiLU, stores FP32 and/or BF16.
+// Every mbarrier wait is bounded; a CTA that gives up records an error flag,
+// waits (bounded) for its own in-flight copies and MMAs, frees its TMEM and
+// returns, so the host sees MG_ERR_TIMEOUT instead of a hung GPU.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "mg_internal.h"
+
+namespace {
+
+constexpr int kBM = 128;       // rows per CTA tile (MMA M)
+constexpr int kBK = 64;        // K per stage (one 128-byte swizzle row of BF16)
+constexpr int kStages = 2;
+constexpr int kThreads = 128;  // 4 warps: one per 32 TMEM lanes
+constexpr unsigned kSpinLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Bounded wait for the given phase parity; false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  for (unsigned it = 0; it < kSpinLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// SM100 shared-memory matrix descriptor, SWIZZLE_128B, K-major.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);          // start address
+  d |= (uint64_t)1 << 16;                          // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)((1024 >> 4) & 0x3FFF) << 32;     // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                          // descriptor version (SM100)
+  d |= (uint64_t)2 << 61;                          // layout: SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int M,
+                   int N, int K, const float* __restrict__ bias, int act, float* __restrict__ C32,
+                   __nv_bfloat16* __restrict__ C16, int ldc, int* __restrict__ err) {
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "N tile");
+  constexpr uint32_t kABytes = kBM * kBK * 2, kBBytes = BN * kBK * 2;
+  constexpr uint32_t kTmemCols = BN < 32 ? 32 : BN;  // allocation unit: a power of two >= 32
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte aligned stage buffers (required by the 128-byte swizzle).
+  unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sA = base;                        // kStages x kABytes
+  unsigned char* sB = base + kStages * kABytes;    // kStages x kBBytes
+  __shared__ uint64_t full_bar[kStages];   // TMA landed
+  __shared__ uint64_t free_bar[kStages];   // MMAs reading the stage have drained
+  __shared__ uint64_t done_bar;            // all MMAs drained
+  __shared__ uint32_t tmem_base_s;
+  __shared__ int failed;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kBM;
+  const int nk = (K + kBK - 1) / kBK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&free_bar[s], 1);
+    }
+    mbar_init(&done_bar, 1);
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {  // TMEM: BN FP32 columns x 128 lanes
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base_s;
+
+  // Producer + MMA issue: one thread.
+  if (threadIdx.x == 0) {
+    constexpr uint32_t idesc = idesc_bf16_f32(kBM, BN);
+    bool ok = true;
+    // Loads issued per stage and not yet waited for (drained on failure).
+    int pending[kStages] = {};
+    for (int s = 0; s < kStages && s < nk; ++s) {
+      mbar_expect_tx(&full_bar[s], kABytes + kBBytes);
+      tma_load_2d(sA + s * kABytes, &mapA, &full_bar[s], s * kBK, m0);
+      tma_load_2d(sB + s * kBBytes, &mapB, &full_bar[s], s * kBK, 0);
+      pending[s] = 1;
+    }
+    for (int kb = 0; kb < nk && ok; ++kb) {
+      const int s = kb % kStages;
+      const uint32_t phase = (uint32_t)((kb / kStages) & 1);
+      if (!mbar_wait(&full_bar[s], phase)) { ok = false; break; }
+      pending[s] = 0;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t a0 = smem_u32(sA + s * kABytes), b0 = smem_u32(sB + s * kBBytes);
+#pragma unroll
+      for (int kk = 0; kk < kBK / 16; ++kk)
+        mma_bf16(tmem, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idesc,
+                 (kb > 0 || kk > 0) ? 1u : 0u);
+      mma_commit(&free_bar[s]);
+      const int next = kb + kStages;
+      if (next < nk) {
+        // The stage may be refilled once the MMAs just issued have read it.
+        if (!mbar_wait(&free_bar[s], phase)) { ok = false; break; }
+        mbar_expect_tx(&full_bar[s], kABytes + kBBytes);
+        tma_load_2d(sA + s * kABytes, &mapA, &full_bar[s], next * kBK, m0);
+        tma_load_2d(sB + s * kBBytes, &mapB, &full_bar[s], next * kBK, 0);
+        pending[s] = 1;
+      }
+    }
+    mma_commit(&done_bar);
+    if (!ok) {
+      failed = 1;
+      // Give copies still in flight into this CTA's shared memory a bounded
+      // chance to land before the CTA exits.
+      for (int s = 0; s < kStages; ++s)
+        if (pending[s]) mbar_wait(&full_bar[s], 0), mbar_wait(&full_bar[s], 1);
+    }
+  }
+  __syncthreads();
+  // Everyone waits for the accumulator (bounded); on failure also drain.
+  const bool ready = mbar_wait(&done_bar, 0);
+  // One CTA-wide decision, so each warp reaches tcgen05.ld converged.
+  const int bad = __syncthreads_or(!ready || failed);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (bad) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+  } else {
+    const int row = m0 + warp * 32 + lane;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t v[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+            "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+            "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+            "=r"(v[30]), "=r"(v[31])
+          : "r"(trow + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int n = c0 + j;
+          if (n < N) {
+            float x = __uint_as_float(v[j]) + (bias ? bias[n] : 0.0f);
+            if (act) x = silu_f(x);
+            if (C32) C32[(int64_t)row * ldc + n] = x;
+            if (C16) C16[(int64_t)row * ldc + n] = __float2bfloat16_rn(x);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
+// ---- host side: tensor maps through the driver entry point ----
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// rows x cols BF16 row-major (cols contiguous), box box_rows x 64, 128-byte swizzle.
+bool make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t cols, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+int launch(mg_context* ctx, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int K, const float* bias,
+           int act, float* C32, __nv_bfloat16* C16, int ldc, int* err) {
+  const size_t smem = 1024 + (size_t)kStages * (kBM * kBK * 2 + BN * kBK * 2);
+  MG_TRY_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  tc_gemm_kernel<BN><<<(unsigned)((M + kBM - 1) / kBM), kThreads, smem, ctx->stream>>>(ma, mb, M, N, K, bias, act, C32,
+                                                                                       C16, ldc, err);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+}  // namespace
+
+namespace mg {
+
+// Internal entry used by the MLP inference path as well.
+int tc_gemm_bf16(mg_context* ctx, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K,
+                 const float* bias, int act, float* C32, __nv_bfloat16* C16, int ldc, int* err) {
+  if (N < 1 || N > 256 || K % 8 != 0 || M <= 0 || K <= 0)
+    return fail(ctx, MG_ERR_ARG, "tensor-core GEMM: need 1 <= N <= 256, K > 0, K % 8 == 0");
+  if (((uintptr_t)A | (uintptr_t)B) & 15)
+    return fail(ctx, MG_ERR_ARG, "tensor-core GEMM: operands must be 16-byte aligned");
+  CUtensorMap ma, mb;
+  const int bn = N <= 16 ? 16 : N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
+  if (!make_map(&ma, A, M, K, kBM) || !make_map(&mb, B, N, K, bn))
+    return fail(ctx, MG_ERR_CUDA, "tensor-core GEMM: cuTensorMapEncodeTiled failed");
+  switch (bn) {
+    case 16: return launch<16>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
+    case 32: return launch<32>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
+    case 64: return launch<64>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
+    case 128: return launch<128>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
+    default: return launch<256>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
+  }
+}
+
+}  // namespace mg
+
+extern "C" int mg_gemm_bf16_tc(mg_context* ctx, const void* A, const void* B, int32_t M, int32_t N, int32_t K,
+                               const float* bias, int32_t silu, float* C) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(A && B && C, "mg_gemm_bf16_tc: null operand");
+  int* err = static_cast<int*>(mg::workspace(ctx, 256));
+  if (!err) return MG_ERR_NOMEM;
+  MG_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  const int rc = mg::tc_gemm_bf16(ctx, static_cast<const __nv_bfloat16*>(A), static_cast<const __nv_bfloat16*>(B), M,
+                                  N, K, bias, silu, C, nullptr, N, err);
+  if (rc != MG_OK) return rc;
+  int h = 0;
+  MG_TRY_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MG_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (h) return mg::fail(ctx, MG_ERR_TIMEOUT, "mg_gemm_bf16_tc: a bounded mbarrier wait gave up");
+  return MG_OK;
+}

@@ -262,6 +262,20 @@ class EtkfBatch:
             pass
 
 
+# ------------------------------------------------ tensor-core GEMM ----
+def gemm_bf16_tc(A: torch.Tensor, B: torch.Tensor, bias: torch.Tensor | None = None,
+                 silu: bool = False) -> torch.Tensor:
+    """C = A B^T (+ bias, SiLU) on the tensor cores: A (M x K) and B (N x K)
+    BF16, C FP32."""
+    _need(A, torch.bfloat16, "A")
+    _need(B, torch.bfloat16, "B")
+    M, K = A.shape
+    N = B.shape[0]
+    C = torch.empty((M, N), dtype=torch.float32, device=A.device)
+    context(A.device.index).call("mg_gemm_bf16_tc", _ptr(A), _ptr(B), M, N, K, _ptr(bias), int(silu), _ptr(C))
+    return C
+
+
 # ----------------------------------------------------- column operator ----
 def column_op(T: torch.Tensor, q: torch.Tensor, w: torch.Tensor, tau: torch.Tensor) -> torch.Tensor:
     """Plain column operator: T, q (ncol x nlev float32) -> y (ncol x nch)."""

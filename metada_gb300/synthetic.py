@@ -360,18 +360,21 @@ def column_letkf_case(nlon: int = 720, nlat: int = 360, nlev: int = 30, k: int =
                       case: int = 4) -> ColumnLetkfCase:
     """Column grid of the learned-operator configuration: (T, ln q) columns of
     nlev levels on an nlon x nlat grid; truth and members from spherical-
-    harmonic fields (T: 255 K +- 15 K, member spread 2 K; ln q: ln 2e-3 +- 1,
-    spread 0.25), clipped to the operator's ranges; p column obs of seeded
+    harmonic fields (T: 255 K +- 15 K; ln q: ln 2e-3 +- 1), clipped to the
+    operator's ranges.  The background mean is the truth plus one error field
+    (T 2 K, ln q 0.25) and the members add centred draws of the same size, so
+    the spread matches the mean's actual error.  p column obs of seeded
     channels at seeded columns, y = H(truth) + N(0, sigma_o^2)."""
     op = column_operator(nlev, 16, case)
     g = rng(case, 10)
-    F = sh_random_fields((k + 1) * 2 * nlev, nlat, nlon, T_trunc, -3.0, g).reshape(k + 1, 2, nlev, nlat * nlon)
-    F = _vertical_ar1(F.reshape(k + 1, 2, nlev, nlat, nlon), 0.8).reshape(k + 1, 2, nlev, nlat * nlon)
+    F = sh_random_fields((k + 2) * 2 * nlev, nlat, nlon, T_trunc, -3.0, g).reshape(k + 2, 2, nlev, nlat * nlon)
+    F = _vertical_ar1(F.reshape(k + 2, 2, nlev, nlat, nlon), 0.8).reshape(k + 2, 2, nlev, nlat * nlon)
     Tt = np.clip(255.0 + 15.0 * F[0, 0], 205.0, 305.0)
     lqt = np.clip(np.log(2e-3) + 1.0 * F[0, 1], np.log(2e-6), np.log(1.5e-2))
     truth = np.concatenate([Tt.reshape(-1), lqt.reshape(-1)])
-    Tm = np.clip(Tt[None] + 2.0 * F[1:, 0], 200.0, 310.0)
-    lqm = np.clip(lqt[None] + 0.25 * F[1:, 1], np.log(1e-6), np.log(2e-2))
+    P = F[2:] - F[2:].mean(axis=0, keepdims=True)
+    Tm = np.clip(Tt[None] + 2.0 * (F[1, 0][None] + P[:, 0]), 200.0, 310.0)
+    lqm = np.clip(lqt[None] + 0.25 * (F[1, 1][None] + P[:, 1]), np.log(1e-6), np.log(2e-2))
     X = np.concatenate([Tm.reshape(k, -1), lqm.reshape(k, -1)], axis=1)
     ncol = nlat * nlon
     g2 = rng(case, 11)

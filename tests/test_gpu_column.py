@@ -69,7 +69,7 @@ def test_mlp_gradients_match_oracle(dev):
     assert rel_err(Y, wY) <= 1e-4
 
 
-def _train(dev, op, ncol=200_000, steps=1500, batch=4096, seed=7):
+def _train(dev, op, ncol=200_000, steps=4000, batch=4096, seed=7):
     T, q = syn.random_columns(ncol, stream=seed)
     Td, qd = torch.tensor(T, device=dev), torch.tensor(q, device=dev)
     w, tau = torch.tensor(op.w, device=dev), torch.tensor(op.tau, device=dev)
