@@ -57,7 +57,7 @@ def parse():
                     help="latlon: the headline LETKF configuration; uneven: 512 global-ETKF cases of "
                          "uneven sizes in one captured graph (reports analyses/s and p50/p99 latency); "
                          "column: the learned column operator (training, H(x) plain vs surrogate, LETKF)")
-    ap.add_argument("--train-steps", type=int, default=3000, help="column workload: Adam steps")
+    ap.add_argument("--train-steps", type=int, default=6000, help="column workload: Adam steps")
     ap.add_argument("--train-batch", type=int, default=4096, help="column workload: columns per Adam step")
     ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
                     help="run one batched LETKF on the reduced 180x90x10x4 case (125k obs) and exit; "

@@ -287,6 +287,36 @@ __device__ int cta_jacobi_fast(T* A, T* V, int kp, int lda, T tol, int max_sweep
   return sweep + 1;
 }
 
+// One Newton-Schulz step towards the orthogonal polar factor of V (k x k):
+// V <- V (3I - V^T V) / 2.  Rotations accumulated in FP32 leave V about
+// sweeps * k * eps away from orthogonal; one step squares that deviation.
+// M (k x lda) is scratch; tmp holds `rows` rows of KMAX values.
+template <typename T, int KMAX>
+__device__ void cta_reorthonormalize(T* V, int k, int lda, T* M, T* tmp, int rows) {
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int i = e / k, j = e - i * k;
+    T s = T(0);
+    for (int m = 0; m < k; ++m) s += V[m * lda + i] * V[m * lda + j];
+    M[i * lda + j] = ((i == j) ? T(1.5) : T(0)) - T(0.5) * s;
+  }
+  __syncthreads();
+  for (int r0 = 0; r0 < k; r0 += rows) {
+    const int nr = (k - r0 < rows) ? k - r0 : rows;
+    for (int e = threadIdx.x; e < nr * k; e += blockDim.x) {
+      const int r = e / k, j = e - r * k;
+      tmp[r * KMAX + j] = V[(r0 + r) * lda + j];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nr * k; e += blockDim.x) {
+      const int r = e / k, j = e - r * k;
+      T s = T(0);
+      for (int m = 0; m < k; ++m) s += tmp[r * KMAX + m] * M[m * lda + j];
+      V[(r0 + r) * lda + j] = s;
+    }
+    __syncthreads();
+  }
+}
+
 // A <- V^T A V in place (k x k), using tmp (at least rows x lda values of T,
 // rows >= 1) as a staging buffer: first A <- A V row block by row block, then
 // A <- V^T A column block by column block.

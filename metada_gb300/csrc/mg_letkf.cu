@@ -30,6 +30,10 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kNVarMax = 8;
+// Off-diagonal threshold of the loose first Jacobi stage (relative to
+// sqrt(a_pp a_qq)); the first-order finish below leaves a remainder of
+// about k * kStage1Tol^2.
+constexpr double kStage1Tol = 3e-4;
 
 struct LetkfParams {
   int k, kp, n_var, nlev;
@@ -172,7 +176,7 @@ __device__ __forceinline__ void gram_rows(TE (&acc)[R][R], const TE* M, const TE
 }
 
 template <typename TE, int KMAX>
-__global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm) {
+__global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 : 1) letkf_batched_kernel(LetkfParams prm) {
   using P = Plan<TE, KMAX>;
   constexpr int LDA = P::LDA, CH = P::CH, R = KMAX / 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -284,7 +288,10 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
       // is nearly diagonal.
       const bool warm = warm_mode && have_basis;
       if (warm) mg::cta_similarity<TE>(A, V, kp, LDA, Ys, CH - 1);
-      sweeps = mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V, kp, LDA, TE(1e-4), prm.sweep_cap, rot, pairbuf, !warm);
+      sweeps = mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V, kp, LDA, TE(kStage1Tol), prm.sweep_cap, rot, pairbuf,
+                                                       !warm);
+      // V1 back to orthogonal (A is free until the rebuild below).
+      mg::cta_reorthonormalize<TE, KMAX>(V, kp, LDA, A, Ys, CH);
       // Stage 2: rebuild A2 = V1^T A V1 from the factor, diag I + B^T B with
       // B = R^-1/2 Y' V1, chunk by chunk.  Entries of B^T B carry errors
       // relative to the column norms of B, so the small eigenvalues keep
@@ -318,11 +325,15 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
           }
         }
       __syncthreads();
-      // Stage 3: tight Jacobi on A2 (nearly diagonal, well scaled); its
-      // rotations are applied to V1 in place, so V ends as V1 V2 without a
-      // product (and stays orthogonal to rounding).
-      sweeps += mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V, kp, LDA, (TE)prm.tol, prm.sweep_cap, rot, pairbuf,
-                                                        false);
+      // Stage 3: A2 = D + E is nearly diagonal (|E_ij| <= kStage1Tol
+      // sqrt(d_i d_j) after stage 1, V1 orthonormal to FP32 rounding), so
+      // f(A2) for f = x^-1/2 and x^-1 is taken to first order by the
+      // Daleckii-Krein formula,
+      //   f(D + E) = f(D) + [E_ij f[d_i, d_j]] + O(|E|^2),
+      // with the divided differences in closed form (no cancellation):
+      //   x^-1/2: -1 / (s_i s_j (s_i + s_j)), s = sqrt(d);  x^-1: -1 / (d_i d_j).
+      // The second-order remainder is ~k kStage1Tol^2 relative (a few 1e-6
+      // at k = 64), and no tight Jacobi is needed.
       for (int i = tid; i < k; i += kThreads) {
         const TE l = A[i * LDA + i];
         lam[i] = l;
@@ -331,28 +342,59 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
       __syncthreads();
       have_basis = true;
       const TE sc = infl_compat ? (TE)prm.rho : TE(1);
-      __syncthreads();
-      for (int i = tid; i < k; i += kThreads) {  // u = diag(sc / lam) V^T b
+      for (int i = tid; i < k; i += kThreads) {  // u = V1^T b
         TE s = TE(0);
         for (int j = 0; j < k; ++j) s += V[j * LDA + i] * bvec[j];
-        uvec[i] = s * sc / lam[i];
+        uvec[i] = s;
       }
       __syncthreads();
-      for (int i = tid; i < k; i += kThreads) {  // wa = V u
+      TE* gvec = rot;  // k values; the Jacobi rotation buffer is free now
+      for (int i = tid; i < k; i += kThreads) {  // g = (sc x^-1)(A2) u
+        TE s = uvec[i];
+        for (int j = 0; j < k; ++j)
+          if (j != i) s -= A[i * LDA + j] * (uvec[j] / lam[j]);
+        gvec[i] = s * sc / lam[i];
+      }
+      __syncthreads();
+      for (int i = tid; i < k; i += kThreads) {  // wa = V1 g
         TE s = TE(0);
-        for (int m = 0; m < k; ++m) s += V[i * LDA + m] * uvec[m];
+        for (int m = 0; m < k; ++m) s += V[i * LDA + m] * gvec[m];
         wa[i] = s;
       }
-      __syncthreads();
-      for (int i = tid; i < k; i += kThreads) uvec[i] = mg::dsqrt<TE>(TE(k - 1) * sc / lam[i]);
-      __syncthreads();
-      for (int e = tid; e < k * k; e += kThreads) {  // W = V diag(sqrt((k-1) sc / lam)) V^T
+      // A <- Wb = (c x^-1/2)(A2), c = sqrt((k-1) sc); W = V1 Wb V1^T is never
+      // formed: the update applies X' V1, then Wb, then V1^T.
+      const TE cw = mg::dsqrt<TE>(TE(k - 1) * sc);
+      for (int e = tid; e < k * k; e += kThreads) {
         const int i = e / k, j = e - i * k;
-        TE s = TE(0);
-        for (int m = 0; m < k; ++m) s += V[i * LDA + m] * uvec[m] * V[j * LDA + m];
-        A[i * LDA + j] = s;
+        const TE si = mg::dsqrt<TE>(lam[i]);
+        if (i == j) {
+          A[i * LDA + i] = cw / si;
+        } else {
+          const TE sj = mg::dsqrt<TE>(lam[j]);
+          A[i * LDA + j] = -cw * A[i * LDA + j] / (si * sj * (si + sj));
+        }
       }
       __syncthreads();
+      if (upd_compat) {  // row sums of W = V1 Wb V1^T 1, kept in uvec
+        for (int i = tid; i < k; i += kThreads) {
+          TE s = TE(0);
+          for (int m = 0; m < k; ++m) s += V[m * LDA + i];
+          gvec[i] = s;  // V1^T 1
+        }
+        __syncthreads();
+        for (int i = tid; i < k; i += kThreads) {
+          TE s = TE(0);
+          for (int m = 0; m < k; ++m) s += A[i * LDA + m] * gvec[m];
+          lam[i] = s;  // Wb V1^T 1 (lam is not needed any more)
+        }
+        __syncthreads();
+        for (int i = tid; i < k; i += kThreads) {
+          TE s = TE(0);
+          for (int m = 0; m < k; ++m) s += V[i * LDA + m] * lam[m];
+          uvec[i] = s;
+        }
+        __syncthreads();
+      }
     }
     if (!ok && tid == 0) atomicExch(prm.status, 1);
 
@@ -365,6 +407,42 @@ __global__ void __launch_bounds__(kThreads) letkf_batched_kernel(LetkfParams prm
     }
     if (tid < nv) xm[tid] = prm.xmean[base + (int64_t)(v0 + tid) * prm.var_stride];
     __syncthreads();
+    if (two_stage) {  // P = ((X' V1) Wb) V1^T, two nv x KMAX buffers in Bc
+      TE* P1 = Bc;
+      TE* P2 = Bc + kNVarMax * KMAX;
+      if (!upd_compat) {
+        for (int e = tid; e < nv * k; e += kThreads) {
+          const int v = e / k, j = e - v * k;
+          TE s = TE(0);
+          for (int m = 0; m < k; ++m) s += Xs[v * KMAX + m] * V[m * LDA + j];
+          P1[v * KMAX + j] = s;
+        }
+        __syncthreads();
+        for (int e = tid; e < nv * k; e += kThreads) {
+          const int v = e / k, j = e - v * k;
+          TE s = TE(0);
+          for (int m = 0; m < k; ++m) s += P1[v * KMAX + m] * A[m * LDA + j];
+          P2[v * KMAX + j] = s;
+        }
+        __syncthreads();
+      }
+      for (int e = tid; e < nv * k; e += kThreads) {
+        const int v = e / k, i = e - v * k;
+        const TE* x = Xs + v * KMAX;
+        double out;
+        if (upd_compat) {  // xa_i = (xm + x'_i wa_i) + x'_i sum_j W_ij, LETKF.hpp:232-238
+          const TE xp = x[i];
+          out = (xm[v] + (double)(xp * wa[i])) + (double)(xp * uvec[i]);
+        } else {
+          TE inc = TE(0), s2 = TE(0);
+          for (int j = 0; j < k; ++j) inc += x[j] * wa[j];
+          for (int m = 0; m < k; ++m) s2 += P2[v * KMAX + m] * V[i * LDA + m];
+          out = (xm[v] + (double)inc) + (double)s2;
+          if (rtps) Ys[v * KMAX + i] = s2;  // analysis perturbation for the spread
+        }
+        prm.Xa[(base + (int64_t)(v0 + v) * prm.var_stride) * k + i] = out;
+      }
+    } else
     for (int e = tid; e < nv * k; e += kThreads) {
       const int v = e / k, i = e - v * k;
       const TE* x = Xs + v * KMAX;
