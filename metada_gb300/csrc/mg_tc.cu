@@ -192,8 +192,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (bad) {
     if (threadIdx.x == 0) atomicExch(err, 1);
   } else {
-    const int row = m0 + warp * 32 + lane;
+    // Each warp stages its 32 rows x 32 columns through shared memory (the
+    // operand stages are free once the MMAs have drained), so the global
+    // stores are row segments: 128 B (FP32) or two 64 B rows (BF16) per
+    // warp instruction.
+    float* stg = reinterpret_cast<float*>(base) + warp * (32 * 33);
+    const int rbase = m0 + warp * 32;
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    const bool pairs16 = C16 && (ldc % 2 == 0) && (((uintptr_t)C16 & 3) == 0);
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 32) {
       uint32_t v[32];
@@ -207,18 +213,43 @@ __global__ void __launch_bounds__(kThreads, 1)
             "=r"(v[30]), "=r"(v[31])
           : "r"(trow + (uint32_t)c0));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < M) {
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int n = c0 + j;
-          if (n < N) {
-            float x = __uint_as_float(v[j]) + (bias ? bias[n] : 0.0f);
-            if (act) x = silu_f(x);
-            if (C32) C32[(int64_t)row * ldc + n] = x;
-            if (C16) C16[(int64_t)row * ldc + n] = __float2bfloat16_rn(x);
+      for (int j = 0; j < 32; ++j) {
+        const int n = c0 + j;
+        float x = __uint_as_float(v[j]) + ((bias && n < N) ? bias[n] : 0.0f);
+        if (act) x = silu_f(x);
+        stg[lane * 33 + j] = x;
+      }
+      __syncwarp();
+      if (C32) {
+        const int n = c0 + lane;
+#pragma unroll 4
+        for (int r = 0; r < 32; ++r) {
+          const int row = rbase + r;
+          if (row < M && n < N) C32[(int64_t)row * ldc + n] = stg[r * 33 + lane];
+        }
+      }
+      if (C16) {
+        if (pairs16) {
+          const int half = lane >> 4, cc = (lane & 15) * 2, n = c0 + cc;
+#pragma unroll 4
+          for (int r = 0; r < 32; r += 2) {
+            const int row = rbase + r + half;
+            if (row >= M) continue;
+            const float x0 = stg[(r + half) * 33 + cc], x1 = stg[(r + half) * 33 + cc + 1];
+            __nv_bfloat16* dst = C16 + (int64_t)row * ldc + n;
+            if (n + 1 < N) *reinterpret_cast<__nv_bfloat162*>(dst) = __floats2bfloat162_rn(x0, x1);
+            else if (n < N) *dst = __float2bfloat16_rn(x0);
+          }
+        } else {
+          const int n = c0 + lane;
+          for (int r = 0; r < 32; ++r) {
+            const int row = rbase + r;
+            if (row < M && n < N) C16[(int64_t)row * ldc + n] = __float2bfloat16_rn(stg[r * 33 + lane]);
           }
         }
       }
+      __syncwarp();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
