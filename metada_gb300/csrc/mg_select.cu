@@ -7,11 +7,17 @@
 // Geographic coordinates: a device-built spatial hash of 1 x 1 degree cells.
 // Each query column visits only the cells its radius can reach (latitude
 // band bound plus a longitude bound from the haversine inequality
-// a >= cos(lat_c) cos(lat_o) sin^2(dlon/2)), evaluates the reference
-// haversine on the candidates, then sorts its list by obs index in shared
-// memory.  Pairs whose GPU distance lies within 1e-9 relative of the radius
-// are re-decided on the host with the reference expression (glibc libm), so
-// the selection is bit-exact whatever the device's transcendental rounding.
+// a >= cos(lat_c) cos(lat_o) sin^2(dlon/2)); the reachable cells of one
+// latitude band are one or two contiguous runs of the cell-sorted obs, which
+// the whole CTA sweeps.  The test on a candidate is the squared chord
+// |u_c - u_o|^2 between unit vectors (u_o stored with the hash), compared
+// with the chord of the radius: haversine <= r  <=>  chord^2 <= 4 sin^2(r/2R),
+// with an absolute error near 1e-16 against a band of 2e-9 relative in
+// chord^2 (radii of 50 km or more; smaller radii evaluate the reference
+// haversine instead).  Lists are sorted by obs index in shared memory.
+// Pairs within 1e-9 relative of the radius are re-decided on the host with
+// the reference expression (glibc libm), so the selection is bit-exact
+// whatever the device's transcendental rounding.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -84,33 +90,55 @@ __global__ void cell_count_kernel(const double* __restrict__ lat, const double* 
     atomicAdd(&cnt[cell_of(lat[o], lon[o])], 1ull);
 }
 
+__device__ __forceinline__ double3 unit_vec(double lat, double lon) {
+  double sa, ca, so, co;
+  sincos(lat * kPi / 180.0, &sa, &ca);
+  sincos(lon * kPi / 180.0, &so, &co);
+  return make_double3(ca * co, ca * so, sa);
+}
+
+// Cell-sorted obs: index, latitude, longitude and unit vector.
+struct CellObs {
+  int32_t* obs;
+  double* lat;
+  double* lon;
+  double* ux;
+  double* uy;
+  double* uz;
+};
+
 __global__ void cell_scatter_kernel(const double* __restrict__ lat, const double* __restrict__ lon,
                                     int64_t p, const int64_t* __restrict__ start,
-                                    unsigned long long* __restrict__ cursor,
-                                    int32_t* __restrict__ cobs, double* __restrict__ clat,
-                                    double* __restrict__ clon) {
+                                    unsigned long long* __restrict__ cursor, CellObs co) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p; o += stride) {
     const int c = cell_of(lat[o], lon[o]);
     const int64_t pos = start[c] + (int64_t)atomicAdd(&cursor[c], 1ull);
-    cobs[pos] = (int32_t)o;
-    clat[pos] = lat[o];
-    clon[pos] = lon[o];
+    co.obs[pos] = (int32_t)o;
+    co.lat[pos] = lat[o];
+    co.lon[pos] = lon[o];
+    const double3 u = unit_vec(lat[o], lon[o]);
+    co.ux[pos] = u.x;
+    co.uy[pos] = u.y;
+    co.uz[pos] = u.z;
   }
 }
 
-// Visits every candidate obs of column (la, lo) and calls f(obs, dist, cls)
-// with cls = +1 (inside), 0 (near the threshold), -1 (outside: not called).
+// Visits every candidate obs of column (la, lo) with the whole CTA and calls
+// f(t, cls) for the candidates at cell-sorted position t with cls = +1
+// (inside) or 0 (within 1e-9 relative of the radius).
 template <typename F>
-__device__ void visit_candidates(double la, double lo, double radius_km,
-                                 const int64_t* __restrict__ start, const int32_t* __restrict__ cobs,
-                                 const double* __restrict__ clat, const double* __restrict__ clon,
-                                 F&& f) {
+__device__ void visit_candidates(double la, double lo, double radius_km, const int64_t* __restrict__ start,
+                                 const CellObs& co, F&& f) {
   const double theta = radius_km / kEarthKm;  // radians
   const double theta_deg = theta * 180.0 / kPi;
   const double sh = sin(0.5 * theta);
   const double a_r = sh * sh;
+  const bool chord = radius_km >= 50.0;
   const double rlo = radius_km * (1.0 - kBorderRel), rhi = radius_km * (1.0 + kBorderRel);
+  const double slo = sin(0.5 * rlo / kEarthKm), shi = sin(0.5 * rhi / kEarthKm);
+  const double c2lo = 4.0 * slo * slo, c2hi = 4.0 * shi * shi;
+  const double3 uc = unit_vec(la, lo);
   int b0 = (int)floor(la + 90.0 - theta_deg - 1e-6);
   int b1 = (int)floor(la + 90.0 + theta_deg + 1e-6);
   b0 = b0 < 0 ? 0 : b0;
@@ -122,28 +150,51 @@ __device__ void visit_candidates(double la, double lo, double radius_km,
     const double cmin = cos(emax * kPi / 180.0);
     const double denom = cosc * cmin;
     int c0 = 0, c1 = kNLonCell - 1;
-    bool full = true;
     if (denom > a_r * (1.0 + 1e-6)) {
       const double sarg = sqrt(a_r / denom) * (1.0 + 1e-9);
       if (sarg < 1.0) {
         const double dl = 2.0 * asin(sarg) * 180.0 / kPi + 1e-6;
         if (2.0 * dl + 2.0 < 360.0) {
-          full = false;
           c0 = (int)floor(lo - dl);
           c1 = (int)floor(lo + dl);
         }
       }
     }
-    for (int cc = c0; cc <= c1; ++cc) {
-      int c = full ? cc : ((cc % kNLonCell) + kNLonCell) % kNLonCell;
-      c += band * kNLonCell;
-      const int64_t s0 = start[c], s1 = start[c + 1];
-      for (int64_t t = s0 + threadIdx.x; t < s1; t += blockDim.x) {
-        const double d = haversine_dev(la, lo, clat[t], clon[t]);
-        if (d <= rlo)
-          f(cobs[t], d, 1, clat[t], clon[t]);
-        else if (d <= rhi)
-          f(cobs[t], d, 0, clat[t], clon[t]);
+    // The cells c0..c1 (mod 360) as at most two contiguous runs of obs.
+    int64_t run_lo[2], run_hi[2];
+    int nrun = 0;
+    const int bb = band * kNLonCell;
+    if (c1 - c0 + 1 >= kNLonCell) {
+      run_lo[0] = start[bb];
+      run_hi[0] = start[bb + kNLonCell];
+      nrun = 1;
+    } else {
+      const int a0 = ((c0 % kNLonCell) + kNLonCell) % kNLonCell;
+      const int a1 = ((c1 % kNLonCell) + kNLonCell) % kNLonCell;
+      if (a0 <= a1) {
+        run_lo[0] = start[bb + a0];
+        run_hi[0] = start[bb + a1 + 1];
+        nrun = 1;
+      } else {
+        run_lo[0] = start[bb + a0];
+        run_hi[0] = start[bb + kNLonCell];
+        run_lo[1] = start[bb];
+        run_hi[1] = start[bb + a1 + 1];
+        nrun = 2;
+      }
+    }
+    for (int rr = 0; rr < nrun; ++rr) {
+      for (int64_t t = run_lo[rr] + threadIdx.x; t < run_hi[rr]; t += blockDim.x) {
+        if (chord) {
+          const double dx = co.ux[t] - uc.x, dy = co.uy[t] - uc.y, dz = co.uz[t] - uc.z;
+          const double c2 = dx * dx + dy * dy + dz * dz;
+          if (c2 <= c2lo) f(t, 1);
+          else if (c2 <= c2hi) f(t, 0);
+        } else {
+          const double d = haversine_dev(la, lo, co.lat[t], co.lon[t]);
+          if (d <= rlo) f(t, 1);
+          else if (d <= rhi) f(t, 0);
+        }
       }
     }
   }
@@ -161,8 +212,7 @@ __device__ __forceinline__ bool key_rejected(const unsigned long long* rej, int 
 
 __global__ void __launch_bounds__(256) geo_count_kernel(
     const double* __restrict__ col_lat, const double* __restrict__ col_lon, int64_t ncol,
-    double radius_km, const int64_t* __restrict__ start, const int32_t* __restrict__ cobs,
-    const double* __restrict__ clat, const double* __restrict__ clon, int64_t* __restrict__ counts,
+    double radius_km, const int64_t* __restrict__ start, CellObs co, int64_t* __restrict__ counts,
     BorderRec* __restrict__ border, unsigned long long* __restrict__ nborder) {
   __shared__ unsigned long long scount;
   const int64_t col = blockIdx.x;
@@ -170,15 +220,14 @@ __global__ void __launch_bounds__(256) geo_count_kernel(
   __syncthreads();
   const double la = col_lat[col], lo = col_lon[col];
   unsigned long long mine = 0;
-  visit_candidates(la, lo, radius_km, start, cobs, clat, clon,
-                   [&](int32_t o, double, int cls, double ola, double olo) {
-                     ++mine;
-                     if (cls == 0) {
-                       const unsigned long long slot = atomicAdd(nborder, 1ull);
-                       if (slot < (unsigned long long)kBorderCap)
-                         border[slot] = BorderRec{col, (int64_t)o, la, lo, ola, olo};
-                     }
-                   });
+  visit_candidates(la, lo, radius_km, start, co, [&](int64_t t, int cls) {
+    ++mine;
+    if (cls == 0) {
+      const unsigned long long slot = atomicAdd(nborder, 1ull);
+      if (slot < (unsigned long long)kBorderCap)
+        border[slot] = BorderRec{col, (int64_t)co.obs[t], la, lo, co.lat[t], co.lon[t]};
+    }
+  });
   atomicAdd(&scount, mine);
   __syncthreads();
   if (threadIdx.x == 0) counts[col] = (int64_t)scount;
@@ -193,8 +242,7 @@ __global__ void apply_rejections_kernel(const unsigned long long* __restrict__ r
 
 __global__ void __launch_bounds__(256) geo_fill_kernel(
     const double* __restrict__ col_lat, const double* __restrict__ col_lon, int64_t ncol,
-    double radius_km, const int64_t* __restrict__ start, const int32_t* __restrict__ cobs,
-    const double* __restrict__ clat, const double* __restrict__ clon,
+    double radius_km, const int64_t* __restrict__ start, CellObs co,
     const int64_t* __restrict__ offsets, const unsigned long long* __restrict__ rej, int nrej,
     const double* __restrict__ obs_lat, const double* __restrict__ obs_lon,
     int32_t* __restrict__ idx, double* __restrict__ dist, int* __restrict__ overflow) {
@@ -211,14 +259,12 @@ __global__ void __launch_bounds__(256) geo_fill_kernel(
   if (threadIdx.x == 0) scount = 0;
   __syncthreads();
   const double la = col_lat[col], lo = col_lon[col];
-  visit_candidates(la, lo, radius_km, start, cobs, clat, clon,
-                   [&](int32_t o, double, int cls, double, double) {
-                     if (cls == 0 && nrej > 0 &&
-                         key_rejected(rej, nrej, ((unsigned long long)col << 32) | (unsigned)o))
-                       return;
-                     const int pos = atomicAdd(&scount, 1);
-                     if (pos < kMaxList) slist[pos] = o;
-                   });
+  visit_candidates(la, lo, radius_km, start, co, [&](int64_t t, int cls) {
+    const int32_t o = co.obs[t];
+    if (cls == 0 && nrej > 0 && key_rejected(rej, nrej, ((unsigned long long)col << 32) | (unsigned)o)) return;
+    const int pos = atomicAdd(&scount, 1);
+    if (pos < kMaxList) slist[pos] = o;
+  });
   __syncthreads();
   const int cnt = scount;
   if (cnt != (int)n) {  // count and fill passes disagree: report, write nothing
@@ -245,10 +291,21 @@ __global__ void __launch_bounds__(256) geo_fill_kernel(
       __syncthreads();
     }
   }
+  const double3 uc = unit_vec(la, lo);
+  const bool chord = radius_km >= 50.0;
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     const int o = slist[t];
     idx[base + t] = o;
-    if (dist) dist[base + t] = haversine_dev(la, lo, obs_lat[o], obs_lon[o]);
+    if (dist) {
+      if (chord) {  // d = 2R asin(chord / 2): well conditioned for chords up to the radius
+        const double3 u = unit_vec(obs_lat[o], obs_lon[o]);
+        const double dx = u.x - uc.x, dy = u.y - uc.y, dz = u.z - uc.z;
+        const double h = 0.5 * sqrt(dx * dx + dy * dy + dz * dz);
+        dist[base + t] = 2.0 * kEarthKm * asin(h < 1.0 ? h : 1.0);
+      } else {
+        dist[base + t] = haversine_dev(la, lo, obs_lat[o], obs_lon[o]);
+      }
+    }
   }
 }
 
@@ -320,8 +377,7 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
   cv.reserve<unsigned long long>(kNCell + 1);
   cv.reserve<int64_t>(kNCell + 1);             // cell start
   cv.reserve<int32_t>(p + 1);
-  cv.reserve<double>(p + 1);
-  cv.reserve<double>(p + 1);
+  for (int a = 0; a < 5; ++a) cv.reserve<double>(p + 1);  // lat, lon, unit vector
   cv.reserve<int64_t>(ncol + 1);               // column counts
   cv.reserve<BorderRec>(kBorderCap);
   cv.reserve<unsigned long long>(kBorderCap);  // rejected keys
@@ -334,9 +390,13 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
   auto* ccount = cv.take<unsigned long long>(kNCell + 1);
   auto* ccursor = cv.take<unsigned long long>(kNCell + 1);
   auto* cstart = cv.take<int64_t>(kNCell + 1);
-  auto* cobs = cv.take<int32_t>(p + 1);
-  auto* clat = cv.take<double>(p + 1);
-  auto* clon = cv.take<double>(p + 1);
+  CellObs co;
+  co.obs = cv.take<int32_t>(p + 1);
+  co.lat = cv.take<double>(p + 1);
+  co.lon = cv.take<double>(p + 1);
+  co.ux = cv.take<double>(p + 1);
+  co.uy = cv.take<double>(p + 1);
+  co.uz = cv.take<double>(p + 1);
   auto* counts = cv.take<int64_t>(ncol + 1);
   auto* border = cv.take<BorderRec>(kBorderCap);
   auto* rej = cv.take<unsigned long long>(kBorderCap);
@@ -358,15 +418,15 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
     MG_TRY_CUDA(cudaGetLastError());
     MG_TRY_CUDA(mg::exclusive_scan(reinterpret_cast<const int64_t*>(ccount), cstart, kNCell, tmp,
                                    tmpb, s));
-    cell_scatter_kernel<<<gb, 256, 0, s>>>(obs_lat, obs_lon, p, cstart, ccursor, cobs, clat, clon);
+    cell_scatter_kernel<<<gb, 256, 0, s>>>(obs_lat, obs_lon, p, cstart, ccursor, co);
     MG_COUNT_LAUNCH();
     MG_TRY_CUDA(cudaGetLastError());
   } else {
     MG_TRY_CUDA(cudaMemsetAsync(cstart, 0, sizeof(int64_t) * (kNCell + 1), s));
   }
   // Pass 1: counts (near-threshold pairs counted and recorded).
-  geo_count_kernel<<<(unsigned)ncol, 256, 0, s>>>(col_lat, col_lon, ncol, radius_km, cstart, cobs,
-                                                  clat, clon, counts, border, nborder);
+  geo_count_kernel<<<(unsigned)ncol, 256, 0, s>>>(col_lat, col_lon, ncol, radius_km, cstart, co, counts, border,
+                                                  nborder);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   unsigned long long nb = 0;
@@ -404,9 +464,8 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
   const size_t smem = sizeof(int32_t) * smem_entries;
   MG_TRY_CUDA(cudaFuncSetAttribute(geo_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
-  geo_fill_kernel<<<(unsigned)ncol, 256, smem, s>>>(col_lat, col_lon, ncol, radius_km, cstart, cobs,
-                                                    clat, clon, offsets, rej, nrej, obs_lat,
-                                                    obs_lon, idx, dist_km, overflow);
+  geo_fill_kernel<<<(unsigned)ncol, 256, smem, s>>>(col_lat, col_lon, ncol, radius_km, cstart, co, offsets, rej,
+                                                    nrej, obs_lat, obs_lon, idx, dist_km, overflow);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   int ovf = 0;

@@ -106,6 +106,12 @@ def select_grid(nx: int, ny: int, obs_xy: torch.Tensor, radius: float) -> tuple[
     return offsets, idx[: total.value]
 
 
+# Last list length per (device, ncol, p, radius): repeated searches of the
+# same shape pass it as the capacity, so the search runs once instead of a
+# sizing call followed by the filling call.
+_GEO_CAP: dict[tuple, int] = {}
+
+
 def select_geo(col_lat: torch.Tensor, col_lon: torch.Tensor, obs_lat: torch.Tensor, obs_lon: torch.Tensor,
                radius_km: float, cap: int | None = None) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
     """Local obs lists for every query column (haversine <= radius_km)."""
@@ -115,18 +121,23 @@ def select_geo(col_lat: torch.Tensor, col_lon: torch.Tensor, obs_lat: torch.Tens
     ctx = context(dev.index)
     ncol = col_lat.shape[0]
     p = obs_lat.shape[0]
+    key = (dev.index, ncol, p, float(radius_km))
     offsets = torch.empty(ncol + 1, dtype=torch.int64, device=dev)
     total = c_int64(0)
     if cap is None:
-        rc = ctx.lib.mg_select_geo(ctx.handle, _ptr(col_lat), _ptr(col_lon), ncol, _ptr(obs_lat), _ptr(obs_lon),
-                                   p, float(radius_km), _ptr(offsets), c_void_p(0), c_void_p(0), 0, byref(total))
-        if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
-            ctx.check(rc)
-        cap = total.value
-    idx = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
-    dist = torch.empty(max(cap, 1), dtype=torch.float64, device=dev)
-    ctx.call("mg_select_geo", _ptr(col_lat), _ptr(col_lon), ncol, _ptr(obs_lat), _ptr(obs_lon), p,
-             float(radius_km), _ptr(offsets), _ptr(idx), _ptr(dist), idx.numel(), byref(total))
+        cap = _GEO_CAP.get(key, 0)
+    for _ in range(2):
+        idx = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+        dist = torch.empty(max(cap, 1), dtype=torch.float64, device=dev)
+        rc = ctx.lib.mg_select_geo(ctx.handle, _ptr(col_lat), _ptr(col_lon), ncol, _ptr(obs_lat), _ptr(obs_lon), p,
+                                   float(radius_km), _ptr(offsets), _ptr(idx) if cap > 0 else c_void_p(0),
+                                   _ptr(dist) if cap > 0 else c_void_p(0), cap, byref(total))
+        if rc == _lib.MG_ERR_CAPACITY and total.value > cap:
+            cap = total.value
+            continue
+        ctx.check(rc)
+        break
+    _GEO_CAP[key] = total.value
     return offsets, idx[: total.value], dist[: total.value]
 
 
