@@ -287,6 +287,138 @@ __device__ int cta_jacobi_fast(T* A, T* V, int kp, int lda, T tol, int max_sweep
   return sweep + 1;
 }
 
+// ---- FP32 Jacobi with the symmetric matrix kept as its upper triangle ----
+//
+// Same round-robin ordering and closed-form 2 x 2 updates as
+// cta_jacobi_fast, arranged for shared-memory bandwidth, the limit of the
+// analysis kernel: pairs come arithmetically from the round number (slot 0
+// pairs (r, m), slot i >= 1 pairs ((r + i) mod m, (r - i) mod m), m = kp - 1),
+// only the blocks (b <= c) of the upper triangle are updated (every entry at
+// [min][max]), and the eigenvectors are kept transposed (Vt, one row per
+// eigenvector) so that a rotation of two eigenvectors is two float4 row
+// streams.
+
+__device__ __forceinline__ void jacobi_pair(int s, int r, int m, int& p, int& q) {
+  if (s == 0) {
+    p = r;
+    q = m;
+  } else {
+    p = r + s;
+    if (p >= m) p -= m;
+    q = r - s;
+    if (q < 0) q += m;
+  }
+}
+
+// Rotation (c, s) zeroing apq, and the two rotated diagonal entries.
+__device__ __forceinline__ float4 jacobi_rot(float app, float aqq, float apq, float tol) {
+  float c = 1.0f, s = 0.0f, t = 0.0f;
+  if (apq != 0.0f && fabsf(apq) > tol * sqrtf(fabsf(app) * fabsf(aqq))) {
+    const float theta = (aqq - app) / (2.0f * apq);
+    t = (theta >= 0.0f ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+    c = 1.0f / sqrtf(t * t + 1.0f);
+    s = t * c;
+  }
+  return make_float4(c, s, app - t * apq, aqq + t * apq);
+}
+
+// Diagonalises A (kp x kp, kp even, lda; read and written in its upper
+// triangle only) to the off-diagonal threshold tol.  Vt (rows of ldv
+// floats, ldv % 4 == 0, ldv >= 4 ceil(kp / 4), 16-byte aligned) receives the
+// eigenvectors as rows: Vt[j * ldv + i] = V_ij.  rot holds kp/2 float4
+// (16-byte aligned).  Returns the sweeps run.
+template <int KMAX, int NT>
+__device__ int cta_jacobi_tri(float* A, int lda, float* Vt, int ldv, int kp, float tol, int max_sweeps,
+                              float4* rot) {
+  constexpr int HM = KMAX / 2;
+  constexpr int NB = (HM * (HM + 1) / 2 + NT - 1) / NT;     // upper-triangle blocks per thread
+  constexpr int NVI = (HM * ((KMAX + 3) / 4) + NT - 1) / NT;  // (pair, 4-row chunk) items per thread
+  const int tid = threadIdx.x, h = kp >> 1, m = kp - 1, nch = (kp + 3) >> 2;
+  for (int e = tid; e < kp * 4 * nch; e += NT) {
+    const int j = e / (4 * nch), i = e - j * (4 * nch);
+    Vt[j * ldv + i] = (i == j) ? 1.0f : 0.0f;
+  }
+  int blk[NB];  // b << 8 | c with b <= c, or -1
+#pragma unroll
+  for (int u = 0; u < NB; ++u) {
+    int e = tid + u * NT, b = 0;
+    if (e >= h * (h + 1) / 2) {
+      blk[u] = -1;
+      continue;
+    }
+    while (e >= h - b) {
+      e -= h - b;
+      ++b;
+    }
+    blk[u] = (b << 8) | (b + e);
+  }
+  __syncthreads();
+  int sweep = 0;
+  while (sweep < max_sweeps) {
+    int rotated = 0;
+    for (int r = 0; r < m; ++r) {
+      for (int i = tid; i < h; i += NT) {
+        int p, q;
+        jacobi_pair(i, r, m, p, q);
+        const float4 R = jacobi_rot(A[p * lda + p], A[q * lda + q], A[min(p, q) * lda + max(p, q)], tol);
+        rot[i] = R;
+        rotated |= (R.y != 0.0f);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < NB; ++u) {
+        if (blk[u] < 0) continue;
+        const int b = blk[u] >> 8, c = blk[u] & 0xff;
+        const float4 pb = rot[b];
+        if (b == c) {
+          if (pb.y == 0.0f) continue;
+          int p, q;
+          jacobi_pair(b, r, m, p, q);
+          A[p * lda + p] = pb.z;
+          A[q * lda + q] = pb.w;
+          A[min(p, q) * lda + max(p, q)] = 0.0f;
+          continue;
+        }
+        const float4 pc = rot[c];
+        if (pb.y == 0.0f && pc.y == 0.0f) continue;
+        int r0, r1, c0, c1;
+        jacobi_pair(b, r, m, r0, r1);
+        jacobi_pair(c, r, m, c0, c1);
+        const int i00 = min(r0, c0) * lda + max(r0, c0), i01 = min(r0, c1) * lda + max(r0, c1);
+        const int i10 = min(r1, c0) * lda + max(r1, c0), i11 = min(r1, c1) * lda + max(r1, c1);
+        const float a00 = A[i00], a01 = A[i01], a10 = A[i10], a11 = A[i11];
+        const float m00 = pb.x * a00 - pb.y * a10, m01 = pb.x * a01 - pb.y * a11;
+        const float m10 = pb.y * a00 + pb.x * a10, m11 = pb.y * a01 + pb.x * a11;
+        A[i00] = pc.x * m00 - pc.y * m01;
+        A[i01] = pc.y * m00 + pc.x * m01;
+        A[i10] = pc.x * m10 - pc.y * m11;
+        A[i11] = pc.y * m10 + pc.x * m11;
+      }
+#pragma unroll
+      for (int u = 0; u < NVI; ++u) {
+        const int e = tid + u * NT;
+        const int sl = e / nch, ch = e - sl * nch;
+        if (sl >= h) break;
+        const float4 ps = rot[sl];
+        if (ps.y == 0.0f) continue;
+        int p, q;
+        jacobi_pair(sl, r, m, p, q);
+        float4* vp = reinterpret_cast<float4*>(Vt + p * ldv) + ch;
+        float4* vq = reinterpret_cast<float4*>(Vt + q * ldv) + ch;
+        const float4 a = *vp, bq = *vq;
+        *vp = make_float4(ps.x * a.x - ps.y * bq.x, ps.x * a.y - ps.y * bq.y, ps.x * a.z - ps.y * bq.z,
+                          ps.x * a.w - ps.y * bq.w);
+        *vq = make_float4(ps.y * a.x + ps.x * bq.x, ps.y * a.y + ps.x * bq.y, ps.y * a.z + ps.x * bq.z,
+                          ps.y * a.w + ps.x * bq.w);
+      }
+      __syncthreads();
+    }
+    ++sweep;
+    if (!__syncthreads_or(rotated)) break;
+  }
+  return sweep;
+}
+
 // One Newton-Schulz step towards the orthogonal polar factor of V (k x k):
 // V <- V (3I - V^T V) / 2.  Rotations accumulated in FP32 leave V about
 // sweeps * k * eps away from orthogonal; one step squares that deviation.

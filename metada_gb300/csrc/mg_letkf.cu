@@ -83,10 +83,13 @@ template <typename TE, int KMAX>
 struct Plan {
   static constexpr bool TWO_STAGE = sizeof(TE) == 4 && KMAX <= 96;
   static constexpr int LDA = KMAX + 1;
+  // The two-stage path's first Jacobi keeps its eigenvectors as float4 rows
+  // (cta_jacobi_tri), so the V region has rows of LDV (multiple of 4).
+  static constexpr int LDV = TWO_STAGE ? KMAX + 4 : LDA;
   static constexpr int CH = 32;                    // list chunk rows
   static constexpr int NCHUNK = TWO_STAGE ? 2 : 1;  // Ys (, Bc)
   static constexpr size_t te_count() {
-    return (size_t)2 * KMAX * LDA + (size_t)NCHUNK * CH * KMAX + 2 * CH + 4 * KMAX + 2 * KMAX +
+    return (size_t)KMAX * LDA + (size_t)KMAX * LDV + (size_t)NCHUNK * CH * KMAX + 2 * CH + 4 * KMAX + 2 * KMAX +
            kNVarMax * KMAX;
   }
   static constexpr size_t bytes() {
@@ -158,16 +161,17 @@ __device__ int for_each_chunk(const LetkfParams& prm, int64_t e0, int64_t e1, in
   return nloc;
 }
 
-// acc += sum_r w_r * M[r, ti*R..] (x) M[r, tj*R..] over the rows of a chunk.
+// acc[a][b] += sum_r w_r M[r, ti + 16a] M[r, tj + 16b] over the rows of a
+// chunk (interleaved tiles: a warp's loads hit consecutive words).
 template <typename TE, int KMAX, int R>
 __device__ __forceinline__ void gram_rows(TE (&acc)[R][R], const TE* M, const TE* w, int cnt, int ti, int tj) {
   for (int r = 0; r < cnt; ++r) {
     const TE wr = w ? w[r] : TE(1);
     TE av[R], bv[R];
 #pragma unroll
-    for (int a = 0; a < R; ++a) av[a] = M[r * KMAX + ti * R + a] * wr;
+    for (int a = 0; a < R; ++a) av[a] = M[r * KMAX + ti + 16 * a] * wr;
 #pragma unroll
-    for (int b = 0; b < R; ++b) bv[b] = M[r * KMAX + tj * R + b];
+    for (int b = 0; b < R; ++b) bv[b] = M[r * KMAX + tj + 16 * b];
 #pragma unroll
     for (int a = 0; a < R; ++a)
 #pragma unroll
@@ -176,13 +180,14 @@ __device__ __forceinline__ void gram_rows(TE (&acc)[R][R], const TE* M, const TE
 }
 
 template <typename TE, int KMAX>
-__global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 : 1) letkf_batched_kernel(LetkfParams prm) {
+__global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 : ((sizeof(TE) == 4 && KMAX <= 96) ? 2 : 1))
+    letkf_batched_kernel(LetkfParams prm) {
   using P = Plan<TE, KMAX>;
   constexpr int LDA = P::LDA, CH = P::CH, R = KMAX / 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TE* A = reinterpret_cast<TE*>(smem_raw);
-  TE* V = A + KMAX * LDA;
-  TE* Ys = V + KMAX * LDA;                   // CH x KMAX
+  TE* const A0 = reinterpret_cast<TE*>(smem_raw);
+  TE* const V0 = A0 + KMAX * LDA;            // KMAX x LDV
+  TE* Ys = V0 + KMAX * P::LDV;               // CH x KMAX
   TE* Bc = Ys + CH * KMAX;                   // two-stage only: CH x KMAX
   TE* sel_r = Ys + P::NCHUNK * CH * KMAX;    // CH
   TE* sel_d = sel_r + CH;                    // CH
@@ -230,6 +235,9 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
     } else {
       ++lev;
     }
+    // The two-stage path may exchange the roles of the A and V regions.
+    TE* A = A0;
+    TE* V = V0;
     const int64_t col = warm_mode ? prm.order[item] : prm.order[item / prm.nlev];
     const int64_t base = prm.col_base[col] + (int64_t)lev * prm.lev_stride;
     const int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
@@ -266,7 +274,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
     for (int a = 0; a < R; ++a)
 #pragma unroll
       for (int b = 0; b < R; ++b) {
-        const int i = ti * R + a, j = tj * R + b;
+        const int i = ti + 16 * a, j = tj + 16 * b;
         if (i < kp && j < kp) {
           TE v = (i < k && j < k) ? acc[a][b] : TE(0);
           if (i == j) v += (i < k) ? diag : TE(1);
@@ -287,9 +295,32 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
       // Stage 1: loose Jacobi on A = diag I + G gives a basis V1 in which A
       // is nearly diagonal.
       const bool warm = warm_mode && have_basis;
-      if (warm) mg::cta_similarity<TE>(A, V, kp, LDA, Ys, CH - 1);
-      sweeps = mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V, kp, LDA, TE(kStage1Tol), prm.sweep_cap, rot, pairbuf,
-                                                       !warm);
+      if constexpr (P::TWO_STAGE) {
+        static_assert((KMAX * LDA + KMAX * P::LDV + P::NCHUNK * CH * KMAX + 2 * CH + 2 * KMAX) % 4 == 0,
+                      "rotation buffer must be 16-byte aligned");
+        if (!warm_mode) {
+          sweeps = mg::cta_jacobi_tri<KMAX, kThreads>(A, LDA, V, P::LDV, kp, (float)kStage1Tol, prm.sweep_cap,
+                                                      reinterpret_cast<float4*>(uvec));
+          // Eigenvector rows -> row-major V in the A region (A is not needed
+          // any more), then the regions exchange roles.
+          for (int e = tid; e < kp * kp; e += kThreads) {
+            const int j = e / kp, i = e - j * kp;
+            A[i * LDA + j] = V[j * P::LDV + i];
+          }
+          __syncthreads();
+          TE* t = A;
+          A = V;
+          V = t;
+        } else {
+          if (warm) mg::cta_similarity<TE>(A, V, kp, LDA, Ys, CH - 1);
+          sweeps = mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V, kp, LDA, TE(kStage1Tol), prm.sweep_cap, rot,
+                                                           pairbuf, !warm);
+        }
+      } else {
+        if (warm) mg::cta_similarity<TE>(A, V, kp, LDA, Ys, CH - 1);
+        sweeps = mg::cta_jacobi_fast<TE, KMAX, kThreads>(A, V, kp, LDA, TE(kStage1Tol), prm.sweep_cap, rot, pairbuf,
+                                                         !warm);
+      }
       // V1 back to orthogonal (A is free until the rebuild below).
       mg::cta_reorthonormalize<TE, KMAX>(V, kp, LDA, A, Ys, CH);
       // Stage 2: rebuild A2 = V1^T A V1 from the factor, diag I + B^T B with
@@ -301,14 +332,37 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
 #pragma unroll
         for (int b = 0; b < R; ++b) acc[a][b] = TE(0);
       for_each_chunk<TE, KMAX, CH>(prm, e0, e1, lev, Ys, sel_o, sel_r, sel_d, wcnt, [&](int cnt) {
-        for (int e = tid; e < cnt * KMAX; e += kThreads) {
-          const int r = e / KMAX, j = e - r * KMAX;
-          TE s = TE(0);
-          if (j < k) {
-            for (int m = 0; m < k; ++m) s += Ys[r * KMAX + m] * V[m * LDA + j];
-            s *= sqrt(sel_r[r]);
+        {  // Bc = diag(sqrt w) Ys V: warp w owns rows 4w..4w+3, lane the columns lane + 32c
+          constexpr int RW = CH / (kThreads / 32), CW = KMAX / 32;
+          const int wrp = tid >> 5, ln = tid & 31;
+          TE sacc[RW][CW];
+#pragma unroll
+          for (int x = 0; x < RW; ++x)
+#pragma unroll
+            for (int c = 0; c < CW; ++c) sacc[x][c] = TE(0);
+          for (int m = 0; m < k; ++m) {
+            TE yv[RW], vv[CW];
+#pragma unroll
+            for (int x = 0; x < RW; ++x) yv[x] = Ys[(wrp * RW + x) * KMAX + m];
+#pragma unroll
+            for (int c = 0; c < CW; ++c) vv[c] = V[m * LDA + ln + 32 * c];
+#pragma unroll
+            for (int x = 0; x < RW; ++x)
+#pragma unroll
+              for (int c = 0; c < CW; ++c) sacc[x][c] += yv[x] * vv[c];
           }
-          Bc[e] = s;
+#pragma unroll
+          for (int x = 0; x < RW; ++x) {
+            const int r = wrp * RW + x;
+            if (r < cnt) {
+              const TE sw = sqrt(sel_r[r]);
+#pragma unroll
+              for (int c = 0; c < CW; ++c) {
+                const int j = ln + 32 * c;
+                Bc[r * KMAX + j] = (j < k) ? sacc[x][c] * sw : TE(0);
+              }
+            }
+          }
         }
         __syncthreads();
         gram_rows<TE, KMAX, R>(acc, Bc, nullptr, cnt, ti, tj);
@@ -317,7 +371,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
       for (int a = 0; a < R; ++a)
 #pragma unroll
         for (int b = 0; b < R; ++b) {
-          const int i = ti * R + a, j = tj * R + b;
+          const int i = ti + 16 * a, j = tj + 16 * b;
           if (i < kp && j < kp) {
             TE v = (i < k && j < k) ? acc[a][b] : TE(0);
             if (i == j) v += (i < k) ? diag : TE(1);
@@ -612,7 +666,7 @@ __global__ void __launch_bounds__(kThreads) letkf_compat_seq_kernel(CompatSeqPar
         for (int a = 0; a < R; ++a)
 #pragma unroll
           for (int b = 0; b < R; ++b)
-            acc[a][b] += Ys[r * KMAX + ti * R + a] * Ys[r * KMAX + tj * R + b];
+            acc[a][b] += Ys[r * KMAX + ti + 16 * a] * Ys[r * KMAX + tj + 16 * b];
       }
       if (tid < k)
         for (int r = 0; r < cnt; ++r) bacc += Ys[r * KMAX + tid] * dd[r];
@@ -637,7 +691,7 @@ __global__ void __launch_bounds__(kThreads) letkf_compat_seq_kernel(CompatSeqPar
     for (int a = 0; a < R; ++a)
 #pragma unroll
       for (int b = 0; b < R; ++b) {
-        const int i = ti * R + a, j = tj * R + b;
+        const int i = ti + 16 * a, j = tj + 16 * b;
         if (i < k && j < k) A[i * LDA + j] = acc[a][b] + (i == j ? (double)(k - 1) : 0.0);
       }
     if (tid < k) bvec[tid] = bacc;
