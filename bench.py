@@ -354,7 +354,7 @@ def run_uneven(args) -> None:
     line = {"metric": "uneven-batch global ETKF analyses/s (512 cases, one captured graph)",
             "value": out["mixed"]["analyses_per_s"], "unit": "analyses/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": out["mixed"]["ms_per_batch"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 update (FP64 Gram and solve)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (two-stage Jacobi + Daleckii-Krein; FP64 means and sums)",
             "data": "synthetic",
             "config": {"workload": "512 cases: n log-uniform 1k-200k, k in {20,32,48,64,100}, p log-uniform "
                                    "100-50k, identity interpolation, sigma_o = 1",

@@ -9,6 +9,12 @@
 //   gram<KMAX>   (case, obs chunk)       partial k x k Gram and b, one launch per member-count bucket
 //   solve        (case)                  FP64 sum of partials, (k-1)/rho I or (k-1) I, transform T
 //   update       (case, 32-state tile)   Xa = xm + X' T; the last tile of a case stamps its finish time
+// The mixed-precision path with the symmetric square root (Hunt et al.
+// 2007) replaces the FP64 Gram and solve by the scheme of the batched
+// LETKF: an FP32 Gram, a loose FP32 Jacobi with one Newton-Schulz
+// re-orthonormalisation (solve1), the Gram rebuilt from the factor
+// B = R^-1/2 Y' V1 (rebuild), and a first-order Daleckii-Krein evaluation of
+// A2^-1/2 and A2^-1 in that basis (solve2).
 // Items are ordered largest first within each kernel.  The same sequence of
 // launches is captured once into a CUDA graph and replayed.  The obs chunk
 // of the Gram items and the member-count bucket boundaries are chosen by an
@@ -41,6 +47,8 @@ struct DevCase {
   double* Gpart;  // nchunk x k x k
   double* bpart;  // nchunk x k
   double* T;      // k x k
+  float* Y32;     // p x k FP32 copy of Y' (mixed Hunt path), or null
+  float* V1;      // k x k stage-1 basis (mixed Hunt path), or null
   int64_t nchunk;
   int64_t ntiles;  // update tiles
 };
@@ -129,7 +137,10 @@ __global__ void __launch_bounds__(kThreads) batch_prep_obs_kernel(const DevCase*
 #pragma unroll
   for (int t = 0; t < 4; ++t) {
     const int i = lane + 32 * t;
-    if (i < k) c.Y[o * k + i] = h[t] - ym;
+    if (i < k) {
+      c.Y[o * k + i] = h[t] - ym;
+      if (c.Y32) c.Y32[o * k + i] = (float)(h[t] - ym);
+    }
   }
   if (lane == 0) {
     c.d[o] = c.yo[o] - ym;
@@ -137,42 +148,44 @@ __global__ void __launch_bounds__(kThreads) batch_prep_obs_kernel(const DevCase*
   }
 }
 
-template <int KMAX>
+template <typename TE, int KMAX>
 __global__ void __launch_bounds__(kThreads) batch_gram_kernel(const DevCase* __restrict__ cases,
                                                               const WorkItem* __restrict__ items) {
   constexpr int CH = (KMAX * 8 > 512) ? 32 : 64, R = KMAX / 16;
-  __shared__ double Ys[CH * KMAX];
-  __shared__ double sr[CH], sd[CH];
+  __shared__ TE Ys[CH * KMAX];
+  __shared__ TE sr[CH], sd[CH];
   const WorkItem it = items[blockIdx.x];
   const DevCase& c = cases[it.c];
   const int k = c.k;
   const int tid = threadIdx.x, ti = tid / 16, tj = tid % 16;
   // it.pad = chunk index within the case, [it.a, it.b) = its obs range
   const int64_t o0 = it.a, o1 = it.b;
-  double acc[R][R];
+  TE acc[R][R];
 #pragma unroll
   for (int a = 0; a < R; ++a)
 #pragma unroll
-    for (int b = 0; b < R; ++b) acc[a][b] = 0.0;
-  double bacc = 0.0;
+    for (int b = 0; b < R; ++b) acc[a][b] = TE(0);
+  TE bacc = TE(0);
   for (int64_t c0 = o0; c0 < o1; c0 += CH) {
     const int cnt = (int)(o1 - c0 < CH ? o1 - c0 : CH);
     for (int e = tid; e < cnt * KMAX; e += kThreads) {
       const int r = e / KMAX, j = e - r * KMAX;
-      Ys[e] = (j < k) ? c.Y[(c0 + r) * k + j] : 0.0;
+      TE v = TE(0);
+      if (j < k) v = (sizeof(TE) == 4) ? (TE)c.Y32[(c0 + r) * k + j] : (TE)c.Y[(c0 + r) * k + j];
+      Ys[e] = v;
     }
     if (tid < cnt) {
-      sr[tid] = c.rinv[c0 + tid];
-      sd[tid] = c.d[c0 + tid];
+      sr[tid] = (TE)c.rinv[c0 + tid];
+      sd[tid] = (TE)c.d[c0 + tid];
     }
     __syncthreads();
     for (int r = 0; r < cnt; ++r) {
-      const double w = sr[r];
-      double av[R], bv[R];
+      const TE w = sr[r];
+      TE av[R], bv[R];
 #pragma unroll
-      for (int a = 0; a < R; ++a) av[a] = Ys[r * KMAX + ti * R + a] * w;
+      for (int a = 0; a < R; ++a) av[a] = Ys[r * KMAX + ti + 16 * a] * w;
 #pragma unroll
-      for (int b = 0; b < R; ++b) bv[b] = Ys[r * KMAX + tj * R + b];
+      for (int b = 0; b < R; ++b) bv[b] = Ys[r * KMAX + tj + 16 * b];
 #pragma unroll
       for (int a = 0; a < R; ++a)
 #pragma unroll
@@ -188,10 +201,219 @@ __global__ void __launch_bounds__(kThreads) batch_gram_kernel(const DevCase* __r
   for (int a = 0; a < R; ++a)
 #pragma unroll
     for (int b = 0; b < R; ++b) {
-      const int i = ti * R + a, j = tj * R + b;
-      if (i < k && j < k) G[i * k + j] = acc[a][b];
+      const int i = ti + 16 * a, j = tj + 16 * b;
+      if (i < k && j < k) G[i * k + j] = (double)acc[a][b];
     }
-  if (tid < k) c.bpart[chunk * k + tid] = bacc;
+  if (tid < k) c.bpart[chunk * k + tid] = (double)bacc;
+}
+
+// ---- mixed path with the symmetric square root (FP32, k <= 112) ----
+constexpr float kStage1Tol = 3e-4f;  // off-diagonal threshold of the loose Jacobi
+
+__host__ __device__ constexpr int mix_lda(int kp) { return kp + 1; }
+__host__ __device__ constexpr int mix_ldv(int kp) { return ((kp + 3) & ~3) + 4; }
+__host__ __device__ constexpr int round4(int x) { return (x + 3) & ~3; }
+__host__ __device__ constexpr size_t solve1_floats(int kp) {
+  return (size_t)round4(kp * mix_lda(kp)) + (size_t)kp * mix_ldv(kp) + 32 * 128 + 4 * 64;
+}
+__host__ __device__ constexpr size_t solve2_floats(int kp) { return 3 * (size_t)kp * mix_lda(kp) + 5 * (size_t)kp; }
+
+// Stage 1 of one case: A = (k-1)/rho I + G (FP32 from the partials), loose
+// Jacobi, V1 back to orthogonal, V1 to global memory.
+__global__ void __launch_bounds__(kThreads) batch_solve1_kernel(const DevCase* __restrict__ cases, int flags) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const DevCase& c = cases[blockIdx.x];
+  const int k = c.k, kp = k + (k & 1), lda = mix_lda(kp), ldv = mix_ldv(kp);
+  float* A = reinterpret_cast<float*>(smem_raw);
+  float* Vt = A + round4(kp * lda);
+  float* tmp = Vt + kp * ldv;
+  float4* rot = reinterpret_cast<float4*>(tmp + 32 * 128);
+  const int tid = threadIdx.x;
+  const double diag = (flags & MG_INFL_COMPAT) ? (double)(k - 1) : (double)(k - 1) / c.rho;
+  for (int e = tid; e < kp * kp; e += kThreads) {
+    const int i = e / kp, j = e - i * kp;
+    double s = 0.0;
+    if (i < k && j < k) {
+      for (int64_t b = 0; b < c.nchunk; ++b) s += c.Gpart[b * k * k + i * k + j];
+      if (i == j) s += diag;
+    } else if (i == j) {
+      s = 1.0;
+    }
+    A[i * lda + j] = (float)s;
+  }
+  __syncthreads();
+  mg::cta_jacobi_tri<128, kThreads>(A, lda, Vt, ldv, kp, kStage1Tol, 30, rot);
+  for (int e = tid; e < kp * kp; e += kThreads) {  // eigenvector rows -> row-major V1 in the A region
+    const int j = e / kp, i = e - j * kp;
+    A[i * lda + j] = Vt[j * ldv + i];
+  }
+  __syncthreads();
+  mg::cta_reorthonormalize<float, 128>(A, kp, lda, Vt, tmp, 32);
+  for (int e = tid; e < k * k; e += kThreads) c.V1[e] = A[(e / k) * lda + e % k];
+}
+
+// Gram of the factor B = diag(sqrt(1/sigma^2)) Y' V1 over one obs chunk:
+// the rebuilt A2 - (k-1)/rho I = V1^T G V1 with errors relative to the
+// column norms of B.
+template <int KMAX>
+__global__ void __launch_bounds__(kThreads) batch_rebuild_kernel(const DevCase* __restrict__ cases,
+                                                                 const WorkItem* __restrict__ items) {
+  constexpr int CH = 32, R = KMAX / 16, LDW = KMAX + 1;
+  constexpr int RW = CH / (kThreads / 32), CW = KMAX / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* V1s = reinterpret_cast<float*>(smem_raw);  // KMAX x LDW
+  float* Ys = V1s + KMAX * LDW;                      // CH x KMAX
+  float* Bc = Ys + CH * KMAX;                        // CH x KMAX
+  __shared__ float sw[CH];
+  const WorkItem it = items[blockIdx.x];
+  const DevCase& c = cases[it.c];
+  const int k = c.k;
+  const int tid = threadIdx.x, ti = tid / 16, tj = tid % 16, wrp = tid >> 5, ln = tid & 31;
+  for (int e = tid; e < KMAX * KMAX; e += kThreads) {
+    const int i = e / KMAX, j = e - i * KMAX;
+    V1s[i * LDW + j] = (i < k && j < k) ? c.V1[i * k + j] : 0.0f;
+  }
+  float acc[R][R];
+#pragma unroll
+  for (int a = 0; a < R; ++a)
+#pragma unroll
+    for (int b = 0; b < R; ++b) acc[a][b] = 0.0f;
+  for (int64_t c0 = it.a; c0 < it.b; c0 += CH) {
+    const int cnt = (int)(it.b - c0 < CH ? it.b - c0 : CH);
+    for (int e = tid; e < cnt * KMAX; e += kThreads) {
+      const int r = e / KMAX, j = e - r * KMAX;
+      Ys[e] = (j < k) ? c.Y32[(c0 + r) * k + j] : 0.0f;
+    }
+    if (tid < cnt) sw[tid] = (float)sqrt(c.rinv[c0 + tid]);
+    __syncthreads();
+    float sacc[RW][CW];
+#pragma unroll
+    for (int x = 0; x < RW; ++x)
+#pragma unroll
+      for (int q = 0; q < CW; ++q) sacc[x][q] = 0.0f;
+    for (int m = 0; m < k; ++m) {
+      float yv[RW], vv[CW];
+#pragma unroll
+      for (int x = 0; x < RW; ++x) yv[x] = Ys[(wrp * RW + x) * KMAX + m];
+#pragma unroll
+      for (int q = 0; q < CW; ++q) vv[q] = V1s[m * LDW + ln + 32 * q];
+#pragma unroll
+      for (int x = 0; x < RW; ++x)
+#pragma unroll
+        for (int q = 0; q < CW; ++q) sacc[x][q] += yv[x] * vv[q];
+    }
+#pragma unroll
+    for (int x = 0; x < RW; ++x) {
+      const int r = wrp * RW + x;
+      if (r < cnt)
+#pragma unroll
+        for (int q = 0; q < CW; ++q) Bc[r * KMAX + ln + 32 * q] = sacc[x][q] * sw[r];
+    }
+    __syncthreads();
+    for (int r = 0; r < cnt; ++r) {
+      float av[R], bv[R];
+#pragma unroll
+      for (int a = 0; a < R; ++a) av[a] = Bc[r * KMAX + ti + 16 * a];
+#pragma unroll
+      for (int b = 0; b < R; ++b) bv[b] = Bc[r * KMAX + tj + 16 * b];
+#pragma unroll
+      for (int a = 0; a < R; ++a)
+#pragma unroll
+        for (int b = 0; b < R; ++b) acc[a][b] += av[a] * bv[b];
+    }
+    __syncthreads();
+  }
+  double* G = c.Gpart + (int64_t)it.pad * k * k;
+#pragma unroll
+  for (int a = 0; a < R; ++a)
+#pragma unroll
+    for (int b = 0; b < R; ++b) {
+      const int i = ti + 16 * a, j = tj + 16 * b;
+      if (i < k && j < k) G[i * k + j] = (double)acc[a][b];
+    }
+}
+
+// Stage 2 of one case: A2 = (k-1)/rho I + sum of the rebuilt partials is
+// nearly diagonal, so W = c V1 (A2^-1/2) V1^T and wa = V1 (A2^-1) V1^T b come
+// from the first-order Daleckii-Krein formula (closed-form divided
+// differences -1/(s_i s_j (s_i + s_j)), s = sqrt(d), and -1/(d_i d_j)).
+__global__ void __launch_bounds__(kThreads) batch_solve2_kernel(const DevCase* __restrict__ cases, int flags,
+                                                                int* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const DevCase& c = cases[blockIdx.x];
+  const int k = c.k, kp = k + (k & 1), lda = mix_lda(kp);
+  float* V = reinterpret_cast<float*>(smem_raw);  // k x k (lda)
+  float* A2 = V + kp * lda;
+  float* Tm = A2 + kp * lda;
+  float* bv = Tm + kp * lda;
+  float* uv = bv + kp;
+  float* gv = uv + kp;
+  float* wa = gv + kp;
+  float* lam = wa + kp;
+  const int tid = threadIdx.x;
+  const bool compat_infl = flags & MG_INFL_COMPAT;
+  const double diag = compat_infl ? (double)(k - 1) : (double)(k - 1) / c.rho;
+  for (int e = tid; e < k * k; e += kThreads) {
+    const int i = e / k, j = e - i * k;
+    V[i * lda + j] = c.V1[e];
+    double s = 0.0;
+    for (int64_t b = 0; b < c.nchunk; ++b) s += c.Gpart[b * k * k + e];
+    if (i == j) s += diag;
+    A2[i * lda + j] = (float)s;
+  }
+  for (int i = tid; i < k; i += kThreads) {
+    double s = 0.0;
+    for (int64_t b = 0; b < c.nchunk; ++b) s += c.bpart[b * k + i];
+    bv[i] = (float)s;
+  }
+  __syncthreads();
+  for (int i = tid; i < k; i += kThreads) {
+    const float l = A2[i * lda + i];
+    lam[i] = l;
+    if (!(l > 0.0f) || !(l < 3.0e38f)) atomicExch(status, 1 + (int)blockIdx.x);
+    float s = 0.0f;  // u = V1^T b
+    for (int j = 0; j < k; ++j) s += V[j * lda + i] * bv[j];
+    uv[i] = s;
+  }
+  __syncthreads();
+  for (int i = tid; i < k; i += kThreads) {  // g = (x^-1)(A2) u
+    float s = uv[i];
+    for (int j = 0; j < k; ++j)
+      if (j != i) s -= A2[i * lda + j] * (uv[j] / lam[j]);
+    gv[i] = s / lam[i];
+  }
+  __syncthreads();
+  for (int i = tid; i < k; i += kThreads) {  // wa = V1 g
+    float s = 0.0f;
+    for (int m = 0; m < k; ++m) s += V[i * lda + m] * gv[m];
+    wa[i] = s;
+  }
+  const float cw = sqrtf((float)(k - 1));
+  for (int e = tid; e < k * k; e += kThreads) {  // A2 <- Wb = (c x^-1/2)(A2)
+    const int i = e / k, j = e - i * k;
+    const float si = sqrtf(lam[i]);
+    if (i == j) {
+      A2[i * lda + i] = cw / si;
+    } else {
+      const float sj = sqrtf(lam[j]);
+      A2[i * lda + j] = -cw * A2[i * lda + j] / (si * sj * (si + sj));
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < k * k; e += kThreads) {  // Tm = V1 Wb
+    const int i = e / k, j = e - i * k;
+    float s = 0.0f;
+    for (int m = 0; m < k; ++m) s += V[i * lda + m] * A2[m * lda + j];
+    Tm[i * lda + j] = s;
+  }
+  __syncthreads();
+  const double scale = compat_infl ? c.rho : 1.0;
+  for (int e = tid; e < k * k; e += kThreads) {  // T[j][i] = scale (wa_j + W_ji), W = Tm V1^T
+    const int j = e / k, i = e - j * k;
+    float s = 0.0f;
+    for (int m = 0; m < k; ++m) s += Tm[j * lda + m] * V[i * lda + m];
+    c.T[j * k + i] = scale * ((double)wa[j] + (double)s);
+  }
 }
 
 // One CTA per case: sum the partials, solve, write T (FP64; the case's
@@ -320,6 +542,10 @@ int build(mg_context* ctx, mg_etkf_batch* b) {
     cv.reserve<double>((size_t)c.nchunk * h.k * h.k);
     cv.reserve<double>((size_t)c.nchunk * h.k);
     cv.reserve<double>((size_t)h.k * h.k);
+    if (!f64) {
+      cv.reserve<float>((size_t)h.p * h.k);
+      cv.reserve<float>((size_t)h.k * h.k);
+    }
     for (int64_t s = 0; s < h.n; s += kStateTile) st_items.push_back({i, 0, s, std::min<int64_t>(h.n, s + kStateTile)});
     for (int64_t o = 0; o < h.p; o += kObsTile) ob_items.push_back({i, 0, o, std::min<int64_t>(h.p, o + kObsTile)});
     for (int64_t s = 0; s < h.n; s += kUpdTile) up_items.push_back({i, 0, s, std::min<int64_t>(h.n, s + kUpdTile)});
@@ -377,6 +603,8 @@ int build(mg_context* ctx, mg_etkf_batch* b) {
     c.Gpart = cv.take<double>((size_t)c.nchunk * h.k * h.k);
     c.bpart = cv.take<double>((size_t)c.nchunk * h.k);
     c.T = cv.take<double>((size_t)h.k * h.k);
+    c.Y32 = f64 ? nullptr : cv.take<float>((size_t)h.p * h.k);
+    c.V1 = f64 ? nullptr : cv.take<float>((size_t)h.k * h.k);
   }
   b->dcases = cv.take<DevCase>(b->ncases);
   b->items = cv.take<WorkItem>(all.size());
@@ -396,6 +624,14 @@ int build(mg_context* ctx, mg_etkf_batch* b) {
   return MG_OK;
 }
 
+// The mixed path with the symmetric square root runs the FP32 two-stage
+// solve; with the Cholesky square root it keeps the FP64 Gram and solve.
+bool mixed_hunt(const mg_etkf_batch* b) {
+  return b->precision == MG_PREC_MIXED && !(b->flags & MG_SQRT_CHOLESKY);
+}
+
+constexpr size_t rebuild_bytes(int kmax) { return sizeof(float) * ((size_t)kmax * (kmax + 1) + 2 * 32 * (size_t)kmax); }
+
 // Enqueues the batch (no allocation, no host synchronisation: capturable).
 int enqueue(mg_context* ctx, mg_etkf_batch* b) {
   cudaStream_t s = ctx->stream;
@@ -413,19 +649,60 @@ int enqueue(mg_context* ctx, mg_etkf_batch* b) {
     batch_prep_obs_kernel<<<(unsigned)b->n_obs_items, kObsTile * 32, 0, s>>>(b->dcases, b->items + b->obs_off);
     MG_COUNT_LAUNCH();
   }
+  const int kp = b->maxk + (b->maxk & 1);
+  if (mixed_hunt(b)) {
+    if (b->gram_cnt[0]) {
+      batch_gram_kernel<float, 32><<<(unsigned)b->gram_cnt[0], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[0]);
+      MG_COUNT_LAUNCH();
+    }
+    if (b->gram_cnt[1]) {
+      batch_gram_kernel<float, 64><<<(unsigned)b->gram_cnt[1], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[1]);
+      MG_COUNT_LAUNCH();
+    }
+    if (b->gram_cnt[2]) {
+      batch_gram_kernel<float, 128><<<(unsigned)b->gram_cnt[2], kThreads, 0, s>>>(b->dcases,
+                                                                                  b->items + b->gram_off[2]);
+      MG_COUNT_LAUNCH();
+    }
+    batch_solve1_kernel<<<(unsigned)b->ncases, kThreads, sizeof(float) * solve1_floats(kp), s>>>(b->dcases, b->flags);
+    MG_COUNT_LAUNCH();
+    if (b->gram_cnt[0]) {
+      batch_rebuild_kernel<32><<<(unsigned)b->gram_cnt[0], kThreads, rebuild_bytes(32), s>>>(b->dcases,
+                                                                                          b->items + b->gram_off[0]);
+      MG_COUNT_LAUNCH();
+    }
+    if (b->gram_cnt[1]) {
+      batch_rebuild_kernel<64><<<(unsigned)b->gram_cnt[1], kThreads, rebuild_bytes(64), s>>>(b->dcases,
+                                                                                          b->items + b->gram_off[1]);
+      MG_COUNT_LAUNCH();
+    }
+    if (b->gram_cnt[2]) {
+      batch_rebuild_kernel<128><<<(unsigned)b->gram_cnt[2], kThreads, rebuild_bytes(128), s>>>(
+          b->dcases, b->items + b->gram_off[2]);
+      MG_COUNT_LAUNCH();
+    }
+    batch_solve2_kernel<<<(unsigned)b->ncases, kThreads, sizeof(float) * solve2_floats(kp), s>>>(b->dcases, b->flags,
+                                                                                                b->status);
+    MG_COUNT_LAUNCH();
+    const size_t usmem = sizeof(float) * ((size_t)b->maxk * b->maxk + 32 * (size_t)(b->maxk + 1));
+    batch_update_kernel<float><<<(unsigned)b->n_update_items, kThreads, usmem, s>>>(b->dcases, b->items + b->update_off,
+                                                                                    b->counters, b->times);
+    MG_COUNT_LAUNCH();
+    MG_TRY_CUDA(cudaGetLastError());
+    return MG_OK;
+  }
   if (b->gram_cnt[0]) {
-    batch_gram_kernel<32><<<(unsigned)b->gram_cnt[0], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[0]);
+    batch_gram_kernel<double, 32><<<(unsigned)b->gram_cnt[0], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[0]);
     MG_COUNT_LAUNCH();
   }
   if (b->gram_cnt[1]) {
-    batch_gram_kernel<64><<<(unsigned)b->gram_cnt[1], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[1]);
+    batch_gram_kernel<double, 64><<<(unsigned)b->gram_cnt[1], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[1]);
     MG_COUNT_LAUNCH();
   }
   if (b->gram_cnt[2]) {
-    batch_gram_kernel<128><<<(unsigned)b->gram_cnt[2], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[2]);
+    batch_gram_kernel<double, 128><<<(unsigned)b->gram_cnt[2], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[2]);
     MG_COUNT_LAUNCH();
   }
-  const int kp = b->maxk + (b->maxk & 1);
   const size_t smem = sizeof(double) * (2 * (size_t)kp * (kp + 1) + 6 * (size_t)kp) + sizeof(int) * (kp + 8) + 64;
   batch_solve_kernel<<<(unsigned)b->ncases, kThreads, smem, s>>>(b->dcases, b->flags, b->status);
   MG_COUNT_LAUNCH();
@@ -449,6 +726,18 @@ int set_attributes(mg_context* ctx, const mg_etkf_batch* b) {
   const size_t usmem = te * ((size_t)b->maxk * b->maxk + 32 * (size_t)(b->maxk + 1));
   if (smem > 227 * 1024 || usmem > 227 * 1024) return mg::fail(ctx, MG_ERR_ARG, "mg_etkf_batch: k too large");
   MG_TRY_CUDA(cudaFuncSetAttribute(batch_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (mixed_hunt(b)) {
+    MG_TRY_CUDA(cudaFuncSetAttribute(batch_solve1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(float) * solve1_floats(kp))));
+    MG_TRY_CUDA(cudaFuncSetAttribute(batch_solve2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(float) * solve2_floats(kp))));
+    MG_TRY_CUDA(cudaFuncSetAttribute(batch_rebuild_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)rebuild_bytes(32)));
+    MG_TRY_CUDA(cudaFuncSetAttribute(batch_rebuild_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)rebuild_bytes(64)));
+    MG_TRY_CUDA(cudaFuncSetAttribute(batch_rebuild_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)rebuild_bytes(128)));
+  }
   if (te == 8)
     MG_TRY_CUDA(cudaFuncSetAttribute(batch_update_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)usmem));
   else

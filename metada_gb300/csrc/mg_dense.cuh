@@ -310,13 +310,21 @@ __device__ __forceinline__ void jacobi_pair(int s, int r, int m, int& p, int& q)
   }
 }
 
-// Rotation (c, s) zeroing apq, and the two rotated diagonal entries.
+// Rotation (c, s) zeroing apq, and the two rotated diagonal entries, for
+// the loose first stage only: the angle comes from the hardware reciprocal
+// square root and approximate division (its error only changes how far the
+// rotation zeroes apq), and c is refined by one Newton step so that
+// c^2 + s^2 = 1 to FP32 rounding (the eigenvector rows stay orthonormal; the
+// Newton-Schulz step after the Jacobi removes the rest).
 __device__ __forceinline__ float4 jacobi_rot(float app, float aqq, float apq, float tol) {
   float c = 1.0f, s = 0.0f, t = 0.0f;
-  if (apq != 0.0f && fabsf(apq) > tol * sqrtf(fabsf(app) * fabsf(aqq))) {
-    const float theta = (aqq - app) / (2.0f * apq);
-    t = (theta >= 0.0f ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
-    c = 1.0f / sqrtf(t * t + 1.0f);
+  if (apq != 0.0f && apq * apq > tol * tol * fabsf(app * aqq)) {
+    const float tau = __fdividef(aqq - app, 2.0f * apq);
+    const float q = fmaf(tau, tau, 1.0f);
+    t = copysignf(__fdividef(1.0f, fabsf(tau) + q * rsqrtf(q)), tau);
+    const float u = fmaf(t, t, 1.0f);
+    const float c0 = rsqrtf(u);
+    c = c0 * fmaf(-0.5f * u * c0, c0, 1.5f);
     s = t * c;
   }
   return make_float4(c, s, app - t * apq, aqq + t * apq);
