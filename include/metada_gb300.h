@@ -299,6 +299,44 @@ int mg_hx_column_mlp(mg_context* ctx, mg_mlp* mlp, const double* X, int32_t k, i
 int mg_gemm_bf16_tc(mg_context* ctx, const void* A, const void* B, int32_t M, int32_t N, int32_t K,
                     const float* bias, int32_t silu, float* C);
 
+/* Stochastic EnKF with perturbed observations, replacing EnKF::Analyse
+ * (src/framework/algorithms/EnKF.hpp:139-254), in place on the members.
+ * HX (p x k row-major) is H of the raw members; obs_pert (p x k row-major)
+ * the observation perturbations eps_i (the reference draws them inside,
+ * from an unseeded generator, chol_L(R) z with z ~ N(0, 1), :336-352; here
+ * the caller supplies them, so runs are reproducible).  The perturbations
+ * are inflated by sqrt(inflation) for every inflation method (:322-335).
+ * Computed in the k-dimensional form (no p x p matrix).  mean_out: the
+ * recomputed analysis mean (device, n, may be NULL); diag (host, may be
+ * NULL): ||yo - mean(HX)||, background and analysis spread.  MG_PREC_MIXED
+ * runs the O(n k^2) update in FP32.  2 <= k <= 112. */
+typedef struct mg_enkf_diag {
+  double innovation_norm;
+  double background_spread;
+  double analysis_spread;
+} mg_enkf_diag;
+int mg_enkf(mg_context* ctx, double* X, int64_t n, int32_t k, int64_t ld, const double* HX, const double* yo,
+            const double* rvar, const double* obs_pert, int64_t p, double inflation, int32_t precision,
+            double* mean_out, mg_enkf_diag* diag);
+
+/* Ensemble diagnostics, replacing Metrics<double>::CalculateAll
+ * (src/framework/algorithms/Metrics.hpp:74-94): for members X (k x n,
+ * member i at X + i*ld, device) against truth (n, device), the ensemble mean
+ * and spread per element (device, n each, may be NULL; the mean is the
+ * member-order sum divided by k, the spread sqrt(sum (x - mean)^2 / (k-1)),
+ * both as the reference computes them) and, on the host, RMSE and bias of
+ * the mean, its correlation with the truth (single-pass sums formula),
+ * CRPS (pair-sum form) and the average spread.  2 <= k <= 256. */
+typedef struct mg_ens_metrics_t {
+  double rmse;
+  double bias;
+  double correlation;
+  double crps;
+  double avg_spread;
+} mg_ens_metrics_t;
+int mg_ens_metrics(mg_context* ctx, const double* X, int64_t n, int32_t k, int64_t ld, const double* truth,
+                   double* mean_out, double* spread_out, mg_ens_metrics_t* out);
+
 /* Statistics of the last mg_letkf_batched call (host). */
 typedef struct mg_letkf_stats {
   int64_t n_points;      /* local analyses run */

@@ -108,6 +108,17 @@ class LetkfStats(Structure):
     ]
 
 
+class EnkfDiag(Structure):
+    """mg_enkf_diag."""
+    _fields_ = [("innovation_norm", c_double), ("background_spread", c_double), ("analysis_spread", c_double)]
+
+
+class EnsMetrics(Structure):
+    """mg_ens_metrics_t."""
+    _fields_ = [("rmse", c_double), ("bias", c_double), ("correlation", c_double), ("crps", c_double),
+                ("avg_spread", c_double)]
+
+
 # name -> argtypes (every function returns int unless listed in _RESTYPES)
 _SIGNATURES = {
     "mg_create": [POINTER(c_void_p), c_int],
@@ -153,6 +164,10 @@ _SIGNATURES = {
     "mg_mlp_train_step": [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, ctypes.c_float, POINTER(ctypes.c_float)],
     "mg_hx_column_mlp": [c_void_p, c_void_p, c_void_p, c_int32, c_int64, c_int64, c_int32, c_void_p, c_void_p, c_int64,
                          c_void_p],
+    "mg_enkf": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_int64,
+                c_double, c_int32, c_void_p, POINTER(EnkfDiag)],
+    "mg_ens_metrics": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p,
+                       POINTER(EnsMetrics)],
     "mg_gemm_bf16_tc": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p],
     "mg_etkf_noalloc": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
                         c_double, c_int32, c_int32, c_void_p],

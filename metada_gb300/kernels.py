@@ -62,6 +62,33 @@ def ens_mean_pert(X: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
     return mean, Xp
 
 
+def enkf(X: torch.Tensor, HX: torch.Tensor, yo: torch.Tensor, rvar: torch.Tensor, obs_pert: torch.Tensor,
+         inflation: float, precision: int = _lib.MG_PREC_FP64) -> tuple[torch.Tensor, dict]:
+    """Stochastic EnKF in place on X (k x n); returns (analysis mean, diagnostics)."""
+    _need(X, torch.float64, "X")
+    k, n = X.shape
+    p = yo.shape[0]
+    mean = torch.empty(n, dtype=torch.float64, device=X.device)
+    d = _lib.EnkfDiag()
+    context(X.device.index).call("mg_enkf", _ptr(X), n, k, n, _ptr(HX), _ptr(yo), _ptr(rvar), _ptr(obs_pert), p,
+                                 float(inflation), precision, _ptr(mean), byref(d))
+    return mean, {f: getattr(d, f) for f, _ in d._fields_}
+
+
+def ens_metrics(X: torch.Tensor, truth: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor, dict]:
+    """Ensemble diagnostics of members X (k x n, float64) against truth (n):
+    (mean, spread, {rmse, bias, correlation, crps, avg_spread})."""
+    _need(X, torch.float64, "X")
+    _need(truth, torch.float64, "truth")
+    k, n = X.shape
+    mean = torch.empty(n, dtype=torch.float64, device=X.device)
+    spread = torch.empty(n, dtype=torch.float64, device=X.device)
+    out = _lib.EnsMetrics()
+    context(X.device.index).call("mg_ens_metrics", _ptr(X), n, k, n, _ptr(truth), _ptr(mean), _ptr(spread),
+                                 byref(out))
+    return mean, spread, {f: getattr(out, f) for f, _ in out._fields_}
+
+
 def hx_idw4(X: torch.Tensor, nx: int, ny: int, obs_xy: torch.Tensor,
             valid: torch.Tensor | None = None) -> torch.Tensor:
     """IDW4 obs operator for grid obs; returns HX (p x k)."""

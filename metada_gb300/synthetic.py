@@ -229,7 +229,12 @@ def trilinear_h(field: np.ndarray, nlon, nlat, nlev, lat, lon, lev, var) -> np.n
 def latlon_letkf_case(nlon: int = 360, nlat: int = 180, nlev: int = 10, nvar: int = 4, k: int = 64,
                       p: int = 500_000, T: int = 90, slope: float = -3.0, sigma_o: float = 1.0,
                       hsupport_km: float = 500.0, vsupport: float = 2.0, rho: float = 1.05,
-                      alpha_v: float = 0.7, case: int = 2) -> LatLonCase:
+                      alpha_v: float = 0.7, case: int = 2, clustered: float = 0.0, n_patches: int = 20,
+                      patch_km: float = 800.0) -> LatLonCase:
+    """Lat-lon LETKF configuration: spherical-harmonic fields (slope, T),
+    AR(1) vertical correlation, p point obs at random levels and variables.
+    A fraction `clustered` of the obs lies in n_patches seeded Gaussian
+    patches (standard deviation patch_km), the rest uniform on the sphere."""
     g = rng(case, 0)
     nfield = (k + 1) * nvar * nlev
     F = sh_random_fields(nfield, nlat, nlon, T, slope, g)
@@ -240,13 +245,24 @@ def latlon_letkf_case(nlon: int = 360, nlat: int = 180, nlev: int = 10, nvar: in
     g2 = rng(case, 1)
     obs_lat = np.rad2deg(np.arcsin(g2.uniform(-1.0, 1.0, p)))
     obs_lon = g2.uniform(0.0, 360.0, p)
+    if clustered > 0.0:
+        gc = rng(case, 3)
+        nc = int(round(clustered * p))
+        clat = np.rad2deg(np.arcsin(gc.uniform(-0.9, 0.9, n_patches)))
+        clon = gc.uniform(0.0, 360.0, n_patches)
+        which = gc.integers(0, n_patches, nc)
+        s_deg = np.rad2deg(patch_km / 6371.0)
+        lat = clat[which] + s_deg * gc.standard_normal(nc)
+        lon = clon[which] + s_deg * gc.standard_normal(nc) / np.cos(np.deg2rad(clat[which]))
+        obs_lat[:nc] = np.clip(lat, -89.9, 89.9)
+        obs_lon[:nc] = np.mod(lon, 360.0)
     obs_lev = g2.uniform(0.0, nlev - 1.0, p)
     obs_var = g2.integers(0, nvar, p).astype(np.int32)
     so = float_config(sigma_o)
     yo = trilinear_h(truth, nlon, nlat, nlev, obs_lat, obs_lon, obs_lev, obs_var) + so * rng(case, 2).standard_normal(p)
     return LatLonCase(nlon, nlat, nlev, nvar, truth, np.ascontiguousarray(X), obs_lat, obs_lon, obs_lev, obs_var,
                       yo, so, hsupport_km, vsupport, float_config(rho),
-                      meta={"T": T, "slope": slope, "alpha_v": alpha_v, "case": case})
+                      meta={"T": T, "slope": slope, "alpha_v": alpha_v, "case": case, "clustered": clustered})
 
 
 def write_simple_state(path, values: np.ndarray, nx: int, ny: int) -> None:

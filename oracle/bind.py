@@ -54,6 +54,8 @@ def load() -> ctypes.CDLL:
                                   vp, c_double, c_int32, vp], ctypes.c_int),
             "orc_sym_eig": ([vp, c_int32, vp, vp], ctypes.c_int),
             "orc_column_op": ([vp, vp, c_int64, c_int32, vp, vp, c_int32, vp], None),
+            "orc_ens_metrics": ([vp, c_int64, c_int32, c_int64, vp, vp, vp, vp], None),
+            "orc_enkf": ([vp, c_int64, c_int32, c_int64, vp, vp, vp, vp, c_int64, c_double, vp, vp, vp], ctypes.c_int),
             "orc_num_threads": ([], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
@@ -210,6 +212,37 @@ def column_op(T, q, w, tau):
     y = np.empty((ncol, nch), dtype=np.float32)
     load().orc_column_op(_p(T), _p(q), ncol, nlev, _p(w), _p(tau), nch, _p(y))
     return y
+
+
+def ens_metrics(X, truth):
+    """Metrics<double>::CalculateAll: (mean, spread, {rmse, bias, correlation,
+    crps, avg_spread}) of members X (k x n)."""
+    X = _f64(X)
+    truth = _f64(truth)
+    k, n = X.shape
+    mean = np.empty(n)
+    spread = np.empty(n)
+    out = np.empty(5)
+    load().orc_ens_metrics(_p(X), n, k, n, _p(truth), _p(mean), _p(spread), _p(out))
+    return mean, spread, dict(zip(("rmse", "bias", "correlation", "crps", "avg_spread"), out.tolist()))
+
+
+def enkf(X, HX, yo, rvar, eps, rho):
+    """Dense-form stochastic EnKF: (analysed members, analysis mean,
+    {innovation_norm, background_spread, analysis_spread}, (max, min) gain)."""
+    X = np.array(X, dtype=np.float64, order="C", copy=True)
+    HX, yo, rvar, eps = _f64(HX), _f64(yo), _f64(rvar), _f64(eps)
+    k, n = X.shape
+    p = yo.shape[0]
+    mean = np.empty(n)
+    diag = np.empty(3)
+    gain = np.empty(2)
+    rc = load().orc_enkf(_p(X), n, k, n, _p(HX), _p(yo), _p(rvar), _p(eps), p, float(rho), _p(mean), _p(diag),
+                         _p(gain))
+    if rc != 0:
+        raise RuntimeError("orc_enkf: S is singular")
+    return X, mean, dict(zip(("innovation_norm", "background_spread", "analysis_spread"), diag.tolist())), \
+        tuple(gain.tolist())
 
 
 def num_threads() -> int:

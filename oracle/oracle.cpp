@@ -590,7 +590,151 @@ int orc_letkf_points(const double* X, int32_t k, int64_t ld, const int64_t* pt_b
   return status;
 }
 
+// Stochastic EnKF, EnKF.hpp:139-254, in the reference's dense form:
+// perturbations inflated by sqrt(rho) (applyInflation :322-335), Yb from the
+// raw members, S = Y'Y'^T/(k-1) + R (p x p, :193-196), K = X'Y'^T S^-1/(k-1)
+// (:199, S^-1 by LU with partial pivoting as MatrixXd::inverse()),
+// xa_i = xm + X'_i + K (yo + eps_i - Yb_i) (:215-224) with the obs
+// perturbations eps given (the reference draws them from an unseeded
+// generator, :336-352), then the mean recomputed (:237).  diag3 = {||d||,
+// background spread, analysis spread} (:184, :334, :240-253); gain2 = {max,
+// min} of K (:201-202), may be NULL.
+int orc_enkf(double* X, int64_t n, int32_t k, int64_t ld, const double* HX, const double* yo,
+             const double* rvar, const double* eps, int64_t p, double rho, double* mean_out, double* diag3,
+             double* gain2) {
+  std::vector<double> mean(n), Xp((size_t)n * k);
+  orc_ens_mean(X, n, k, ld, mean.data());
+  const double sr = std::sqrt(rho);
+  double bss = 0.0;
+  for (int64_t s = 0; s < n; ++s)
+    for (int i = 0; i < k; ++i) {
+      const double v = (X[(int64_t)i * ld + s] - mean[s]) * sr;
+      Xp[(size_t)i * n + s] = v;
+      bss += v * v;
+    }
+  std::vector<double> Yp((size_t)p * k), d(p);
+  double dn = 0.0;
+  for (int64_t o = 0; o < p; ++o) {
+    double s = 0.0;
+    for (int i = 0; i < k; ++i) s += HX[o * k + i];
+    const double ym = s / (double)k;
+    for (int i = 0; i < k; ++i) Yp[o * k + i] = HX[o * k + i] - ym;
+    d[o] = yo[o] - ym;
+    dn += d[o] * d[o];
+  }
+  std::vector<double> S((size_t)p * p), Si((size_t)p * p);
+  for (int64_t a = 0; a < p; ++a)
+    for (int64_t b = 0; b < p; ++b) {
+      double s = 0.0;
+      for (int i = 0; i < k; ++i) s += Yp[a * k + i] * Yp[b * k + i];
+      S[(size_t)a * p + b] = s / (double)(k - 1) + (a == b ? rvar[a] : 0.0);
+    }
+  if (!lu_inverse(S.data(), (int)p, Si.data())) return -1;
+  // M = Y'^T S^-1 (k x p); K = X' M / (k - 1) (n x p).
+  std::vector<double> M((size_t)k * p, 0.0);
+  for (int i = 0; i < k; ++i)
+    for (int64_t b = 0; b < p; ++b) {
+      double s = 0.0;
+      for (int64_t a = 0; a < p; ++a) s += Yp[a * k + i] * Si[(size_t)a * p + b];
+      M[(size_t)i * p + b] = s;
+    }
+  double kmax = -1e300, kmin = 1e300;
+  std::vector<double> Krow(p), Xa((size_t)n * k);
+  for (int64_t s = 0; s < n; ++s) {
+    for (int64_t b = 0; b < p; ++b) {
+      double v = 0.0;
+      for (int i = 0; i < k; ++i) v += Xp[(size_t)i * n + s] * M[(size_t)i * p + b];
+      v /= (double)(k - 1);
+      Krow[b] = v;
+      kmax = std::max(kmax, v);
+      kmin = std::min(kmin, v);
+    }
+    for (int i = 0; i < k; ++i) {
+      double inc = 0.0;
+      for (int64_t b = 0; b < p; ++b) inc += Krow[b] * ((yo[b] + eps[b * k + i]) - HX[b * k + i]);
+      Xa[(size_t)i * n + s] = mean[s] + (Xp[(size_t)i * n + s] + inc);
+    }
+  }
+  for (int i = 0; i < k; ++i)
+    for (int64_t s = 0; s < n; ++s) X[(int64_t)i * ld + s] = Xa[(size_t)i * n + s];
+  std::vector<double> am(n);
+  orc_ens_mean(X, n, k, ld, am.data());
+  double ass = 0.0;
+  for (int i = 0; i < k; ++i)
+    for (int64_t s = 0; s < n; ++s) {
+      const double v = X[(int64_t)i * ld + s] - am[s];
+      ass += v * v;
+    }
+  if (mean_out) std::memcpy(mean_out, am.data(), sizeof(double) * n);
+  if (diag3) {
+    diag3[0] = std::sqrt(dn);
+    diag3[1] = std::sqrt(bss / ((double)n * k));
+    diag3[2] = std::sqrt(ass / ((double)k * n));
+  }
+  if (gain2) {
+    gain2[0] = kmax;
+    gain2[1] = kmin;
+  }
+  return 0;
+}
+
 int orc_sym_eig(double* A, int32_t k, double* w, double* V) { return jacobi_eig(A, k, w, V); }
+
+// Metrics<double>::CalculateAll (Metrics.hpp:74-94) and the functions it
+// calls, in their order: mean by member-order sums then a division by k
+// (:108-121), spread sqrt(sum (x - mean)^2 / (k - 1)) (:137-150), RMSE
+// (:265-273), bias (:166-173), correlation by the single-pass sums formula
+// (:189-206), CRPS with the O(k^2) pair sum per element (:232-252), average
+// spread (:286-293).  Sequential sums over the state, as the reference.
+void orc_ens_metrics(const double* X, int64_t n, int32_t k, int64_t ld, const double* truth, double* mean,
+                     double* spread, double* out5) {
+  for (int64_t i = 0; i < n; ++i) mean[i] = 0.0;
+  for (int j = 0; j < k; ++j)
+    for (int64_t i = 0; i < n; ++i) mean[i] += X[(int64_t)j * ld + i];
+  for (int64_t i = 0; i < n; ++i) mean[i] /= (double)k;
+  for (int64_t i = 0; i < n; ++i) spread[i] = 0.0;
+  for (int j = 0; j < k; ++j)
+    for (int64_t i = 0; i < n; ++i) {
+      const double d = X[(int64_t)j * ld + i] - mean[i];
+      spread[i] += d * d;
+    }
+  for (int64_t i = 0; i < n; ++i) spread[i] = std::sqrt(spread[i] / (double)(k - 1));
+  double rmse = 0.0, bias = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double d = mean[i] - truth[i];
+    rmse += d * d;
+  }
+  rmse = std::sqrt(rmse / (double)n);
+  for (int64_t i = 0; i < n; ++i) bias += mean[i] - truth[i];
+  bias /= (double)n;
+  double sx = 0.0, sy = 0.0, sxy = 0.0, sx2 = 0.0, sy2 = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    sx += mean[i];
+    sy += truth[i];
+    sxy += mean[i] * truth[i];
+    sx2 += mean[i] * mean[i];
+    sy2 += truth[i] * truth[i];
+  }
+  const double nn = (double)n;
+  const double corr = (nn * sxy - sx * sy) / std::sqrt((nn * sx2 - sx * sx) * (nn * sy2 - sy * sy));
+  double crps = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    double sd = 0.0, st = 0.0;
+    for (int j = 0; j < k; ++j)
+      for (int l = 0; l < k; ++l) sd += std::fabs(X[(int64_t)j * ld + i] - X[(int64_t)l * ld + i]);
+    for (int j = 0; j < k; ++j) st += std::fabs(X[(int64_t)j * ld + i] - truth[i]);
+    crps += st / (double)k - sd / (2.0 * k * k);
+  }
+  crps /= (double)n;
+  double avg = 0.0;
+  for (int64_t i = 0; i < n; ++i) avg += spread[i];
+  avg /= (double)n;
+  out5[0] = rmse;
+  out5[1] = bias;
+  out5[2] = corr;
+  out5[3] = crps;
+  out5[4] = avg;
+}
 
 void orc_column_op(const float* T, const float* q, int64_t ncol, int32_t nlev, const float* w,
                    const float* tau, int32_t nch, float* y) {

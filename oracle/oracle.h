@@ -131,6 +131,15 @@ int orc_letkf_points(const double* X, int32_t k, int64_t ld,
                      const double* loc_w, double rho, int32_t flags,
                      double* out);
 
+/* Stochastic EnKF, EnKF.hpp:139-254, dense p x p form, in place on the
+ * members; eps (p x k row-major) are the obs perturbations the reference
+ * would draw.  mean_out: analysis mean; diag3 = {||yo - ym||, background
+ * spread, analysis spread}; gain2 = {max, min} of the gain (may be NULL).
+ * Returns 0, or -1 if S is singular. */
+int orc_enkf(double* X, int64_t n, int32_t k, int64_t ld, const double* HX, const double* yo,
+             const double* rvar, const double* eps, int64_t p, double rho, double* mean_out, double* diag3,
+             double* gain2);
+
 /* Symmetric eigen-decomposition by cyclic Jacobi (FP64), A = V diag(w) V^T.
  * A (k x k, row-major) is overwritten.  Returns the number of sweeps. */
 int orc_sym_eig(double* A, int32_t k, double* w, double* V);
@@ -140,6 +149,12 @@ int orc_sym_eig(double* A, int32_t k, double* w, double* V);
  * and nch channels; T and q are ncol x nlev row-major, y ncol x nch. */
 void orc_column_op(const float* T, const float* q, int64_t ncol, int32_t nlev,
                    const float* w, const float* tau, int32_t nch, float* y);
+
+/* Ensemble diagnostics, Metrics<double>::CalculateAll (Metrics.hpp:74-94):
+ * mean and spread per state element (n each), and out5 = {RMSE, bias,
+ * correlation, CRPS, average spread}.  Members start at X + j*ld. */
+void orc_ens_metrics(const double* X, int64_t n, int32_t k, int64_t ld, const double* truth, double* mean,
+                     double* spread, double* out5);
 
 /* Number of OpenMP threads the oracle uses. */
 int orc_num_threads(void);

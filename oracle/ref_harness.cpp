@@ -8,12 +8,31 @@
 // (the reference's YAML backend needs yaml-cpp, which is not installed).
 // Output goes to oracle/_ref/ and is never shipped.
 //
-// usage: ref_harness etkf|letkf NX NY K ENS_PREFIX OBS_FILE ERROR INFLATION
-//                    RADIUS OUT_DIR
+// usage: ref_harness etkf|letkf|enkf NX NY K ENS_PREFIX OBS_FILE ERROR
+//                    INFLATION RADIUS OUT_DIR [SEED]
 //   reads ENS_PREFIX<i>.txt (i = 1..K, SimpleState text) and OBS_FILE
 //   (GridObservation text format, grid coordinates); writes the analysed
 //   members as raw little-endian doubles to OUT_DIR/member_<i>.bin
-//   (i = 0..K-1) and Ensemble::Mean() to OUT_DIR/mean.bin.
+//   (i = 0..K-1) and Ensemble::Mean() to OUT_DIR/mean.bin.  For enkf, the
+//   reference's std::random_device is replaced at compile time by a device
+//   that returns SEED, so its std::mt19937 / std::normal_distribution draw a
+//   reproducible sequence; the harness draws the same sequence again and
+//   writes the perturbations it produced (obs-major, p x k) to
+//   OUT_DIR/obs_pert.bin, and {||d||, background spread, analysis spread,
+//   max gain, min gain} from getAnalysisResults() to OUT_DIR/enkf_diag.bin.
+#include <random>
+
+namespace harness {
+inline unsigned int g_seed = 0;
+}
+namespace std {
+// Stands in for std::random_device inside EnKF.hpp (see the macro below).
+struct harness_seeded_device {
+  using result_type = unsigned int;
+  result_type operator()() { return harness::g_seed; }
+};
+}  // namespace std
+
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -32,6 +51,9 @@
 #include "Geometry.hpp"
 #include "IdentityControlVariableBackend.hpp"
 #include "LETKF.hpp"
+#define random_device harness_seeded_device
+#include "EnKF.hpp"
+#undef random_device
 #include "Logger.hpp"
 #include "ObsOperator.hpp"
 #include "Observation.hpp"
@@ -47,11 +69,12 @@ static void dump(const std::string& path, const double* p, size_t n) {
 
 int main(int argc, char** argv) {
   try {
-    if (argc != 11) {
-      std::cerr << "usage: ref_harness etkf|letkf NX NY K ENS_PREFIX OBS_FILE ERROR INFLATION "
-                   "RADIUS OUT_DIR\n";
+    if (argc != 11 && argc != 12) {
+      std::cerr << "usage: ref_harness etkf|letkf|enkf NX NY K ENS_PREFIX OBS_FILE ERROR INFLATION "
+                   "RADIUS OUT_DIR [SEED]\n";
       return 2;
     }
+    if (argc == 12) harness::g_seed = (unsigned int)std::strtoul(argv[11], nullptr, 10);
     const std::string algo = argv[1];
     const int nx = std::atoi(argv[2]), ny = std::atoi(argv[3]), k = std::atoi(argv[4]);
     const std::string ens_prefix = argv[5], obs_file = argv[6];
@@ -82,6 +105,7 @@ int main(int argc, char** argv) {
     std::vector<fw::ConfigValue> types{fw::ConfigValue(fw::ConfigMap{{"obs_A", type_cfg}})};
     fw::ConfigMap analysis{{"algorithm", fw::ConfigValue(algo)},
                            {"inflation", fw::ConfigValue(inflation)},
+                           {"inflation_method", fw::ConfigValue("multiplicative")},
                            {"localization_radius", fw::ConfigValue(radius)},
                            {"format", fw::ConfigValue("txt")},
                            {"output_base_file", fw::ConfigValue(out + "/analysis")}};
@@ -111,6 +135,24 @@ int main(int argc, char** argv) {
     } else if (algo == "letkf") {
       fw::LETKF<Tag> letkf(ensemble, observations, obs_operator, config.GetSubsection("analysis"));
       letkf.Analyse();
+    } else if (algo == "enkf") {
+      // EnKF reads the "analysis" subsection itself (EnKF.hpp:109).
+      fw::EnKF<Tag> enkf(ensemble, observations, obs_operator, config);
+      enkf.Analyse();
+      const auto r = enkf.getAnalysisResults();
+      const double dg[5] = {r.innovation_norm, r.background_spread, r.analysis_spread, r.max_kalman_gain,
+                            r.min_kalman_gain};
+      dump(out + "/enkf_diag.bin", dg, 5);
+      // The same draws as generateObservationPerturbations (EnKF.hpp:340-360)
+      // with R = sigma^2 I (chol_L(R) = sigma I).
+      const int p = (int)observations.size();
+      std::mt19937 gen(harness::g_seed);
+      std::normal_distribution<double> dist(0.0, 1.0);
+      const auto cov = observations.getCovariance();
+      std::vector<double> eps((size_t)p * k);
+      for (int i = 0; i < p; ++i)
+        for (int j = 0; j < k; ++j) eps[(size_t)i * k + j] = std::sqrt(cov[(size_t)i]) * dist(gen);
+      dump(out + "/obs_pert.bin", eps.data(), eps.size());
     } else {
       throw std::runtime_error("unknown algorithm " + algo);
     }

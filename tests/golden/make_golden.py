@@ -9,7 +9,11 @@ from the reference tree) on:
   * the seeded 64 x 64, 32-member, 1024-observation global ETKF case
     (inflation 1.05, error 0.5);
   * two seeded small-grid LETKF cases (some grid points without local
-    observations).
+    observations);
+  * the stochastic EnKF (EnKF.hpp) on the tutorial data and on the seeded
+    64 x 64 case, with the harness's seeded generator in place of the
+    reference's std::random_device; the perturbations it drew are stored
+    with the outputs.
 
 Run from the repository root, in a checkout that has the reference tree:
     python tests/golden/make_golden.py [REFERENCE_ROOT]
@@ -66,10 +70,10 @@ def read_grid_obs(path: Path, missing: float = -999.0):
 
 
 def run_harness(algo: str, nx: int, ny: int, k: int, ens_prefix: str, obs_file: str, error: float,
-                rho: float, radius: float, out: Path) -> tuple[np.ndarray, np.ndarray]:
+                rho: float, radius: float, out: Path, seed: int | None = None) -> tuple[np.ndarray, np.ndarray]:
     out.mkdir(parents=True, exist_ok=True)
     cmd = [str(HARNESS), algo, str(nx), str(ny), str(k), ens_prefix, obs_file, repr(error), repr(rho),
-           repr(radius), str(out)]
+           repr(radius), str(out)] + ([str(seed)] if seed is not None else [])
     subprocess.run(cmd, check=True)
     n = nx * ny
     members = np.stack([np.fromfile(out / f"member_{i}.bin", dtype="<f8", count=n) for i in range(k)])
@@ -139,6 +143,31 @@ def main(ref_root: str | None = None) -> None:
             np.savez_compressed(HERE / f"{name}.npz", X=Xr, obs_xy=c.obs_xy, yo=yor, sigma=c.sigma_o, rho=c.rho,
                                 radius=c.radius, nx=c.nx, ny=c.ny, members=m, mean=mu)
             print(f"{name}.npz", m.shape)
+
+        # --- stochastic EnKF (seeded perturbations) ---
+        outs = {}
+        m, mu = run_harness("enkf", nx, ny, k, str(tut / "ens_"), str(tut / "obs_format.txt"), 0.1, 1.0, 0.0,
+                            tmp / "enkf_tut", seed=1234)
+        p = len(yo)
+        outs.update(tut_members=m, tut_mean=mu,
+                    tut_eps=np.fromfile(tmp / "enkf_tut" / "obs_pert.bin", dtype="<f8").reshape(p, k),
+                    tut_diag=np.fromfile(tmp / "enkf_tut" / "enkf_diag.bin", dtype="<f8"))
+        c = syn.global_etkf_grid(case=5)
+        d = tmp / "enkf_c1"
+        d.mkdir()
+        ens, obsf = grid_case_to_files(c, d)
+        kc = c.X.shape[0]
+        m, mu = run_harness("enkf", c.nx, c.ny, kc, ens, obsf, 0.5, 1.05, 0.0, d / "out", seed=7)
+        Xr = np.stack([read_simple_state(d / f"ens_{i + 1}.txt") for i in range(kc)])
+        _, yor = read_grid_obs(Path(obsf))
+        pc = len(yor)
+        outs.update(c1_X=Xr, c1_obs_xy=c.obs_xy, c1_yo=yor, c1_sigma=c.sigma_o, c1_rho=syn.float_config(1.05),
+                    c1_members=m, c1_mean=mu,
+                    c1_eps=np.fromfile(d / "out" / "obs_pert.bin", dtype="<f8").reshape(pc, kc),
+                    c1_diag=np.fromfile(d / "out" / "enkf_diag.bin", dtype="<f8"))
+        np.savez_compressed(HERE / "enkf.npz", tut_X=X, tut_obs_xy=obs_xy, tut_yo=yo, tut_sigma=sigma, nx=nx, ny=ny,
+                            c1_nx=c.nx, c1_ny=c.ny, **outs)
+        print("enkf.npz", {k2: np.shape(v) for k2, v in outs.items()})
 
 
 if __name__ == "__main__":

@@ -164,6 +164,37 @@ def test_letkf_latlon_small_matches_oracle(dev, precision, k):
     assert st.total_local > 0 and st.max_local > 0
 
 
+@pytest.mark.parametrize("precision", [_lib.MG_PREC_FP64, _lib.MG_PREC_MIXED])
+def test_letkf_highres_shape_rtps_k80(dev, precision):
+    """The high-resolution configuration's analysis at reduced size: k = 80
+    (the k <= 96 kernels), 60 % of the obs in 20 Gaussian patches (strongly
+    uneven local counts), 300 km support, RTPS with alpha = 0.9; against the
+    oracle on a sample of columns."""
+    c = syn.latlon_letkf_case(nlon=144, nlat=72, nlev=6, nvar=4, k=80, p=40_000, T=40, hsupport_km=300.0,
+                              rho=0.9, case=33, clustered=0.6)
+    Xd, HX, off, idx, dist, st = _run_latlon(dev, c, precision, flags=_lib.MG_RTPS)
+    counts = np.diff(off)
+    assert counts.max() > 8 * max(1.0, np.median(counts))  # the patches make the counts uneven
+    cols = np.random.default_rng(3).choice(c.nlat * c.nlon, 300, replace=False)
+    base, want = _oracle_latlon(c, HX.cpu().numpy(), off, idx, dist, cols, flags=ob.ORC_RTPS)
+    got = Xd.cpu().numpy()
+    gv = np.stack([got[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)
+    tol = FP64_TOL if precision == _lib.MG_PREC_FP64 else MIXED_TOL
+    assert rel_err(gv, want) <= tol
+
+
+@pytest.mark.parametrize("k", [2, 33, 47])
+def test_letkf_mixed_odd_member_counts(dev, k):
+    """Member counts that pad the k x k system (odd k) or leave lanes idle."""
+    c = _latlon_case(72, 36, 4, 2, k, 15_000, 20, case=34)
+    Xd, HX, off, idx, dist, st = _run_latlon(dev, c, _lib.MG_PREC_MIXED)
+    cols = np.arange(c.nlat * c.nlon)
+    base, want = _oracle_latlon(c, HX.cpu().numpy(), off, idx, dist, cols)
+    got = Xd.cpu().numpy()
+    gv = np.stack([got[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)
+    assert rel_err(gv, want) <= MIXED_TOL
+
+
 @pytest.mark.slow
 def test_letkf_latlon_full_size_sampled(dev):
     """The 360 x 180 x 10 x 4, 64-member, 500k-obs configuration: FP64 and

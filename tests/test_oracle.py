@@ -180,3 +180,46 @@ def test_column_operator_formula(built):
     cq = np.cumsum(q[c].astype(np.float64))
     want = np.sum(w[ch].astype(np.float64) * np.exp(-float(tau[ch]) * cq) * T[c].astype(np.float64) ** 4 / 1e8)
     assert abs(y[c, ch] - want) <= 1e-6 * abs(want)
+
+
+# Known-answer tests of Metrics<double>::CalculateAll, from the reference's
+# own tests (tests/framework/algorithms/MetricsTest.cpp:28-42 fixture,
+# expectations at :64-200): truth [1, 2, 3, 4]; members truth + 0.1,
+# truth - 0.1, truth.
+METRICS_TRUTH = np.array([1.0, 2.0, 3.0, 4.0])
+METRICS_MEMBERS = np.array([[1.1, 2.1, 3.1, 4.1], [0.9, 1.9, 2.9, 3.9], [1.0, 2.0, 3.0, 4.0]])
+METRICS_UNCORRELATED = np.array([[10.0, 2.0, 300.0, 4.0], [4.0, 3.0, 20.0, 1.0], [2.0, 30.0, 1.0, 43.0]])
+
+
+def test_metrics_match_reference_known_answers(built):
+    mean, spread, m = ob.ens_metrics(METRICS_MEMBERS, METRICS_TRUTH)
+    np.testing.assert_allclose(mean, METRICS_TRUTH, atol=1e-6)
+    np.testing.assert_allclose(spread, 0.1, atol=1e-6)
+    assert abs(m["bias"]) <= 1e-6
+    assert abs(m["correlation"] - 1.0) <= 1e-6
+    assert abs(m["crps"] - 0.022222222222222227) <= 1e-6 and m["crps"] > 0
+    assert abs(m["rmse"]) <= 1e-6
+    assert abs(m["avg_spread"] - 0.1) <= 1e-6
+    _, _, b = ob.ens_metrics(METRICS_MEMBERS + 0.5, METRICS_TRUTH)
+    assert abs(b["bias"] - 0.5) <= 1e-6 and abs(b["rmse"] - 0.5) <= 1e-6 and abs(b["correlation"] - 1.0) <= 1e-6
+    _, _, u = ob.ens_metrics(METRICS_UNCORRELATED, METRICS_TRUTH)
+    assert abs(u["correlation"] - 0.34105511573854358) <= 1e-6
+    assert u["rmse"] > 1.0 and u["crps"] > 1.0
+
+
+@pytest.mark.parametrize("which", ["tut", "c1"])
+def test_enkf_matches_reference(built, which):
+    """The dense EnKF restatement against the reference's own EnKF.hpp, run by
+    the header harness with a seeded generator (tests/golden/enkf.npz)."""
+    g = np.load(GOLDEN / "enkf.npz")
+    X, xy, yo = g[f"{which}_X"], g[f"{which}_obs_xy"], g[f"{which}_yo"]
+    nx, ny = (int(g["nx"]), int(g["ny"])) if which == "tut" else (int(g["c1_nx"]), int(g["c1_ny"]))
+    s = float(g[f"{which}_sigma"])
+    rho = 1.0 if which == "tut" else float(g["c1_rho"])
+    HX = ob.hx_idw4(X, nx, ny, xy)
+    Xa, mean, diag, gain = ob.enkf(X, HX, yo, np.full(len(yo), s * s), g[f"{which}_eps"], rho)
+    assert rel_err(Xa, g[f"{which}_members"]) <= 1e-10
+    assert rel_err(mean, g[f"{which}_mean"]) <= 1e-10
+    want = g[f"{which}_diag"]
+    got = [diag["innovation_norm"], diag["background_spread"], diag["analysis_spread"], gain[0], gain[1]]
+    np.testing.assert_allclose(got, want, rtol=1e-10)
