@@ -1,6 +1,7 @@
 // Drop-in GPU analysis policies for METADA.
 //
-// metada_gb300::ETKF<Tag> and metada_gb300::LETKF<Tag> keep the signature and
+// metada_gb300::ETKF<Tag>, LETKF<Tag> and EnKF<Tag> (with Metrics<T>) keep the
+// signature and
 // behaviour of the reference policies (src/framework/algorithms/ETKF.hpp:76-210,
 // LETKF.hpp:37-253): construct from (Ensemble&, Observation&, const
 // ObsOperator&, const Config&), call Analyse(), then saveEnsemble().  A METADA
@@ -33,8 +34,12 @@
 #include <cmath>
 #include <cstdint>
 #include <functional>
+#include <iomanip>
 #include <limits>
 #include <memory>
+#include <ostream>
+#include <random>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -385,6 +390,190 @@ class LETKF {
   mg_letkf_stats stats_{};
   std::function<void()> analyse_;
   std::function<void()> save_;
+};
+
+// Stochastic EnKF with perturbed observations on the GPU (EnKF.hpp:66-254).
+// Constructed like the reference from the root configuration (it reads the
+// "analysis" subsection itself, EnKF.hpp:109): inflation, inflation_method,
+// output_base_file, format, plus precision and seed.  The perturbations are
+// chol_L(R) z with z drawn obs-major from std::mt19937 and
+// std::normal_distribution<double> as generateObservationPerturbations
+// draws them (:340-360); the generator is seeded with "seed" when given
+// (the reference seeds it from std::random_device, which is what happens
+// here without the key), so a run with seed s reproduces the reference run
+// whose random_device returned s.  The update runs in the k-dimensional
+// form (mg_enkf): the gain's max/min and the condition number of S, which
+// need the n x p gain or the p x p S, are reported as NaN.
+template <typename BackendTag>
+class EnKF {
+ public:
+  struct AnalysisResults {  // EnKF.hpp:84-96
+    double innovation_norm;
+    double analysis_increment_norm;
+    double background_spread;
+    double analysis_spread;
+    double max_kalman_gain;
+    double min_kalman_gain;
+    double condition_number;
+    int ensemble_size;
+    int observation_count;
+    std::string inflation_method;
+    double inflation_factor;
+  };
+
+  template <typename Ens, typename Obs, typename H, typename Cfg>
+  EnKF(Ens& ensemble, Obs& obs, const H& obs_op, const Cfg& config, int device = 0)
+      : ctx_(std::make_shared<Context>(device)) {
+    const auto a = config.GetSubsection("analysis");
+    settings_.inflation = static_cast<double>(a.Get("inflation").asFloat());
+    settings_.output_base_file = a.Get("output_base_file").asString();
+    settings_.format = a.Get("format").asString();
+    method_ = a.Get("inflation_method").asString();
+    if (method_ != "multiplicative" && method_ != "additive" && method_ != "relaxation") method_ = "multiplicative";
+    const std::string prec = detail::cfg_string(a, "precision", "fp64");
+    if (prec != "fp64" && prec != "mixed") throw std::invalid_argument("precision must be fp64 or mixed");
+    settings_.precision = prec == "fp64" ? MG_PREC_FP64 : MG_PREC_MIXED;
+    settings_.host_h = detail::cfg_string(a, "obs_operator_on_device", "auto") == "host";
+    has_seed_ = a.HasKey("seed");
+    if (has_seed_) seed_ = static_cast<unsigned int>(a.Get("seed").asInt());
+    analyse_ = [this, &ensemble, &obs, &obs_op]() { run(ensemble, obs, obs_op); };
+    save_ = [this, &ensemble]() { save(ensemble); };
+  }
+
+  void Analyse() { analyse_(); }
+  void saveEnsemble() const { save_(); }
+  AnalysisResults getAnalysisResults() const { return results_; }
+
+ private:
+  template <typename Ens, typename Obs, typename H>
+  void run(Ens& ens, Obs& obs, const H& op) {
+    const int k = static_cast<int>(ens.Size());
+    const size_t n = ens.GetMember(0).size();
+    std::vector<double> host;
+    detail::gather_members(ens, host, k, n);
+    const detail::HostObs ho = detail::collect_obs(obs);
+    detail::HostGrid grid;
+    const bool have_grid = ho.grid && ens.GetMember(0).geometry() != nullptr;
+    if (have_grid) grid = detail::collect_grid(*ens.GetMember(0).geometry());
+    const size_t p = ho.size();
+    std::vector<double> eps(p * (size_t)k);
+    {
+      unsigned int s = seed_;
+      if (!has_seed_) {
+        std::random_device rd;
+        s = rd();
+      }
+      std::mt19937 gen(s);
+      std::normal_distribution<double> dist(0.0, 1.0);
+      for (size_t o = 0; o < p; ++o) {
+        const double sd = std::isfinite(ho.rvar[o]) ? std::sqrt(ho.rvar[o]) : 0.0;
+        for (int j = 0; j < k; ++j) eps[o * k + j] = sd * dist(gen);
+      }
+    }
+    DeviceBuffer<double> X, HX, yo, rvar, E;
+    X.upload(host, ctx_->stream());
+    detail::obs_space(*ctx_, ens, obs, op, ho, have_grid ? &grid : nullptr, X, k, n, settings_.host_h, HX);
+    yo.upload(ho.yo, ctx_->stream());
+    rvar.upload(ho.rvar, ctx_->stream());
+    E.upload(eps, ctx_->stream());
+    mg_enkf_diag d{};
+    ctx_->check(mg_enkf(ctx_->get(), X.data(), (int64_t)n, k, (int64_t)n, HX.data(), yo.data(), rvar.data(),
+                        E.data(), (int64_t)p, settings_.inflation, settings_.precision, nullptr, &d),
+                "mg_enkf");
+    std::vector<double> before = host;
+    X.download(host.data(), host.size(), ctx_->stream());
+    detail::scatter_members(ens, host, k, n);
+    ens.RecomputeMean();  // EnKF.hpp:237-238
+    ens.RecomputePerturbations();
+    double inc = 0.0;
+    for (size_t i = 0; i < host.size(); ++i) inc += (host[i] - before[i]) * (host[i] - before[i]);
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    results_ = AnalysisResults{d.innovation_norm, std::sqrt(inc), d.background_spread, d.analysis_spread, nan, nan,
+                               nan, k, (int)p, method_, settings_.inflation};
+  }
+
+  template <typename Ens>
+  void save(Ens& ens) const {  // EnKF.hpp:260-278
+    ens.Mean().saveToFile(settings_.output_base_file + "_mean." + settings_.format);
+    for (size_t i = 0; i < ens.Size(); ++i)
+      ens.GetMember(i).saveToFile(settings_.output_base_file + "_member_" + std::to_string(i) + "." +
+                                  settings_.format);
+  }
+
+  detail::Settings settings_;
+  std::string method_;
+  bool has_seed_ = false;
+  unsigned int seed_ = 0;
+  std::shared_ptr<Context> ctx_;
+  AnalysisResults results_{};
+  std::function<void()> analyse_;
+  std::function<void()> save_;
+};
+
+// Ensemble diagnostics on the GPU with the reference's interface
+// (Metrics.hpp:22-295): MetricValues and Metrics<T>::CalculateAll over
+// member vectors.
+template <typename T = double>
+struct MetricValues {
+  std::vector<T> mean;
+  std::vector<T> spread;
+  T rmse;
+  T bias;
+  T correlation;
+  T crps;
+  T avg_spread;
+
+  std::string ToString(int precision = 6) const {  // Metrics.hpp:35-45
+    std::stringstream ss;
+    ss << std::fixed << std::setprecision(precision);
+    ss << "Metrics:\n";
+    ss << "  RMSE: " << rmse << "\n";
+    ss << "  Bias: " << bias << "\n";
+    ss << "  Correlation: " << correlation << "\n";
+    ss << "  CRPS: " << crps << "\n";
+    ss << "  Average Spread: " << avg_spread << "\n";
+    return ss.str();
+  }
+  friend std::ostream& operator<<(std::ostream& os, const MetricValues<T>& m) { return os << m.ToString(); }
+};
+
+template <typename T = double>
+class Metrics {
+ public:
+  static MetricValues<T> CalculateAll(const std::vector<std::vector<T>>& ensemble_data, const std::vector<T>& truth,
+                                      size_t state_dim, size_t ens_size, int device = 0) {
+    static_assert(sizeof(T) == sizeof(double), "the GPU diagnostics run in double precision");
+    Context ctx(device);
+    std::vector<double> host(ens_size * state_dim);
+    for (size_t j = 0; j < ens_size; ++j)
+      for (size_t i = 0; i < state_dim; ++i) host[j * state_dim + i] = static_cast<double>(ensemble_data[j][i]);
+    std::vector<double> tr(truth.begin(), truth.begin() + state_dim);
+    DeviceBuffer<double> X, t, mean, spread;
+    X.upload(host, ctx.stream());
+    t.upload(tr, ctx.stream());
+    mean.resize(state_dim);
+    spread.resize(state_dim);
+    mg_ens_metrics_t out{};
+    ctx.check(mg_ens_metrics(ctx.get(), X.data(), (int64_t)state_dim, (int32_t)ens_size, (int64_t)state_dim,
+                             t.data(), mean.data(), spread.data(), &out),
+              "mg_ens_metrics");
+    MetricValues<T> v;
+    v.mean.resize(state_dim);
+    v.spread.resize(state_dim);
+    std::vector<double> hm(state_dim), hs(state_dim);
+    mean.download(hm.data(), state_dim, ctx.stream());
+    spread.download(hs.data(), state_dim, ctx.stream());
+    for (size_t i = 0; i < state_dim; ++i) {
+      v.mean[i] = static_cast<T>(hm[i]);
+      v.spread[i] = static_cast<T>(hs[i]);
+    }
+    v.rmse = out.rmse;
+    v.bias = out.bias;
+    v.correlation = out.correlation;
+    v.crps = out.crps;
+    v.avg_spread = out.avg_spread;
+    return v;
+  }
 };
 
 }  // namespace metada_gb300

@@ -8,7 +8,7 @@
 //   CASE_DIR/meta.txt: "nx ny k p sigma rho radius"; X.bin (k x nx*ny f64),
 //   obs_xy.bin (p x 2 int32), yo.bin (p f64).
 //   MODE: letkf_sequential | letkf_batched_reference | letkf_batched_hunt_mixed |
-//         etkf_reference | etkf_reference_host_h
+//         etkf_reference | etkf_reference_host_h | enkf_seed1234
 //   writes OUT_DIR/members.bin (k x n f64) and OUT_DIR/mean.bin.
 #include <cmath>
 #include <cstdint>
@@ -70,6 +70,7 @@ struct Ensemble {
     for (auto& v : mean.data) v *= 1.0 / static_cast<double>(members.size());
   }
   State& Mean() { return mean; }
+  void RecomputePerturbations() {}  // the policies do not read them back
 };
 
 struct ObsPoint {
@@ -126,10 +127,11 @@ struct ObsOperator {  // IdentityObsOperator::apply for grid obs on SimpleState
 struct Value {
   std::string s;
   float asFloat() const { return std::stof(s); }
+  int asInt() const { return std::stoi(s); }
   std::string asString() const { return s; }
 };
 
-struct Config {
+struct Config {  // one flat map; GetSubsection("analysis") is the map itself
   std::map<std::string, std::string> kv;
   Value Get(const std::string& k) const {
     auto it = kv.find(k);
@@ -137,6 +139,7 @@ struct Config {
     return {it->second};
   }
   bool HasKey(const std::string& k) const { return kv.count(k) > 0; }
+  const Config& GetSubsection(const std::string&) const { return *this; }
 };
 
 }  // namespace mock
@@ -198,6 +201,15 @@ int main(int argc, char** argv) {
       cfg.kv["obs_operator_on_device"] = "host";
       metada_gb300::ETKF<MockTag> a(ens, obs, H, cfg);
       a.Analyse();
+    } else if (mode == "enkf_seed1234") {
+      cfg.kv["inflation_method"] = "multiplicative";
+      cfg.kv["seed"] = "1234";
+      metada_gb300::EnKF<MockTag> a(ens, obs, H, cfg);
+      a.Analyse();
+      const auto r = a.getAnalysisResults();
+      std::ofstream fd(out + "/diag.bin", std::ios::binary);
+      const double d[3] = {r.innovation_norm, r.background_spread, r.analysis_spread};
+      fd.write(reinterpret_cast<const char*>(d), sizeof(d));
     } else {
       throw std::runtime_error("unknown mode " + mode);
     }

@@ -1,4 +1,4 @@
-// Compile check: metada_gb300::LETKF / ETKF instantiated with the REFERENCE's
+// Compile check: metada_gb300::LETKF / ETKF / EnKF / Metrics instantiated with the REFERENCE's
 // own adapter types (framework::Ensemble/Observation/ObsOperator/Config over
 // the Simple backend, GridObservation and IdentityObsOperator), exactly as
 // applications/data_assimilation/ensemble/letkf.cpp:46-65 builds them.  Built
@@ -36,7 +36,20 @@ int run(const fw::ConfigMap& root, const fw::ConfigMap& logger_cfg) {
   metada_gb300::ETKF<Tag> etkf(ensemble, observations, obs_operator, config.GetSubsection("analysis"));
   etkf.Analyse();
   etkf.saveEnsemble();
-  return 0;
+  // fw::EnKF<Tag> takes the root configuration (EnKF.hpp:100-109).
+  metada_gb300::EnKF<Tag> enkf(ensemble, observations, obs_operator, config);
+  enkf.Analyse();
+  enkf.saveEnsemble();
+  const auto results = enkf.getAnalysisResults();
+  // Metrics<double>::CalculateAll over member vectors (Metrics.hpp:74-94).
+  std::vector<std::vector<double>> data;
+  for (size_t i = 0; i < ensemble.Size(); ++i) {
+    const auto& m = ensemble.GetMember(i);
+    const double* d = m.template getDataPtr<double>();
+    data.emplace_back(d, d + m.size());
+  }
+  const auto mv = metada_gb300::Metrics<>::CalculateAll(data, data[0], data[0].size(), data.size());
+  return (results.ensemble_size > 0 && mv.rmse >= 0.0) ? 0 : 1;
 }
 
 int main(int argc, char**) { return argc > 100 ? run({}, {}) : 0; }
