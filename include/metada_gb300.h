@@ -299,6 +299,47 @@ int mg_hx_column_mlp(mg_context* ctx, mg_mlp* mlp, const double* X, int32_t k, i
 int mg_gemm_bf16_tc(mg_context* ctx, const void* A, const void* B, int32_t M, int32_t N, int32_t K,
                     const float* bias, int32_t silu, float* C);
 
+/* Text I/O of the analysis path on the device (text and output buffers
+ * on the host; parsed arrays on the device).
+ *
+ * mg_parse_grid_obs replaces GridObservation::loadFromFile
+ * (src/backends/common/observation/GridObservation.hpp:395-474) for the
+ * "Time Z Y X ZNU XLONG_U XLAT_U Value" format: data lines after the first
+ * separator line following a header line, read as int x4, double x4 with
+ * std::istream rules, kept unless Value == missing_value, in file order.
+ * xyz (count x 3: x, y, z) and vals (count x 4: znu, xlong_u, xlat_u,
+ * value); *count receives the number kept (MG_ERR_CAPACITY if > cap).
+ *
+ * mg_parse_values replaces SimpleState::readFromFile (SimpleState.hpp:248-263):
+ * every double of every line, up to the first failed extraction of a line.
+ *
+ * mg_format_state replaces SimpleState::saveToFile (SimpleState.hpp:160-188):
+ * ny rows of nx "%12.6f" values joined by one space; *nbytes receives the
+ * text length (MG_ERR_CAPACITY, without writing, if out is NULL or cap is
+ * smaller).
+ *
+ * Numbers are converted exactly as strtod/printf do (device fast paths,
+ * host for the rest).  No counterpart for the device placement in the
+ * reference. */
+int mg_parse_grid_obs(mg_context* ctx, const char* text, int64_t nbytes, double missing_value, int32_t* xyz,
+                      double* vals, int64_t cap, int64_t* count);
+int mg_parse_values(mg_context* ctx, const char* text, int64_t nbytes, double* out, int64_t cap, int64_t* count);
+int mg_format_state(mg_context* ctx, const double* values, int32_t nx, int32_t ny, char* out, int64_t cap,
+                    int64_t* nbytes);
+
+/* Nearest grid node of geographic observations on a curvilinear nx x ny
+ * grid (node n = j*nx + i at node_lat[n], node_lon[n], degrees), replacing
+ * the per-observation scan of IdentityObsOperator::convertGeographicToGrid
+ * (src/backends/common/obsoperator/IdentityObsOperator.hpp:470-505): the
+ * first node in index order minimising sqrt((lon - lon_n)^2 + (lat - lat_n)^2),
+ * found through a device spatial hash, bit-identical to the scan.  out_xy
+ * (p x 2 int32, device) receives (i, j), the format mg_hx_idw4 reads;
+ * with out_k (p, may be NULL) also the first z minimising
+ * |obs_level - vcoord[z]| (:491-500).  All arrays on the device. */
+int mg_nearest_node(mg_context* ctx, const double* node_lat, const double* node_lon, int32_t nx, int32_t ny,
+                    const double* obs_lat, const double* obs_lon, int64_t p, const double* vcoord, int32_t nz,
+                    const double* obs_level, int32_t* out_xy, int32_t* out_k);
+
 /* Stochastic EnKF with perturbed observations, replacing EnKF::Analyse
  * (src/framework/algorithms/EnKF.hpp:139-254), in place on the members.
  * HX (p x k row-major) is H of the raw members; obs_pert (p x k row-major)

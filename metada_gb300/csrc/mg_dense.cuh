@@ -423,6 +423,18 @@ __device__ int cta_jacobi_tri(float* A, int lda, float* Vt, int ldv, int kp, flo
     }
     ++sweep;
     if (!__syncthreads_or(rotated)) break;
+    // A sweep that rotated may still have left every pair under the
+    // threshold: test all pairs at once (one barrier) instead of running a
+    // further sweep whose rounds would only confirm it.
+    int open = 0;
+    for (int i = tid >> 5; i < kp - 1; i += NT / 32) {
+      const float aii = A[i * lda + i];
+      for (int j = i + 1 + (tid & 31); j < kp; j += 32) {
+        const float aij = A[i * lda + j];
+        open |= (aij != 0.0f && aij * aij > tol * tol * fabsf(aii * A[j * lda + j]));
+      }
+    }
+    if (!__syncthreads_or(open)) break;
   }
   return sweep;
 }

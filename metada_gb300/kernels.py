@@ -62,6 +62,65 @@ def ens_mean_pert(X: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
     return mean, Xp
 
 
+def parse_grid_obs(text: bytes, missing_value: float = -999.0,
+                   device: int = 0) -> tuple[torch.Tensor, torch.Tensor]:
+    """GridObservation text -> (xyz int32 p x 3: x, y, z; vals float64 p x 4:
+    znu, xlong_u, xlat_u, value) on the device."""
+    ctx = context(device)
+    count = c_int64(0)
+    rc = ctx.lib.mg_parse_grid_obs(ctx.handle, text, len(text), float(missing_value), c_void_p(0), c_void_p(0), 0,
+                                   byref(count))
+    if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
+        ctx.check(rc)
+    dev = torch.device("cuda", device)
+    xyz = torch.empty((max(count.value, 1), 3), dtype=torch.int32, device=dev)
+    vals = torch.empty((max(count.value, 1), 4), dtype=torch.float64, device=dev)
+    ctx.call("mg_parse_grid_obs", text, len(text), float(missing_value), _ptr(xyz), _ptr(vals), count.value,
+             byref(count))
+    return xyz[: count.value], vals[: count.value]
+
+
+def parse_values(text: bytes, device: int = 0) -> torch.Tensor:
+    """SimpleState text -> its values (float64) on the device."""
+    ctx = context(device)
+    count = c_int64(0)
+    rc = ctx.lib.mg_parse_values(ctx.handle, text, len(text), c_void_p(0), 0, byref(count))
+    if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
+        ctx.check(rc)
+    out = torch.empty(max(count.value, 1), dtype=torch.float64, device=torch.device("cuda", device))
+    ctx.call("mg_parse_values", text, len(text), _ptr(out), count.value, byref(count))
+    return out[: count.value]
+
+
+def format_state(values: torch.Tensor, nx: int, ny: int) -> bytes:
+    """SimpleState::saveToFile text of ny rows of nx values ("%12.6f")."""
+    _need(values, torch.float64, "values")
+    ctx = context(values.device.index)
+    nbytes = c_int64(0)
+    rc = ctx.lib.mg_format_state(ctx.handle, _ptr(values), nx, ny, c_void_p(0), 0, byref(nbytes))
+    if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
+        ctx.check(rc)
+    buf = ctypes.create_string_buffer(max(nbytes.value, 1))
+    ctx.call("mg_format_state", _ptr(values), nx, ny, buf, nbytes.value, byref(nbytes))
+    return buf.raw[: nbytes.value]
+
+
+def nearest_node(node_lat: torch.Tensor, node_lon: torch.Tensor, nx: int, ny: int, obs_lat: torch.Tensor,
+                 obs_lon: torch.Tensor, vcoord: torch.Tensor | None = None,
+                 obs_level: torch.Tensor | None = None) -> tuple[torch.Tensor, torch.Tensor | None]:
+    """Nearest node (i, j) of each geographic observation on a curvilinear
+    grid (and the nearest vertical index when vcoord/obs_level are given)."""
+    for t, nm in ((node_lat, "node_lat"), (node_lon, "node_lon"), (obs_lat, "obs_lat"), (obs_lon, "obs_lon")):
+        _need(t, torch.float64, nm)
+    p = obs_lat.shape[0]
+    xy = torch.empty((p, 2), dtype=torch.int32, device=obs_lat.device)
+    kk = torch.empty(p, dtype=torch.int32, device=obs_lat.device) if vcoord is not None else None
+    context(obs_lat.device.index).call("mg_nearest_node", _ptr(node_lat), _ptr(node_lon), nx, ny, _ptr(obs_lat),
+                                       _ptr(obs_lon), p, _ptr(vcoord), vcoord.shape[0] if vcoord is not None else 0,
+                                       _ptr(obs_level), _ptr(xy), _ptr(kk))
+    return xy, kk
+
+
 def enkf(X: torch.Tensor, HX: torch.Tensor, yo: torch.Tensor, rvar: torch.Tensor, obs_pert: torch.Tensor,
          inflation: float, precision: int = _lib.MG_PREC_FP64) -> tuple[torch.Tensor, dict]:
     """Stochastic EnKF in place on X (k x n); returns (analysis mean, diagnostics)."""

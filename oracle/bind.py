@@ -55,6 +55,7 @@ def load() -> ctypes.CDLL:
             "orc_sym_eig": ([vp, c_int32, vp, vp], ctypes.c_int),
             "orc_column_op": ([vp, vp, c_int64, c_int32, vp, vp, c_int32, vp], None),
             "orc_ens_metrics": ([vp, c_int64, c_int32, c_int64, vp, vp, vp, vp], None),
+            "orc_nearest_node": ([vp, vp, c_int32, c_int32, vp, vp, c_int64, vp, c_int32, vp, vp, vp], None),
             "orc_enkf": ([vp, c_int64, c_int32, c_int64, vp, vp, vp, vp, c_int64, c_double, vp, vp, vp], ctypes.c_int),
             "orc_num_threads": ([], ctypes.c_int),
         }
@@ -225,6 +226,18 @@ def ens_metrics(X, truth):
     out = np.empty(5)
     load().orc_ens_metrics(_p(X), n, k, n, _p(truth), _p(mean), _p(spread), _p(out))
     return mean, spread, dict(zip(("rmse", "bias", "correlation", "crps", "avg_spread"), out.tolist()))
+
+
+def nearest_node(node_lat, node_lon, nx, ny, obs_lat, obs_lon, vcoord=None, obs_level=None):
+    node_lat, node_lon, obs_lat, obs_lon = map(_f64, (node_lat, node_lon, obs_lat, obs_lon))
+    p = obs_lat.shape[0]
+    xy = np.empty((p, 2), dtype=np.int32)
+    kk = np.empty(p, dtype=np.int32) if vcoord is not None else None
+    vc = _f64(vcoord) if vcoord is not None else None
+    lev = _f64(obs_level) if obs_level is not None else None
+    load().orc_nearest_node(_p(node_lat), _p(node_lon), nx, ny, _p(obs_lat), _p(obs_lon), p, _p(vc),
+                            0 if vc is None else vc.shape[0], _p(lev), _p(xy), _p(kk))
+    return xy, kk
 
 
 def enkf(X, HX, yo, rvar, eps, rho):

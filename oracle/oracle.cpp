@@ -678,6 +678,43 @@ int orc_enkf(double* X, int64_t n, int32_t k, int64_t ld, const double* HX, cons
   return 0;
 }
 
+// IdentityObsOperator::convertGeographicToGrid with 2-D coordinates
+// (IdentityObsOperator.hpp:470-505): scan every node in index order, keep
+// the first strict minimum of the Euclidean degree distance; vertical index
+// likewise over vcoord.
+void orc_nearest_node(const double* node_lat, const double* node_lon, int32_t nx, int32_t ny,
+                      const double* obs_lat, const double* obs_lon, int64_t p, const double* vcoord, int32_t nz,
+                      const double* obs_level, int32_t* out_xy, int32_t* out_k) {
+  const int64_t nn = (int64_t)nx * ny;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t o = 0; o < p; ++o) {
+    double min_dist = std::numeric_limits<double>::max();
+    int64_t min_idx = 0;
+    for (int64_t idx = 0; idx < nn; ++idx) {
+      const double dist = std::sqrt((obs_lon[o] - node_lon[idx]) * (obs_lon[o] - node_lon[idx]) +
+                                    (obs_lat[o] - node_lat[idx]) * (obs_lat[o] - node_lat[idx]));
+      if (dist < min_dist) {
+        min_dist = dist;
+        min_idx = idx;
+      }
+    }
+    out_xy[2 * o] = (int32_t)(min_idx % nx);
+    out_xy[2 * o + 1] = (int32_t)(min_idx / nx);
+    if (out_k) {
+      double md = std::numeric_limits<double>::max();
+      int kb = 0;
+      for (int z = 0; z < nz; ++z) {
+        const double d = std::abs(obs_level[o] - vcoord[z]);
+        if (d < md) {
+          md = d;
+          kb = z;
+        }
+      }
+      out_k[o] = kb;
+    }
+  }
+}
+
 int orc_sym_eig(double* A, int32_t k, double* w, double* V) { return jacobi_eig(A, k, w, V); }
 
 // Metrics<double>::CalculateAll (Metrics.hpp:74-94) and the functions it

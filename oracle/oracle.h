@@ -140,6 +140,12 @@ int orc_enkf(double* X, int64_t n, int32_t k, int64_t ld, const double* HX, cons
              const double* rvar, const double* eps, int64_t p, double rho, double* mean_out, double* diag3,
              double* gain2);
 
+/* Nearest node of geographic obs on a curvilinear grid by the reference's
+ * scan (IdentityObsOperator.hpp:470-505); out_k may be NULL. */
+void orc_nearest_node(const double* node_lat, const double* node_lon, int32_t nx, int32_t ny,
+                      const double* obs_lat, const double* obs_lon, int64_t p, const double* vcoord, int32_t nz,
+                      const double* obs_level, int32_t* out_xy, int32_t* out_k);
+
 /* Symmetric eigen-decomposition by cyclic Jacobi (FP64), A = V diag(w) V^T.
  * A (k x k, row-major) is overwritten.  Returns the number of sweeps. */
 int orc_sym_eig(double* A, int32_t k, double* w, double* V);

@@ -1,0 +1,52 @@
+"""GPU: nearest-node search of geographic obs on a curvilinear grid (spatial
+hash) against the reference's scan restated in the oracle: bit-identical
+node choice, including ties, obs outside the grid and the vertical index."""
+import numpy as np
+import pytest
+import torch
+
+import oracle.bind as ob
+from metada_gb300 import kernels as K
+
+pytestmark = pytest.mark.gpu
+
+
+def _grid(nx, ny, seed):
+    g = np.random.default_rng(seed)
+    lon, lat = np.meshgrid(np.linspace(70.0, 140.0, nx), np.linspace(5.0, 55.0, ny))
+    lon = lon + 0.8 * np.sin(np.deg2rad(lat) * 3.0) + 0.05 * g.standard_normal(lon.shape)
+    lat = lat + 0.4 * np.cos(np.deg2rad(lon) * 2.0)
+    return np.ascontiguousarray(lat.ravel()), np.ascontiguousarray(lon.ravel())
+
+
+@pytest.mark.parametrize("nx,ny,p", [(40, 30, 2000), (300, 200, 20000)])
+def test_nearest_node_matches_scan(dev, nx, ny, p):
+    lat, lon = _grid(nx, ny, nx)
+    g = np.random.default_rng(p)
+    oa = g.uniform(0.0, 60.0, p)    # some obs outside the grid
+    ol = g.uniform(60.0, 150.0, p)
+    # exact ties: obs at the midpoint of two nodes, and on nodes
+    oa[:50], ol[:50] = 0.5 * (lat[:50] + lat[1:51]), 0.5 * (lon[:50] + lon[1:51])
+    oa[50:100], ol[50:100] = lat[200:250], lon[200:250]
+    vc = np.array([1000.0, 925.0, 850.0, 700.0, 500.0, 300.0, 100.0])
+    lev = g.uniform(50.0, 1050.0, p)
+    lev[:20] = 0.5 * (1000.0 + 925.0)  # ties between two levels: the first wins
+    want_xy, want_k = ob.nearest_node(lat, lon, nx, ny, oa, ol, vc, lev)
+    T = lambda a: torch.tensor(a, device=dev)  # noqa: E731
+    xy, kk = K.nearest_node(T(lat), T(lon), nx, ny, T(oa), T(ol), T(vc), T(lev))
+    assert np.array_equal(xy.cpu().numpy(), want_xy)
+    assert np.array_equal(kk.cpu().numpy(), want_k)
+
+
+def test_nearest_node_feeds_idw4(dev):
+    """(i, j) from the search is the grid-obs input of the IDW4 operator."""
+    nx, ny = 50, 40
+    lat, lon = _grid(nx, ny, 3)
+    g = np.random.default_rng(9)
+    X = g.standard_normal((6, nx * ny))
+    oa, ol = g.uniform(10, 50, 300), g.uniform(75, 135, 300)
+    T = lambda a: torch.tensor(a, device=dev)  # noqa: E731
+    xy, _ = K.nearest_node(T(lat), T(lon), nx, ny, T(oa), T(ol))
+    HX = K.hx_idw4(T(X), nx, ny, xy).cpu().numpy()
+    wxy, _ = ob.nearest_node(lat, lon, nx, ny, oa, ol)
+    assert np.array_equal(HX, ob.hx_idw4(X, nx, ny, wxy))

@@ -223,3 +223,17 @@ def test_enkf_matches_reference(built, which):
     want = g[f"{which}_diag"]
     got = [diag["innovation_norm"], diag["background_spread"], diag["analysis_spread"], gain[0], gain[1]]
     np.testing.assert_allclose(got, want, rtol=1e-10)
+
+
+def test_nearest_node_scan_matches_numpy(built):
+    """The restated scan of IdentityObsOperator::convertGeographicToGrid
+    (first strict minimum in node order) against numpy's argmin."""
+    g = np.random.default_rng(4)
+    nx, ny = 30, 20
+    lon, lat = np.meshgrid(np.linspace(100.0, 130.0, nx), np.linspace(10.0, 30.0, ny))
+    lon = lon + 0.3 * np.sin(lat / 5.0)
+    ol, oa = g.uniform(95, 135, 500), g.uniform(5, 35, 500)
+    xy, _ = ob.nearest_node(lat.ravel(), lon.ravel(), nx, ny, oa, ol)
+    d = np.sqrt((ol[:, None] - lon.ravel()[None]) ** 2 + (oa[:, None] - lat.ravel()[None]) ** 2)
+    idx = np.argmin(d, axis=1)  # first minimum, as the scan
+    assert np.array_equal(xy[:, 0], idx % nx) and np.array_equal(xy[:, 1], idx // nx)
