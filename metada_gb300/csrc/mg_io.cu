@@ -1,0 +1,667 @@
+// Text I/O of the analysis path on the device: the GridObservation text
+// format (GridObservation::loadFromFile, src/backends/common/observation/
+// GridObservation.hpp:395-474), SimpleState files (SimpleState::readFromFile,
+// src/backends/simple/SimpleState.hpp:248-263) and the state writer
+// (SimpleState::saveToFile, :160-188).
+//
+// The text is copied to the device once; lines are indexed in parallel
+// (per-4 KB chunk counts, a scan, then the line starts), and every line is
+// scanned by one thread with the extraction rules of std::istream:
+//   * int: skip white space, optional sign, at least one digit;
+//   * double: skip white space, [sign] (digits [. digits] | . digits)
+//     [(e|E) [sign] digits]; no inf/nan/hex (libstdc++ rejects them);
+//   * the next extraction starts right after the previous one.
+// Decimal to binary: a mantissa of at most 19 digits that is below 2^53 with
+// a decimal exponent in [-22, 22] is converted by one correctly rounded
+// multiplication or division by an exact power of ten (Clinger's fast path),
+// which equals strtod; every other number sends its line to the host, where
+// std::istringstream (the reference's own extraction) reads it.
+// The writer prints "%12.6f" values (std::fixed, setprecision(6),
+// setw(12)) joined by one space, one row of x values per line: |v| < 2^53
+// is rounded exactly to 6 decimals (round half to even on the binary value,
+// as printf) with 128-bit integer arithmetic; other values (and NaN/inf) are
+// printed on the host.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "mg_internal.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int64_t kChunk = 4096;
+
+__device__ __forceinline__ bool is_ws(char c) {
+  return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r';
+}
+__device__ __forceinline__ bool is_digit(char c) { return c >= '0' && c <= '9'; }
+
+// ---- line index ----
+__global__ void line_count_kernel(const char* __restrict__ t, int64_t n, int64_t* __restrict__ counts) {
+  const int64_t c0 = (int64_t)blockIdx.x * kChunk;
+  const int64_t c1 = c0 + kChunk < n ? c0 + kChunk : n;
+  __shared__ int red[kThreads / 32];
+  int cnt = 0;
+  for (int64_t i = c0 + threadIdx.x; i < c1; i += kThreads) cnt += (i == 0 || t[i - 1] == '\n') ? 1 : 0;
+  for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < kThreads / 32; ++w) s += red[w];
+    counts[blockIdx.x] = s;
+  }
+}
+
+// Line starts in text order: a chunk's threads take consecutive 16-byte
+// pieces; a block-wide exclusive scan of the per-thread counts gives each
+// thread's first slot.
+__global__ void line_fill_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ offsets,
+                                 int64_t* __restrict__ starts) {
+  constexpr int kPiece = (int)(kChunk / kThreads);  // 16 bytes per thread
+  const int64_t c0 = (int64_t)blockIdx.x * kChunk;
+  const int64_t p0 = c0 + (int64_t)threadIdx.x * kPiece;
+  int cnt = 0;
+  for (int j = 0; j < kPiece; ++j) {
+    const int64_t i = p0 + j;
+    if (i < n && (i == 0 || t[i - 1] == '\n')) ++cnt;
+  }
+  __shared__ int scan[kThreads];
+  scan[threadIdx.x] = cnt;
+  __syncthreads();
+  for (int off = 1; off < kThreads; off <<= 1) {  // inclusive Hillis-Steele scan
+    const int v = threadIdx.x >= off ? scan[threadIdx.x - off] : 0;
+    __syncthreads();
+    scan[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int64_t slot = offsets[blockIdx.x] + scan[threadIdx.x] - cnt;
+  for (int j = 0; j < kPiece; ++j) {
+    const int64_t i = p0 + j;
+    if (i < n && (i == 0 || t[i - 1] == '\n')) starts[slot++] = i;
+  }
+}
+
+// ---- std::istream-style extraction ----
+__device__ bool extract_int(const char* t, int64_t& pos, int64_t end, int& out) {
+  while (pos < end && is_ws(t[pos])) ++pos;
+  bool neg = false;
+  if (pos < end && (t[pos] == '+' || t[pos] == '-')) neg = t[pos++] == '-';
+  if (pos >= end || !is_digit(t[pos])) return false;
+  long long v = 0;
+  while (pos < end && is_digit(t[pos])) {
+    v = v * 10 + (t[pos++] - '0');
+    if (v > 2147483648ll) return false;  // overflow: failbit
+  }
+  if (!neg && v > 2147483647ll) return false;
+  out = (int)(neg ? -v : v);
+  return true;
+}
+
+__device__ __forceinline__ double pow10_exact(int e) {  // 10^e, 0 <= e <= 22, exact in binary64
+  const double p[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                        1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+  return p[e];
+}
+
+// Returns 1 on success, 0 on a failed extraction, 2 if the number is valid
+// but outside the exact fast path (the host converts it).
+__device__ int extract_double(const char* t, int64_t& pos, int64_t end, double& out) {
+  while (pos < end && is_ws(t[pos])) ++pos;
+  bool neg = false;
+  if (pos < end && (t[pos] == '+' || t[pos] == '-')) neg = t[pos++] == '-';
+  unsigned long long m = 0;
+  int sig = 0, drop = 0, frac = 0, ndig = 0;
+  while (pos < end && is_digit(t[pos])) {
+    const int d = t[pos++] - '0';
+    ++ndig;
+    if (sig == 0 && d == 0) continue;
+    if (sig < 19) {
+      m = m * 10 + d;
+      ++sig;
+    } else {
+      ++drop;  // digit beyond 19 significant ones
+    }
+  }
+  if (pos < end && t[pos] == '.') {
+    ++pos;
+    while (pos < end && is_digit(t[pos])) {
+      const int d = t[pos++] - '0';
+      ++ndig;
+      if (sig == 0 && d == 0) {
+        ++frac;
+        continue;
+      }
+      if (sig < 19) {
+        m = m * 10 + d;
+        ++sig;
+        ++frac;
+      } else {
+        ++drop;  // a digit beyond 19 significant ones: not exact, the host converts
+      }
+    }
+  }
+  if (ndig == 0) return 0;
+  int ex = 0;
+  if (pos < end && (t[pos] == 'e' || t[pos] == 'E')) {
+    int64_t q = pos + 1;
+    bool eneg = false;
+    if (q < end && (t[q] == '+' || t[q] == '-')) eneg = t[q++] == '-';
+    if (q >= end || !is_digit(t[q])) return 0;  // "1e" with no exponent digits fails
+    int v = 0;
+    while (q < end && is_digit(t[q])) {
+      if (v < 100000) v = v * 10 + (t[q] - '0');
+      ++q;
+    }
+    ex = eneg ? -v : v;
+    pos = q;
+  }
+  if (m == 0) {
+    out = neg ? -0.0 : 0.0;
+    return 1;
+  }
+  if (drop > 0) return 2;
+  const int e10 = ex - frac;
+  if (m >= (1ull << 53) || e10 < -22 || e10 > 22) return 2;
+  const double md = (double)m;  // exact
+  const double v = e10 >= 0 ? __dmul_rn(md, pow10_exact(e10)) : __ddiv_rn(md, pow10_exact(-e10));
+  out = neg ? -v : v;
+  return 1;
+}
+
+// ---- GridObservation text ----
+enum LineType : int32_t { kEmpty = 0, kHeader = 1, kSep = 2, kData = 3, kBad = 4, kHost = 5 };
+
+__device__ bool line_contains(const char* t, int64_t s, int64_t e, const char* pat, int np) {
+  for (int64_t i = s; i + np <= e; ++i) {
+    int j = 0;
+    while (j < np && t[i + j] == pat[j]) ++j;
+    if (j == np) return true;
+  }
+  return false;
+}
+
+struct ObsLines {
+  int32_t* type;
+  int32_t* ival;   // L x 4: time, z, y, x
+  double* dval;    // L x 4: znu, xlong_u, xlat_u, value
+};
+
+__global__ void obs_lines_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
+                                 int64_t L, ObsLines ol, unsigned long long* __restrict__ first_header) {
+  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L) return;
+  const int64_t s = starts[l];
+  const int64_t e = (l + 1 < L) ? starts[l + 1] - 1 : ((n > 0 && t[n - 1] == '\n') ? n - 1 : n);
+  int32_t ty;
+  if (e <= s) {
+    ty = kEmpty;
+  } else if (line_contains(t, s, e, "Time", 4) && line_contains(t, s, e, "XLONG_U", 7)) {
+    ty = kHeader;
+    atomicMin(first_header, (unsigned long long)l);
+  } else {
+    bool only = true;
+    for (int64_t i = s; i < e; ++i) {
+      const char c = t[i];
+      if (c != '-' && c != ' ' && c != '\t') {
+        only = false;
+        break;
+      }
+    }
+    if (only && line_contains(t, s, e, "---", 3)) {
+      ty = kSep;
+    } else {
+      int64_t pos = s;
+      int iv[4];
+      double dv[4];
+      bool ok = true;
+      int host = 0;
+      for (int f = 0; f < 4 && ok; ++f) ok = extract_int(t, pos, e, iv[f]);
+      for (int f = 0; f < 4 && ok; ++f) {
+        const int r = extract_double(t, pos, e, dv[f]);
+        if (r == 0) ok = false;
+        if (r == 2) host = 1;
+      }
+      ty = !ok ? kBad : (host ? kHost : kData);
+      if (ty == kData) {
+        for (int f = 0; f < 4; ++f) {
+          ol.ival[l * 4 + f] = iv[f];
+          ol.dval[l * 4 + f] = dv[f];
+        }
+      }
+    }
+  }
+  ol.type[l] = ty;
+}
+
+__global__ void obs_sep_kernel(const int32_t* __restrict__ type, int64_t L,
+                               const unsigned long long* __restrict__ first_header,
+                               unsigned long long* __restrict__ first_sep) {
+  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l < L && type[l] == kSep && (unsigned long long)l > *first_header) atomicMin(first_sep, (unsigned long long)l);
+}
+
+__global__ void obs_keep_kernel(const ObsLines ol, int64_t L, const unsigned long long* __restrict__ first_sep,
+                                double missing, int64_t* __restrict__ keep) {
+  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L) return;
+  keep[l] = ((unsigned long long)l > *first_sep && ol.type[l] == kData && ol.dval[l * 4 + 3] != missing) ? 1 : 0;
+}
+
+__global__ void obs_write_kernel(const ObsLines ol, int64_t L, const int64_t* __restrict__ keep,
+                                 const int64_t* __restrict__ pos, int32_t* __restrict__ xyz,
+                                 double* __restrict__ vals) {
+  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L || !keep[l]) return;
+  const int64_t o = pos[l];
+  xyz[3 * o + 0] = ol.ival[l * 4 + 3];  // x
+  xyz[3 * o + 1] = ol.ival[l * 4 + 2];  // y
+  xyz[3 * o + 2] = ol.ival[l * 4 + 1];  // z
+  for (int f = 0; f < 4; ++f) vals[4 * o + f] = ol.dval[l * 4 + f];
+}
+
+// ---- SimpleState values: per line, doubles until the first failed extraction ----
+__global__ void values_count_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
+                                    int64_t L, int64_t* __restrict__ counts, int32_t* __restrict__ host) {
+  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L) return;
+  const int64_t s = starts[l];
+  const int64_t e = (l + 1 < L) ? starts[l + 1] - 1 : ((n > 0 && t[n - 1] == '\n') ? n - 1 : n);
+  int64_t pos = s, c = 0;
+  int h = 0;
+  double v;
+  for (;;) {
+    const int r = extract_double(t, pos, e, v);
+    if (r == 0) break;
+    if (r == 2) h = 1;
+    ++c;
+  }
+  counts[l] = c;
+  host[l] = h;
+}
+
+__global__ void values_write_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
+                                    int64_t L, const int64_t* __restrict__ offs, const int32_t* __restrict__ host,
+                                    double* __restrict__ out) {
+  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L || host[l]) return;
+  const int64_t s = starts[l];
+  const int64_t e = (l + 1 < L) ? starts[l + 1] - 1 : ((n > 0 && t[n - 1] == '\n') ? n - 1 : n);
+  int64_t pos = s, o = offs[l];
+  double v;
+  while (extract_double(t, pos, e, v) == 1) out[o++] = v;
+}
+
+// ---- "%12.6f" writer ----
+// Exact value of |v| * 10^6 rounded half-to-even, for finite |v| < 2^53.
+__device__ bool micro_units(double v, unsigned long long& q) {
+  const double a = fabs(v);
+  if (!(a < 9007199254740992.0)) return false;
+  if (a == 0.0) {
+    q = 0;
+    return true;
+  }
+  int e2;
+  const double fr = frexp(a, &e2);               // a = fr * 2^e2, fr in [0.5, 1)
+  const unsigned long long m = (unsigned long long)ldexp(fr, 53);  // exact 53-bit mantissa
+  const int e = e2 - 53;                          // a = m * 2^e
+  const unsigned __int128 P = (unsigned __int128)m * 15625u;  // m * 5^6
+  const int sh = e + 6;                           // a * 10^6 = P * 2^sh
+  if (sh >= 0) {  // sh <= 6 since |v| < 2^53; P << sh < 2^73, so check the high word
+    const unsigned __int128 w = P << sh;
+    q = (unsigned long long)w;
+    return (w >> 64) == 0;
+  }
+  const int s = -sh;
+  if (s >= 100) {
+    q = 0;
+    return true;
+  }
+  const unsigned __int128 qq = P >> s;
+  const unsigned __int128 rem = P - (qq << s);
+  const unsigned __int128 half = (unsigned __int128)1 << (s - 1);
+  unsigned __int128 r = qq;
+  if (rem > half || (rem == half && (qq & 1))) r += 1;
+  if (r >> 64) return false;
+  q = (unsigned long long)r;
+  return true;
+}
+
+// Characters of the formatted value (without padding) into buf; returns the
+// length, or -1 if the host must format it.
+__device__ int format_f6(double v, char* buf) {
+  unsigned long long q;
+  if (!micro_units(v, q)) return -1;
+  char tmp[40];
+  int n = 0;
+  unsigned long long ip = q / 1000000ull, fp = q % 1000000ull;
+  for (int d = 0; d < 6; ++d) {
+    tmp[n++] = (char)('0' + fp % 10);
+    fp /= 10;
+  }
+  tmp[n++] = '.';
+  do {
+    tmp[n++] = (char)('0' + ip % 10);
+    ip /= 10;
+  } while (ip);
+  if (signbit(v)) tmp[n++] = '-';
+  for (int i = 0; i < n; ++i) buf[i] = tmp[n - 1 - i];
+  return n;
+}
+
+__global__ void fmt_len_kernel(const double* __restrict__ v, int64_t count, int32_t nx, int64_t* __restrict__ len,
+                               int32_t* __restrict__ host) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  char buf[40];
+  const int n = format_f6(v[i], buf);
+  host[i] = n < 0 ? 1 : 0;
+  const int w = n < 0 ? 0 : (n < 12 ? 12 : n);
+  len[i] = w + 1;  // the separator: " " inside a row, "\n" at its end
+}
+
+__global__ void fmt_write_kernel(const double* __restrict__ v, int64_t count, int32_t nx,
+                                 const int64_t* __restrict__ off, const int32_t* __restrict__ host,
+                                 char* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  char* o = out + off[i];
+  if (!host[i]) {
+    char buf[40];
+    const int n = format_f6(v[i], buf);
+    const int pad = n < 12 ? 12 - n : 0;
+    for (int k = 0; k < pad; ++k) o[k] = ' ';
+    for (int k = 0; k < n; ++k) o[pad + k] = buf[k];
+    o[pad + n] = ((i + 1) % nx == 0) ? '\n' : ' ';
+  }
+}
+
+template <typename F>
+int with_lines(mg_context* ctx, const char* text, int64_t nbytes, F&& body) {
+  cudaStream_t s = ctx->stream;
+  const int64_t nch = (nbytes + kChunk - 1) / kChunk;
+  mg::Carver cv;
+  cv.reserve<char>(nbytes + 1);
+  cv.reserve<int64_t>(nch + 1);
+  cv.reserve<int64_t>(nch + 1);
+  cv.reserve<char>(mg::scan_temp_bytes(nch));
+  void* ws = mg::workspace(ctx, cv.off);
+  if (!ws) return MG_ERR_NOMEM;
+  cv = mg::Carver{static_cast<char*>(ws), 0};
+  char* t = cv.take<char>(nbytes + 1);
+  int64_t* ccount = cv.take<int64_t>(nch + 1);
+  int64_t* coff = cv.take<int64_t>(nch + 1);
+  void* tmp = cv.take<char>(mg::scan_temp_bytes(nch));
+  MG_TRY_CUDA(cudaMemcpyAsync(t, text, nbytes, cudaMemcpyHostToDevice, s));
+  line_count_kernel<<<(unsigned)nch, kThreads, 0, s>>>(t, nbytes, ccount);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(mg::exclusive_scan(ccount, coff, nch, tmp, mg::scan_temp_bytes(nch), s));
+  int64_t L = 0;
+  MG_TRY_CUDA(cudaMemcpyAsync(&L, coff + nch, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MG_TRY_CUDA(cudaStreamSynchronize(s));
+  // The per-line buffers live in a second allocation: the workspace above
+  // holds the text.
+  int64_t* starts = nullptr;
+  MG_TRY_CUDA(cudaMallocAsync(&starts, sizeof(int64_t) * (L + 1), s));
+  line_fill_kernel<<<(unsigned)nch, kThreads, 0, s>>>(t, nbytes, coff, starts);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  const int rc = body(t, L, starts);
+  cudaFreeAsync(starts, s);
+  return rc;
+}
+
+// The lines a host istringstream must read (numbers outside the fast path).
+std::vector<int64_t> host_lines(mg_context* ctx, const int32_t* flags, int64_t L, int32_t want, int* rc) {
+  std::vector<int32_t> h(L);
+  *rc = MG_OK;
+  if (L == 0) return {};
+  if (cudaMemcpyAsync(h.data(), flags, sizeof(int32_t) * L, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+    *rc = mg::fail(ctx, MG_ERR_CUDA, "text I/O: device copy failed");
+    return {};
+  }
+  std::vector<int64_t> out;
+  for (int64_t l = 0; l < L; ++l)
+    if (h[l] == want) out.push_back(l);
+  return out;
+}
+
+std::string host_line(const char* text, int64_t nbytes, const std::vector<int64_t>& starts, int64_t l) {
+  const int64_t s = starts[l];
+  int64_t e = (l + 1 < (int64_t)starts.size()) ? starts[l + 1] - 1 : nbytes;
+  if (l + 1 >= (int64_t)starts.size() && nbytes > 0 && text[nbytes - 1] == '\n') e = nbytes - 1;
+  return std::string(text + s, text + e);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mg_parse_grid_obs(mg_context* ctx, const char* text, int64_t nbytes, double missing_value, int32_t* xyz,
+                      double* vals, int64_t cap, int64_t* count) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(text && nbytes >= 0 && count, "mg_parse_grid_obs: bad arguments");
+  *count = 0;
+  if (nbytes == 0) return MG_OK;
+  cudaStream_t s = ctx->stream;
+  return with_lines(ctx, text, nbytes, [&](const char* t, int64_t L, int64_t* starts) -> int {
+    ObsLines ol{};
+    unsigned long long* marks = nullptr;  // first header, first separator after it
+    int64_t *keep = nullptr, *pos = nullptr;
+    void* tmp = nullptr;
+    const size_t tmpb = mg::scan_temp_bytes(L);
+    MG_TRY_CUDA(cudaMallocAsync(&ol.type, sizeof(int32_t) * L, s));
+    MG_TRY_CUDA(cudaMallocAsync(&ol.ival, sizeof(int32_t) * 4 * L, s));
+    MG_TRY_CUDA(cudaMallocAsync(&ol.dval, sizeof(double) * 4 * L, s));
+    MG_TRY_CUDA(cudaMallocAsync(&marks, sizeof(unsigned long long) * 2, s));
+    MG_TRY_CUDA(cudaMallocAsync(&keep, sizeof(int64_t) * (L + 1), s));
+    MG_TRY_CUDA(cudaMallocAsync(&pos, sizeof(int64_t) * (L + 1), s));
+    MG_TRY_CUDA(cudaMallocAsync(&tmp, tmpb, s));
+    auto release = [&]() {
+      cudaFreeAsync(ol.type, s);
+      cudaFreeAsync(ol.ival, s);
+      cudaFreeAsync(ol.dval, s);
+      cudaFreeAsync(marks, s);
+      cudaFreeAsync(keep, s);
+      cudaFreeAsync(pos, s);
+      cudaFreeAsync(tmp, s);
+    };
+    MG_TRY_CUDA(cudaMemsetAsync(marks, 0xff, sizeof(unsigned long long) * 2, s));
+    const unsigned g = (unsigned)((L + kThreads - 1) / kThreads);
+    obs_lines_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, ol, marks);
+    MG_COUNT_LAUNCH();
+    obs_sep_kernel<<<g, kThreads, 0, s>>>(ol.type, L, marks, marks + 1);
+    MG_COUNT_LAUNCH();
+    MG_TRY_CUDA(cudaGetLastError());
+    // Lines with numbers outside the fast path: the reference's own
+    // extraction on the host.
+    int rc = MG_OK;
+    const std::vector<int64_t> hl = host_lines(ctx, ol.type, L, kHost, &rc);
+    if (rc != MG_OK) return release(), rc;
+    if (!hl.empty()) {
+      std::vector<int64_t> hs(L);
+      MG_TRY_CUDA(cudaMemcpyAsync(hs.data(), starts, sizeof(int64_t) * L, cudaMemcpyDeviceToHost, s));
+      MG_TRY_CUDA(cudaStreamSynchronize(s));
+      for (int64_t l : hl) {
+        std::istringstream iss(host_line(text, nbytes, hs, l));
+        int time, z, y, x;
+        double znu, lon, lat, v;
+        int32_t ty = kBad;
+        if (iss >> time >> z >> y >> x >> znu >> lon >> lat >> v) {
+          const int32_t iv[4] = {time, z, y, x};
+          const double dv[4] = {znu, lon, lat, v};
+          MG_TRY_CUDA(cudaMemcpyAsync(ol.ival + 4 * l, iv, sizeof(iv), cudaMemcpyHostToDevice, s));
+          MG_TRY_CUDA(cudaMemcpyAsync(ol.dval + 4 * l, dv, sizeof(dv), cudaMemcpyHostToDevice, s));
+          ty = kData;
+        }
+        MG_TRY_CUDA(cudaMemcpyAsync(ol.type + l, &ty, sizeof(ty), cudaMemcpyHostToDevice, s));
+        MG_TRY_CUDA(cudaStreamSynchronize(s));
+      }
+    }
+    obs_keep_kernel<<<g, kThreads, 0, s>>>(ol, L, marks + 1, missing_value, keep);
+    MG_COUNT_LAUNCH();
+    MG_TRY_CUDA(mg::exclusive_scan(keep, pos, L, tmp, tmpb, s));
+    int64_t total = 0;
+    MG_TRY_CUDA(cudaMemcpyAsync(&total, pos + L, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MG_TRY_CUDA(cudaStreamSynchronize(s));
+    *count = total;
+    if (total > cap || (total > 0 && (!xyz || !vals))) {
+      release();
+      return mg::fail(ctx, MG_ERR_CAPACITY, "mg_parse_grid_obs: output arrays too small");
+    }
+    if (total > 0) {
+      obs_write_kernel<<<g, kThreads, 0, s>>>(ol, L, keep, pos, xyz, vals);
+      MG_COUNT_LAUNCH();
+    }
+    MG_TRY_CUDA(cudaGetLastError());
+    release();
+    return MG_OK;
+  });
+}
+
+int mg_parse_values(mg_context* ctx, const char* text, int64_t nbytes, double* out, int64_t cap, int64_t* count) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(text && nbytes >= 0 && count, "mg_parse_values: bad arguments");
+  *count = 0;
+  if (nbytes == 0) return MG_OK;
+  cudaStream_t s = ctx->stream;
+  return with_lines(ctx, text, nbytes, [&](const char* t, int64_t L, int64_t* starts) -> int {
+    int64_t *counts = nullptr, *offs = nullptr;
+    int32_t* host = nullptr;
+    void* tmp = nullptr;
+    const size_t tmpb = mg::scan_temp_bytes(L);
+    MG_TRY_CUDA(cudaMallocAsync(&counts, sizeof(int64_t) * (L + 1), s));
+    MG_TRY_CUDA(cudaMallocAsync(&offs, sizeof(int64_t) * (L + 1), s));
+    MG_TRY_CUDA(cudaMallocAsync(&host, sizeof(int32_t) * L, s));
+    MG_TRY_CUDA(cudaMallocAsync(&tmp, tmpb, s));
+    auto release = [&]() {
+      cudaFreeAsync(counts, s);
+      cudaFreeAsync(offs, s);
+      cudaFreeAsync(host, s);
+      cudaFreeAsync(tmp, s);
+    };
+    const unsigned g = (unsigned)((L + kThreads - 1) / kThreads);
+    values_count_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, counts, host);
+    MG_COUNT_LAUNCH();
+    MG_TRY_CUDA(cudaGetLastError());
+    int rc = MG_OK;
+    const std::vector<int64_t> hl = host_lines(ctx, host, L, 1, &rc);
+    if (rc != MG_OK) return release(), rc;
+    std::vector<int64_t> hs;
+    std::vector<std::vector<double>> hv(hl.size());
+    if (!hl.empty()) {
+      hs.resize(L);
+      MG_TRY_CUDA(cudaMemcpyAsync(hs.data(), starts, sizeof(int64_t) * L, cudaMemcpyDeviceToHost, s));
+      MG_TRY_CUDA(cudaStreamSynchronize(s));
+      for (size_t q = 0; q < hl.size(); ++q) {
+        std::istringstream iss(host_line(text, nbytes, hs, hl[q]));
+        double v;
+        while (iss >> v) hv[q].push_back(v);
+        const int64_t c = (int64_t)hv[q].size();
+        MG_TRY_CUDA(cudaMemcpyAsync(counts + hl[q], &c, sizeof(c), cudaMemcpyHostToDevice, s));
+        MG_TRY_CUDA(cudaStreamSynchronize(s));
+      }
+    }
+    MG_TRY_CUDA(mg::exclusive_scan(counts, offs, L, tmp, tmpb, s));
+    int64_t total = 0;
+    MG_TRY_CUDA(cudaMemcpyAsync(&total, offs + L, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    MG_TRY_CUDA(cudaStreamSynchronize(s));
+    *count = total;
+    if (total > cap || (total > 0 && !out)) {
+      release();
+      return mg::fail(ctx, MG_ERR_CAPACITY, "mg_parse_values: output array too small");
+    }
+    if (total > 0) {
+      values_write_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, offs, host, out);
+      MG_COUNT_LAUNCH();
+      MG_TRY_CUDA(cudaGetLastError());
+      for (size_t q = 0; q < hl.size(); ++q) {
+        if (hv[q].empty()) continue;
+        int64_t o = 0;
+        MG_TRY_CUDA(cudaMemcpyAsync(&o, offs + hl[q], sizeof(o), cudaMemcpyDeviceToHost, s));
+        MG_TRY_CUDA(cudaStreamSynchronize(s));
+        MG_TRY_CUDA(cudaMemcpyAsync(out + o, hv[q].data(), sizeof(double) * hv[q].size(), cudaMemcpyHostToDevice, s));
+      }
+      MG_TRY_CUDA(cudaStreamSynchronize(s));
+    }
+    release();
+    return MG_OK;
+  });
+}
+
+int mg_format_state(mg_context* ctx, const double* values, int32_t nx, int32_t ny, char* out, int64_t cap,
+                    int64_t* nbytes) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(values && nx > 0 && ny > 0 && nbytes, "mg_format_state: bad arguments");
+  cudaStream_t s = ctx->stream;
+  const int64_t count = (int64_t)nx * ny;
+  const size_t tmpb = mg::scan_temp_bytes(count);
+  int64_t *len = nullptr, *off = nullptr;
+  int32_t* host = nullptr;
+  void* tmp = nullptr;
+  MG_TRY_CUDA(cudaMallocAsync(&len, sizeof(int64_t) * (count + 1), s));
+  MG_TRY_CUDA(cudaMallocAsync(&off, sizeof(int64_t) * (count + 1), s));
+  MG_TRY_CUDA(cudaMallocAsync(&host, sizeof(int32_t) * count, s));
+  MG_TRY_CUDA(cudaMallocAsync(&tmp, tmpb, s));
+  auto release = [&]() {
+    cudaFreeAsync(len, s);
+    cudaFreeAsync(off, s);
+    cudaFreeAsync(host, s);
+    cudaFreeAsync(tmp, s);
+  };
+  const unsigned g = (unsigned)((count + kThreads - 1) / kThreads);
+  fmt_len_kernel<<<g, kThreads, 0, s>>>(values, count, nx, len, host);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  // Values the device does not format: their text length comes from the host.
+  int rc = MG_OK;
+  const std::vector<int64_t> hl = host_lines(ctx, host, count, 1, &rc);
+  if (rc != MG_OK) return release(), rc;
+  std::vector<std::string> htxt(hl.size());
+  for (size_t q = 0; q < hl.size(); ++q) {
+    double v = 0.0;
+    MG_TRY_CUDA(cudaMemcpyAsync(&v, values + hl[q], sizeof(v), cudaMemcpyDeviceToHost, s));
+    MG_TRY_CUDA(cudaStreamSynchronize(s));
+    std::ostringstream os;
+    os << std::fixed;
+    os.precision(6);
+    os.width(12);
+    os << v;
+    htxt[q] = os.str() + (((hl[q] + 1) % nx == 0) ? "\n" : " ");
+    const int64_t l = (int64_t)htxt[q].size();
+    MG_TRY_CUDA(cudaMemcpyAsync(len + hl[q], &l, sizeof(l), cudaMemcpyHostToDevice, s));
+    MG_TRY_CUDA(cudaStreamSynchronize(s));
+  }
+  MG_TRY_CUDA(mg::exclusive_scan(len, off, count, tmp, tmpb, s));
+  int64_t total = 0;
+  MG_TRY_CUDA(cudaMemcpyAsync(&total, off + count, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  MG_TRY_CUDA(cudaStreamSynchronize(s));
+  *nbytes = total;
+  if (total > cap || !out) {
+    release();
+    return out ? mg::fail(ctx, MG_ERR_CAPACITY, "mg_format_state: output buffer too small") : MG_ERR_CAPACITY;
+  }
+  char* dout = nullptr;
+  MG_TRY_CUDA(cudaMallocAsync(&dout, (size_t)total, s));
+  fmt_write_kernel<<<g, kThreads, 0, s>>>(values, count, nx, off, host, dout);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  MG_TRY_CUDA(cudaMemcpyAsync(out, dout, (size_t)total, cudaMemcpyDeviceToHost, s));
+  MG_TRY_CUDA(cudaStreamSynchronize(s));
+  for (size_t q = 0; q < hl.size(); ++q) {
+    int64_t o = 0;
+    MG_TRY_CUDA(cudaMemcpy(&o, off + hl[q], sizeof(o), cudaMemcpyDeviceToHost));
+    std::memcpy(out + o, htxt[q].data(), htxt[q].size());
+  }
+  cudaFreeAsync(dout, s);
+  release();
+  return MG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+"""GPU: the device text I/O against the reference's formats.  Expected
+values come from Python's own conversions (float() is correctly rounded as
+strtod is; '%12.6f' rounds the binary value exactly as printf does), with
+the reference's line rules (GridObservation.hpp:395-474, SimpleState.hpp:
+160-188, 248-263) restated below."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from metada_gb300 import kernels as K
+from metada_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+HEADER = "Time Z   Y   X   ZNU      XLONG_U    XLAT_U     Simple"
+SEP = "-" * 80
+
+
+def _ref_parse_obs(text: str, missing: float):
+    """The loop of GridObservation::loadFromFile on well-formed tokens."""
+    out = []
+    header = started = False
+    for line in text.split("\n"):
+        if not line:
+            continue
+        if "Time" in line and "XLONG_U" in line:
+            header = True
+            continue
+        if "---" in line and not line.strip("- \t"):
+            if header:
+                started = True
+            continue
+        if not started:
+            continue
+        parts = line.split()
+        try:
+            t, z, y, x = (int(v) for v in parts[:4])
+            znu, lon, lat, val = (float(v) for v in parts[4:8])
+        except (ValueError, IndexError):
+            continue
+        if len(parts) < 8:
+            continue
+        if val != missing:
+            out.append((x, y, z, znu, lon, lat, val))
+    return out
+
+
+def test_parse_grid_obs_written_by_the_reference_writer(dev):
+    c = syn.global_etkf_grid(case=9)
+    import tempfile
+    from pathlib import Path
+
+    with tempfile.TemporaryDirectory() as td:
+        p = Path(td) / "obs.txt"
+        syn.write_grid_obs(p, c.obs_xy, c.yo)
+        text = p.read_bytes()
+    xyz, vals = K.parse_grid_obs(text)
+    want = _ref_parse_obs(text.decode(), -999.0)
+    assert xyz.shape[0] == len(want) == len(c.yo)
+    w = np.array(want)
+    assert np.array_equal(xyz.cpu().numpy(), w[:, :3].astype(np.int32))
+    assert np.array_equal(vals.cpu().numpy(), w[:, 3:])
+
+
+def test_parse_grid_obs_line_rules_and_number_forms(dev):
+    lines = [
+        "0 1 2 3 0.5 1.0 2.0 9.0",          # before any header: ignored
+        HEADER,
+        "0 1 2 3 0.5 1.0 2.0 8.0",          # header but no separator yet: ignored
+        SEP,
+        "0    1   3   4  0.7035   -82.7143   32.6471     0.2052",
+        "",
+        "0\t1\t3\t9\t0.7035\t-79.8571\t32.6471\t-999.0",   # missing value: dropped
+        "0 1 5 6 .5 +1.25 -0.0 1e-3",
+        "0 1 5 7 7.0e+1 1E2 3.5E-2 -0.0",
+        "0 1 5 8 0.1 0.2 0.3 123456789012345678901234.5",    # long mantissa: host path
+        "0 1 5 9 0.1 0.2 0.3 4.9e-324",                      # subnormal: host path
+        "bad line with words",
+        "0 1 5",                                             # too few fields
+        "0 1 5 10 0.25 0.5 0.75 1.5\r",                      # CRLF line
+        SEP,                                                 # later separators: skipped
+        HEADER,
+        "0 1 6 0 1 2 3 4 trailing tokens are ignored",
+    ]
+    text = ("\n".join(lines) + "\n").encode()
+    xyz, vals = K.parse_grid_obs(text)
+    want = [
+        (4, 3, 1, 0.7035, -82.7143, 32.6471, 0.2052),
+        (6, 5, 1, 0.5, 1.25, -0.0, 1e-3),
+        (7, 5, 1, 70.0, 100.0, 0.035, -0.0),
+        (8, 5, 1, 0.1, 0.2, 0.3, float("123456789012345678901234.5")),
+        (9, 5, 1, 0.1, 0.2, 0.3, 4.9e-324),
+        (10, 5, 1, 0.25, 0.5, 0.75, 1.5),
+        (0, 6, 1, 1.0, 2.0, 3.0, 4.0),
+    ]
+    w = np.array(want)
+    assert np.array_equal(xyz.cpu().numpy(), w[:, :3].astype(np.int32))
+    got = vals.cpu().numpy()
+    assert np.array_equal(got, w[:, 3:])
+    assert math.copysign(1.0, got[1, 2]) < 0 and math.copysign(1.0, got[2, 3]) < 0  # -0.0 kept
+
+
+@pytest.mark.parametrize("nx,ny", [(36, 18), (360, 180)])
+def test_state_round_trip(dev, nx, ny):
+    g = np.random.default_rng(nx)
+    v = g.standard_normal(nx * ny) * 10.0 ** g.integers(-7, 9, nx * ny)
+    v[:8] = [0.0078125, -0.0078125, 2.5e-7, -2.5e-7, -0.0, 0.5e-6, 1.0 / 3.0, 2.0 ** 60]  # ties, -0, host path
+    text = K.format_state(torch.tensor(v, device=dev), nx, ny)
+    rows = [" ".join("%12.6f" % x for x in v[y * nx:(y + 1) * nx]) for y in range(ny)]
+    want = ("\n".join(rows) + "\n").encode()
+    assert text == want
+    back = K.parse_values(text).cpu().numpy()
+    assert np.array_equal(back, np.array([float(t) for t in want.split()]))
+
+
+def test_parse_values_stops_a_line_at_the_first_failed_extraction(dev):
+    text = b"1.5 2.5 x 3.5\n  4 5e1\n\n-0.25 .75 7.\n1 2 3 4 5 6 7 8 9 10 11 12.000000000000000000001\n"
+    got = K.parse_values(text).cpu().numpy()
+    want = [1.5, 2.5, 4.0, 50.0, -0.25, 0.75, 7.0] + [float(i) for i in range(1, 12)] + [12.000000000000000000001]
+    assert np.array_equal(got, np.array(want))
