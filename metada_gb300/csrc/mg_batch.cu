@@ -14,7 +14,11 @@
 // LETKF: an FP32 Gram, a loose FP32 Jacobi with one Newton-Schulz
 // re-orthonormalisation (solve1), the Gram rebuilt from the factor
 // B = R^-1/2 Y' V1 (rebuild), and a first-order Daleckii-Krein evaluation of
-// A2^-1/2 and A2^-1 in that basis (solve2).
+// A2^-1/2 and A2^-1 in that basis (solve2).  It touches no FP64 element with
+// the FP64 pipe, which GB300 runs at about 1/64 of the FP32 rate:
+//   prep_obs_mixed (case, 32 obs)     Y', d, 1/sigma^2 in FP32 (FP64 values as FP32 pairs)
+//   update_mixed   (case, 512 states) member mean, X', Xa = m + X' T and the FP64
+//                                     write-back in one pass (no prep_state, no X' buffer)
 // Items are ordered largest first within each kernel.  The same sequence of
 // launches is captured once into a CUDA graph and replayed.  The obs chunk
 // of the Gram items and the member-count bucket boundaries are chosen by an
@@ -25,6 +29,7 @@
 #include <vector>
 
 #include "mg_dense.cuh"
+#include "mg_ffloat.cuh"
 #include "mg_internal.h"
 
 struct DevCase {
@@ -47,10 +52,16 @@ struct DevCase {
   double* Gpart;  // nchunk x k x k
   double* bpart;  // nchunk x k
   double* T;      // k x k
-  float* Y32;     // p x k FP32 copy of Y' (mixed Hunt path), or null
-  float* V1;      // k x k stage-1 basis (mixed Hunt path), or null
+  // mixed path with the symmetric square root (FP32 throughout), else null
+  float* Y32;     // p x k Y'
+  float* d32;     // p innovations
+  float* rinv32;  // p 1/sigma^2
+  float* Gp32;    // nchunk x k x k partial Grams
+  float* bp32;    // nchunk x k partial b
+  float* V1;      // k x k stage-1 basis
+  float* T32;     // k x k transform
   int64_t nchunk;
-  int64_t ntiles;  // update tiles
+  int64_t ntiles;  // update items of the case
 };
 
 struct WorkItem {
@@ -77,6 +88,7 @@ struct mg_etkf_batch {
   unsigned long long* counters = nullptr;  // per-case finished update tiles
   unsigned long long* times = nullptr;     // [0] start, [1 + c] case finish (ns)
   int* status = nullptr;
+  const int* order = nullptr;  // case indices, largest k first (one CTA per case kernels)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
@@ -139,12 +151,228 @@ __global__ void __launch_bounds__(kThreads) batch_prep_obs_kernel(const DevCase*
     const int i = lane + 32 * t;
     if (i < k) {
       c.Y[o * k + i] = h[t] - ym;
-      if (c.Y32) c.Y32[o * k + i] = (float)(h[t] - ym);
     }
   }
   if (lane == 0) {
     c.d[o] = c.yo[o] - ym;
     c.rinv[o] = 1.0 / c.rvar[o];
+  }
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// Mixed path: Y', d and 1/sigma^2 in FP32 for kObsWarp obs per warp, all
+// their member values gathered before any is used.  The FP64 values enter
+// as FP32 pairs (split_double); the member mean is taken twice (of the pairs,
+// then of the residuals), so Y' keeps full FP32 accuracy however large the
+// values are against their spread.
+constexpr int kObsWarp = 4;
+constexpr int kObsItem = kObsWarp * (kThreads / 32);
+
+__global__ void __launch_bounds__(kThreads) batch_prep_obs_mixed_kernel(const DevCase* __restrict__ cases,
+                                                                        const WorkItem* __restrict__ items,
+                                                                        unsigned long long* times) {
+  const WorkItem it = items[blockIdx.x];
+  const DevCase& c = cases[it.c];
+  if (blockIdx.x == 0 && threadIdx.x == 0) times[0] = globaltimer();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int k = c.k;
+  const int64_t ob = it.a + (int64_t)warp * kObsWarp;
+  double hv[kObsWarp][4];
+#pragma unroll
+  for (int u = 0; u < kObsWarp; ++u) {
+    const int64_t o = ob + u;
+    const bool valid = o < it.b;
+    const int64_t node = (valid && !c.HX) ? c.obs_node[o] : 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int i = lane + 32 * t;
+      hv[u][t] = 0.0;
+      if (valid && i < k) hv[u][t] = c.HX ? c.HX[o * k + i] : c.X[(int64_t)i * c.ld + node];
+    }
+  }
+  const float inv_k = 1.0f / (float)k;
+#pragma unroll
+  for (int u = 0; u < kObsWarp; ++u) {
+    const int64_t o = ob + u;
+    float hh[4], hl[4], s = 0.0f;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      mg::split_double(hv[u][t], hh[t], hl[t]);
+      s += hh[t] + hl[t];
+    }
+    const float m1 = warp_sum(s) * inv_k;
+    float pv[4], s2 = 0.0f;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      pv[t] = (lane + 32 * t < k) ? __fadd_rn(__fsub_rn(hh[t], m1), hl[t]) : 0.0f;
+      s2 += pv[t];
+    }
+    const float m2 = warp_sum(s2) * inv_k;
+    if (o < it.b) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int i = lane + 32 * t;
+        if (i < k) c.Y32[o * k + i] = pv[t] - m2;
+      }
+      if (lane == 0) {  // FP32 pairs again: no FP64 instruction per obs
+        float yh, yl, vh, vl;
+        mg::split_double(c.yo[o], yh, yl);
+        mg::split_double(c.rvar[o], vh, vl);
+        c.d32[o] = __fsub_rn(__fadd_rn(__fsub_rn(yh, m1), yl), m2);
+        c.rinv32[o] = 1.0f / __fadd_rn(vh, vl);
+      }
+    }
+  }
+}
+
+// Mixed path update, fused with the member mean: for each tile of kUpdS
+// states of one case, split the members into FP32 pairs, take the FP32 mean
+// m, X' = (hi - m) + lo in shared memory, Xa' = T^T X' by a register-tiled
+// FP32 product (thread: R consecutive members x 4 states), and write
+// m + Xa' back in place as FP64 through a TwoSum pair.  The transform is
+// staged once per item of kUpdItemS states.
+constexpr int kUpdS = 64;
+constexpr int kUpdItemS = 512;
+
+__host__ __device__ constexpr int upd_kmax(int k) { return k <= 32 ? 32 : (k <= 64 ? 64 : 128); }
+__host__ __device__ constexpr size_t upd_ts_floats(int maxk) { return (size_t)maxk * upd_kmax(maxk); }
+__host__ __device__ constexpr size_t upd_bytes(int maxk) {
+  return sizeof(float) * (upd_ts_floats(maxk) + (size_t)maxk * kUpdS + 5 * kUpdS);
+}
+
+template <int R>
+__device__ __forceinline__ void load_row(const float* p, float (&v)[R]) {
+  if constexpr (R % 4 == 0) {
+#pragma unroll
+    for (int a = 0; a < R; a += 4) {
+      const float4 t = *reinterpret_cast<const float4*>(p + a);
+      v[a] = t.x;
+      v[a + 1] = t.y;
+      v[a + 2] = t.z;
+      v[a + 3] = t.w;
+    }
+  } else {
+#pragma unroll
+    for (int a = 0; a < R; a += 2) {
+      const float2 t = *reinterpret_cast<const float2*>(p + a);
+      v[a] = t.x;
+      v[a + 1] = t.y;
+    }
+  }
+}
+
+template <int KMAX>
+__device__ __forceinline__ void update_mixed_item(const DevCase& c, const WorkItem& it, float* Ts, float* Xs,
+                                                  float* part, float* ms) {
+  constexpr int R = KMAX / 16, JQ = KMAX / 4;
+  const int k = c.k, tid = threadIdx.x;
+  for (int e = tid; e < k * KMAX; e += kThreads) {
+    const int j = e / KMAX, i = e % KMAX;
+    Ts[e] = i < k ? c.T32[j * k + i] : 0.0f;
+  }
+  const float inv_k = 1.0f / (float)k;
+  const int s = tid % kUpdS, q = tid / kUpdS;        // mean phase: state, member quarter
+  const int ti = tid / 16, ts = tid % 16, i0 = ti * R;  // product: members i0.., states 4 ts..
+  for (int64_t s0 = it.a; s0 < it.b; s0 += kUpdS) {
+    const int cnt = (int)(it.b - s0 < kUpdS ? it.b - s0 : kUpdS);
+    float lo[JQ];
+    float sum = 0.0f;
+    const double* xs = c.X + s0 + s;
+    // all loads of a batch are issued before any is split (the split branches)
+    constexpr int LB = JQ < 16 ? JQ : 16;
+#pragma unroll
+    for (int u0 = 0; u0 < JQ; u0 += LB) {
+      double raw[LB];
+#pragma unroll
+      for (int v = 0; v < LB; ++v) {
+        const int j = q + 4 * (u0 + v);
+        raw[v] = (j < k && s < cnt) ? __ldcs(xs + (int64_t)j * c.ld) : 0.0;
+      }
+#pragma unroll
+      for (int v = 0; v < LB; ++v) {
+        const int j = q + 4 * (u0 + v);
+        float h, l;
+        mg::split_double(raw[v], h, l);
+        lo[u0 + v] = l;
+        if (j < k) Xs[j * kUpdS + s] = h;
+        sum += h + l;
+      }
+    }
+    part[q * kUpdS + s] = sum;
+    __syncthreads();
+    const float mf = (((part[s] + part[kUpdS + s]) + part[2 * kUpdS + s]) + part[3 * kUpdS + s]) * inv_k;
+    if (q == 0) ms[s] = mf;
+#pragma unroll
+    for (int u = 0; u < JQ; ++u) {
+      const int j = q + 4 * u;
+      if (j < k) Xs[j * kUpdS + s] = __fadd_rn(__fsub_rn(Xs[j * kUpdS + s], mf), lo[u]);
+    }
+    __syncthreads();
+    float acc[R][4];
+#pragma unroll
+    for (int a = 0; a < R; ++a) acc[a][0] = acc[a][1] = acc[a][2] = acc[a][3] = 0.0f;
+    if (i0 < k) {
+#pragma unroll 4
+      for (int j = 0; j < k; ++j) {
+        const float4 xv = *reinterpret_cast<const float4*>(Xs + j * kUpdS + 4 * ts);
+        float tv[R];
+        load_row<R>(Ts + j * KMAX + i0, tv);
+#pragma unroll
+        for (int a = 0; a < R; ++a) {
+          acc[a][0] = fmaf(tv[a], xv.x, acc[a][0]);
+          acc[a][1] = fmaf(tv[a], xv.y, acc[a][1]);
+          acc[a][2] = fmaf(tv[a], xv.z, acc[a][2]);
+          acc[a][3] = fmaf(tv[a], xv.w, acc[a][3]);
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < R; ++a)
+      if (i0 + a < k)
+        *reinterpret_cast<float4*>(Xs + (i0 + a) * kUpdS + 4 * ts) = make_float4(acc[a][0], acc[a][1], acc[a][2],
+                                                                                 acc[a][3]);
+    __syncthreads();
+    for (int e = tid; e < k * kUpdS; e += kThreads) {
+      const int i = e / kUpdS, ss = e % kUpdS;
+      if (ss < cnt) {
+        float y, ye;
+        mg::two_sum(ms[ss], Xs[e], y, ye);
+        c.X[(int64_t)i * c.ld + s0 + ss] = mg::pair_to_double(y, ye);
+      }
+    }
+    if (c.mean_out && tid < cnt) c.mean_out[s0 + tid] = mg::pair_to_double(ms[tid], 0.0f);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 2) batch_update_mixed_kernel(const DevCase* __restrict__ cases,
+                                                                         const WorkItem* __restrict__ items,
+                                                                         int maxk, unsigned long long* counters,
+                                                                         unsigned long long* times) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const WorkItem it = items[blockIdx.x];
+  const DevCase& c = cases[it.c];
+  float* Ts = reinterpret_cast<float*>(smem_raw);
+  float* Xs = Ts + upd_ts_floats(maxk);
+  float* part = Xs + (size_t)maxk * kUpdS;
+  float* ms = part + 4 * kUpdS;
+  const int km = upd_kmax(c.k);
+  if (km == 32)
+    update_mixed_item<32>(c, it, Ts, Xs, part, ms);
+  else if (km == 64)
+    update_mixed_item<64>(c, it, Ts, Xs, part, ms);
+  else
+    update_mixed_item<128>(c, it, Ts, Xs, part, ms);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned long long done = atomicAdd(&counters[it.c], 1ull) + 1ull;
+    if ((int64_t)done == c.ntiles) times[1 + it.c] = globaltimer();
   }
 }
 
@@ -171,12 +399,22 @@ __global__ void __launch_bounds__(kThreads) batch_gram_kernel(const DevCase* __r
     for (int e = tid; e < cnt * KMAX; e += kThreads) {
       const int r = e / KMAX, j = e - r * KMAX;
       TE v = TE(0);
-      if (j < k) v = (sizeof(TE) == 4) ? (TE)c.Y32[(c0 + r) * k + j] : (TE)c.Y[(c0 + r) * k + j];
+      if (j < k) {
+        if constexpr (sizeof(TE) == 4)
+          v = c.Y32[(c0 + r) * k + j];
+        else
+          v = c.Y[(c0 + r) * k + j];
+      }
       Ys[e] = v;
     }
     if (tid < cnt) {
-      sr[tid] = (TE)c.rinv[c0 + tid];
-      sd[tid] = (TE)c.d[c0 + tid];
+      if constexpr (sizeof(TE) == 4) {
+        sr[tid] = c.rinv32[c0 + tid];
+        sd[tid] = c.d32[c0 + tid];
+      } else {
+        sr[tid] = c.rinv[c0 + tid];
+        sd[tid] = c.d[c0 + tid];
+      }
     }
     __syncthreads();
     for (int r = 0; r < cnt; ++r) {
@@ -196,15 +434,17 @@ __global__ void __launch_bounds__(kThreads) batch_gram_kernel(const DevCase* __r
     __syncthreads();
   }
   const int64_t chunk = it.pad;
-  double* G = c.Gpart + chunk * k * k;
+  // partials in the element type (FP32 partials are summed in FP32)
+  TE* G = (sizeof(TE) == 4) ? (TE*)c.Gp32 + chunk * k * k : (TE*)c.Gpart + chunk * k * k;
+  TE* bp = (sizeof(TE) == 4) ? (TE*)c.bp32 : (TE*)c.bpart;
 #pragma unroll
   for (int a = 0; a < R; ++a)
 #pragma unroll
     for (int b = 0; b < R; ++b) {
       const int i = ti + 16 * a, j = tj + 16 * b;
-      if (i < k && j < k) G[i * k + j] = (double)acc[a][b];
+      if (i < k && j < k) G[i * k + j] = acc[a][b];
     }
-  if (tid < k) c.bpart[chunk * k + tid] = (double)bacc;
+  if (tid < k) bp[chunk * k + tid] = bacc;
 }
 
 // ---- mixed path with the symmetric square root (FP32, k <= 112) ----
@@ -220,26 +460,27 @@ __host__ __device__ constexpr size_t solve2_floats(int kp) { return 3 * (size_t)
 
 // Stage 1 of one case: A = (k-1)/rho I + G (FP32 from the partials), loose
 // Jacobi, V1 back to orthogonal, V1 to global memory.
-__global__ void __launch_bounds__(kThreads) batch_solve1_kernel(const DevCase* __restrict__ cases, int flags) {
+__global__ void __launch_bounds__(kThreads) batch_solve1_kernel(const DevCase* __restrict__ cases,
+                                                                const int* __restrict__ order, int flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const DevCase& c = cases[blockIdx.x];
+  const DevCase& c = cases[order[blockIdx.x]];
   const int k = c.k, kp = k + (k & 1), lda = mix_lda(kp), ldv = mix_ldv(kp);
   float* A = reinterpret_cast<float*>(smem_raw);
   float* Vt = A + round4(kp * lda);
   float* tmp = Vt + kp * ldv;
   float4* rot = reinterpret_cast<float4*>(tmp + 32 * 128);
   const int tid = threadIdx.x;
-  const double diag = (flags & MG_INFL_COMPAT) ? (double)(k - 1) : (double)(k - 1) / c.rho;
+  const float diagf = (flags & MG_INFL_COMPAT) ? (float)(k - 1) : (float)(k - 1) / (float)c.rho;
   for (int e = tid; e < kp * kp; e += kThreads) {
     const int i = e / kp, j = e - i * kp;
-    double s = 0.0;
+    float s = 0.0f;
     if (i < k && j < k) {
-      for (int64_t b = 0; b < c.nchunk; ++b) s += c.Gpart[b * k * k + i * k + j];
-      if (i == j) s += diag;
+      for (int64_t b = 0; b < c.nchunk; ++b) s += c.Gp32[b * k * k + i * k + j];
+      if (i == j) s += diagf;
     } else if (i == j) {
-      s = 1.0;
+      s = 1.0f;
     }
-    A[i * lda + j] = (float)s;
+    A[i * lda + j] = s;
   }
   __syncthreads();
   mg::cta_jacobi_tri<128, kThreads>(A, lda, Vt, ldv, kp, kStage1Tol, 30, rot);
@@ -284,7 +525,7 @@ __global__ void __launch_bounds__(kThreads) batch_rebuild_kernel(const DevCase* 
       const int r = e / KMAX, j = e - r * KMAX;
       Ys[e] = (j < k) ? c.Y32[(c0 + r) * k + j] : 0.0f;
     }
-    if (tid < cnt) sw[tid] = (float)sqrt(c.rinv[c0 + tid]);
+    if (tid < cnt) sw[tid] = sqrtf(c.rinv32[c0 + tid]);
     __syncthreads();
     float sacc[RW][CW];
 #pragma unroll
@@ -323,13 +564,13 @@ __global__ void __launch_bounds__(kThreads) batch_rebuild_kernel(const DevCase* 
     }
     __syncthreads();
   }
-  double* G = c.Gpart + (int64_t)it.pad * k * k;
+  float* G = c.Gp32 + (int64_t)it.pad * k * k;
 #pragma unroll
   for (int a = 0; a < R; ++a)
 #pragma unroll
     for (int b = 0; b < R; ++b) {
       const int i = ti + 16 * a, j = tj + 16 * b;
-      if (i < k && j < k) G[i * k + j] = (double)acc[a][b];
+      if (i < k && j < k) G[i * k + j] = acc[a][b];
     }
 }
 
@@ -337,10 +578,12 @@ __global__ void __launch_bounds__(kThreads) batch_rebuild_kernel(const DevCase* 
 // nearly diagonal, so W = c V1 (A2^-1/2) V1^T and wa = V1 (A2^-1) V1^T b come
 // from the first-order Daleckii-Krein formula (closed-form divided
 // differences -1/(s_i s_j (s_i + s_j)), s = sqrt(d), and -1/(d_i d_j)).
-__global__ void __launch_bounds__(kThreads) batch_solve2_kernel(const DevCase* __restrict__ cases, int flags,
+__global__ void __launch_bounds__(kThreads) batch_solve2_kernel(const DevCase* __restrict__ cases,
+                                                                const int* __restrict__ order, int flags,
                                                                 int* status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const DevCase& c = cases[blockIdx.x];
+  const int ci = order[blockIdx.x];
+  const DevCase& c = cases[ci];
   const int k = c.k, kp = k + (k & 1), lda = mix_lda(kp);
   float* V = reinterpret_cast<float*>(smem_raw);  // k x k (lda)
   float* A2 = V + kp * lda;
@@ -352,25 +595,25 @@ __global__ void __launch_bounds__(kThreads) batch_solve2_kernel(const DevCase* _
   float* lam = wa + kp;
   const int tid = threadIdx.x;
   const bool compat_infl = flags & MG_INFL_COMPAT;
-  const double diag = compat_infl ? (double)(k - 1) : (double)(k - 1) / c.rho;
+  const float diag = compat_infl ? (float)(k - 1) : (float)(k - 1) / (float)c.rho;
   for (int e = tid; e < k * k; e += kThreads) {
     const int i = e / k, j = e - i * k;
     V[i * lda + j] = c.V1[e];
-    double s = 0.0;
-    for (int64_t b = 0; b < c.nchunk; ++b) s += c.Gpart[b * k * k + e];
+    float s = 0.0f;
+    for (int64_t b = 0; b < c.nchunk; ++b) s += c.Gp32[b * k * k + e];
     if (i == j) s += diag;
-    A2[i * lda + j] = (float)s;
+    A2[i * lda + j] = s;
   }
   for (int i = tid; i < k; i += kThreads) {
-    double s = 0.0;
-    for (int64_t b = 0; b < c.nchunk; ++b) s += c.bpart[b * k + i];
-    bv[i] = (float)s;
+    float s = 0.0f;
+    for (int64_t b = 0; b < c.nchunk; ++b) s += c.bp32[b * k + i];
+    bv[i] = s;
   }
   __syncthreads();
   for (int i = tid; i < k; i += kThreads) {
     const float l = A2[i * lda + i];
     lam[i] = l;
-    if (!(l > 0.0f) || !(l < 3.0e38f)) atomicExch(status, 1 + (int)blockIdx.x);
+    if (!(l > 0.0f) || !(l < 3.0e38f)) atomicExch(status, 1 + ci);
     float s = 0.0f;  // u = V1^T b
     for (int j = 0; j < k; ++j) s += V[j * lda + i] * bv[j];
     uv[i] = s;
@@ -407,21 +650,23 @@ __global__ void __launch_bounds__(kThreads) batch_solve2_kernel(const DevCase* _
     Tm[i * lda + j] = s;
   }
   __syncthreads();
-  const double scale = compat_infl ? c.rho : 1.0;
+  const float scale = compat_infl ? (float)c.rho : 1.0f;
   for (int e = tid; e < k * k; e += kThreads) {  // T[j][i] = scale (wa_j + W_ji), W = Tm V1^T
     const int j = e / k, i = e - j * k;
     float s = 0.0f;
     for (int m = 0; m < k; ++m) s += Tm[j * lda + m] * V[i * lda + m];
-    c.T[j * k + i] = scale * ((double)wa[j] + (double)s);
+    c.T32[j * k + i] = scale * (wa[j] + s);
   }
 }
 
 // One CTA per case: sum the partials, solve, write T (FP64; the case's
 // k x k system is its only O(k^3) work).
-__global__ void __launch_bounds__(kThreads) batch_solve_kernel(const DevCase* __restrict__ cases, int flags,
+__global__ void __launch_bounds__(kThreads) batch_solve_kernel(const DevCase* __restrict__ cases,
+                                                               const int* __restrict__ order, int flags,
                                                                int* status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const DevCase& c = cases[blockIdx.x];
+  const int ci = order[blockIdx.x];
+  const DevCase& c = cases[ci];
   const int k = c.k, kp = k + (k & 1), lda = kp + 1;
   double* A = reinterpret_cast<double*>(smem_raw);
   double* V = A + kp * lda;
@@ -461,7 +706,7 @@ __global__ void __launch_bounds__(kThreads) batch_solve_kernel(const DevCase* __
     const int j = e / k, i = e - j * k;
     c.T[j * k + i] = scale * (wa[j] + A[j * lda + i]);
   }
-  if (tid == 0 && !ok) atomicExch(status, 1 + (int)blockIdx.x);
+  if (tid == 0 && !ok) atomicExch(status, 1 + ci);
 }
 
 template <typename TE>
@@ -508,9 +753,16 @@ int kclass_of(int k, int mode) {
   return 2;
 }
 
+// The mixed path with the symmetric square root runs the FP32 two-stage
+// solve; with the Cholesky square root it keeps the FP64 Gram and solve.
+bool mixed_hunt(const mg_etkf_batch* b) {
+  return b->precision == MG_PREC_MIXED && !(b->flags & MG_SQRT_CHOLESKY);
+}
+
 // Builds the item tables and workspace for the current tuning.
 int build(mg_context* ctx, mg_etkf_batch* b) {
   const bool f64 = b->precision == MG_PREC_FP64;
+  const bool mh = mixed_hunt(b);
   const size_t te = f64 ? 8 : 4;
   std::vector<DevCase> dc(b->ncases);
   std::vector<WorkItem> st_items, ob_items, up_items, gr_items[3];
@@ -532,31 +784,42 @@ int build(mg_context* ctx, mg_etkf_batch* b) {
     c.rho = h.rho;
     c.mean_out = h.mean_out;
     c.nchunk = (h.p + b->gram_chunk - 1) / b->gram_chunk;
-    c.ntiles = (h.n + kUpdTile - 1) / kUpdTile;
     b->maxk = std::max(b->maxk, h.k);
-    cv.reserve<double>(h.n);
-    cv.reserve<char>((size_t)h.n * h.k * te);
-    cv.reserve<double>((size_t)h.p * h.k);
-    cv.reserve<double>(h.p);
-    cv.reserve<double>(h.p);
-    cv.reserve<double>((size_t)c.nchunk * h.k * h.k);
-    cv.reserve<double>((size_t)c.nchunk * h.k);
-    cv.reserve<double>((size_t)h.k * h.k);
-    if (!f64) {
+    if (mh) {  // FP32 workspace only; the update reads and writes the members in place
+      const int64_t upd = kUpdItemS;
+      c.ntiles = (h.n + upd - 1) / upd;
       cv.reserve<float>((size_t)h.p * h.k);
+      cv.reserve<float>(h.p);
+      cv.reserve<float>(h.p);
+      cv.reserve<float>((size_t)c.nchunk * h.k * h.k);
+      cv.reserve<float>((size_t)c.nchunk * h.k);
       cv.reserve<float>((size_t)h.k * h.k);
+      cv.reserve<float>((size_t)h.k * h.k);
+      for (int64_t o = 0; o < h.p; o += kObsItem) ob_items.push_back({i, 0, o, std::min<int64_t>(h.p, o + kObsItem)});
+      for (int64_t s = 0; s < h.n; s += upd) up_items.push_back({i, 0, s, std::min<int64_t>(h.n, s + upd)});
+    } else {
+      c.ntiles = (h.n + kUpdTile - 1) / kUpdTile;
+      cv.reserve<double>(h.n);
+      cv.reserve<char>((size_t)h.n * h.k * te);
+      cv.reserve<double>((size_t)h.p * h.k);
+      cv.reserve<double>(h.p);
+      cv.reserve<double>(h.p);
+      cv.reserve<double>((size_t)c.nchunk * h.k * h.k);
+      cv.reserve<double>((size_t)c.nchunk * h.k);
+      cv.reserve<double>((size_t)h.k * h.k);
+      for (int64_t s = 0; s < h.n; s += kStateTile)
+        st_items.push_back({i, 0, s, std::min<int64_t>(h.n, s + kStateTile)});
+      for (int64_t o = 0; o < h.p; o += kObsTile) ob_items.push_back({i, 0, o, std::min<int64_t>(h.p, o + kObsTile)});
+      for (int64_t s = 0; s < h.n; s += kUpdTile) up_items.push_back({i, 0, s, std::min<int64_t>(h.n, s + kUpdTile)});
     }
-    for (int64_t s = 0; s < h.n; s += kStateTile) st_items.push_back({i, 0, s, std::min<int64_t>(h.n, s + kStateTile)});
-    for (int64_t o = 0; o < h.p; o += kObsTile) ob_items.push_back({i, 0, o, std::min<int64_t>(h.p, o + kObsTile)});
-    for (int64_t s = 0; s < h.n; s += kUpdTile) up_items.push_back({i, 0, s, std::min<int64_t>(h.n, s + kUpdTile)});
     for (int64_t ch = 0; ch < c.nchunk; ++ch) {
       const int64_t o0 = ch * b->gram_chunk;
       gr_items[c.kclass].push_back({i, (int32_t)ch, o0, std::min<int64_t>(h.p, o0 + b->gram_chunk)});
     }
   }
-  // Largest first (work per item ~ k^2 for the Gram, k for the others).
+  // Largest first (work per item ~ k^2 x its length for the Gram and the update).
   auto by_k = [&](const WorkItem& x, const WorkItem& y) {
-    const int64_t wx = (int64_t)dc[x.c].k * (x.b - x.a), wy = (int64_t)dc[y.c].k * (y.b - y.a);
+    const int64_t wx = (int64_t)dc[x.c].k * dc[x.c].k * (x.b - x.a), wy = (int64_t)dc[y.c].k * dc[y.c].k * (y.b - y.a);
     return wx > wy;
   };
   for (auto& g : gr_items) std::stable_sort(g.begin(), g.end(), by_k);
@@ -581,6 +844,7 @@ int build(mg_context* ctx, mg_etkf_batch* b) {
   cv.reserve<unsigned long long>(b->ncases);
   cv.reserve<unsigned long long>(b->ncases + 1);
   cv.reserve<int>(4);
+  cv.reserve<int>(b->ncases);
   if (cv.off > b->ws_bytes) {
     if (b->ws) cudaFree(b->ws);
     b->ws = nullptr;
@@ -595,24 +859,42 @@ int build(mg_context* ctx, mg_etkf_batch* b) {
   for (int i = 0; i < b->ncases; ++i) {
     const mg_etkf_case& h = b->host_cases[i];
     DevCase& c = dc[i];
-    c.mean = cv.take<double>(h.n);
-    c.Xp = cv.take<char>((size_t)h.n * h.k * te);
-    c.Y = cv.take<double>((size_t)h.p * h.k);
-    c.d = cv.take<double>(h.p);
-    c.rinv = cv.take<double>(h.p);
-    c.Gpart = cv.take<double>((size_t)c.nchunk * h.k * h.k);
-    c.bpart = cv.take<double>((size_t)c.nchunk * h.k);
-    c.T = cv.take<double>((size_t)h.k * h.k);
-    c.Y32 = f64 ? nullptr : cv.take<float>((size_t)h.p * h.k);
-    c.V1 = f64 ? nullptr : cv.take<float>((size_t)h.k * h.k);
+    if (mh) {
+      c.mean = nullptr;
+      c.Xp = nullptr;
+      c.Y = c.d = c.rinv = c.Gpart = c.bpart = c.T = nullptr;
+      c.Y32 = cv.take<float>((size_t)h.p * h.k);
+      c.d32 = cv.take<float>(h.p);
+      c.rinv32 = cv.take<float>(h.p);
+      c.Gp32 = cv.take<float>((size_t)c.nchunk * h.k * h.k);
+      c.bp32 = cv.take<float>((size_t)c.nchunk * h.k);
+      c.V1 = cv.take<float>((size_t)h.k * h.k);
+      c.T32 = cv.take<float>((size_t)h.k * h.k);
+    } else {
+      c.mean = cv.take<double>(h.n);
+      c.Xp = cv.take<char>((size_t)h.n * h.k * te);
+      c.Y = cv.take<double>((size_t)h.p * h.k);
+      c.d = cv.take<double>(h.p);
+      c.rinv = cv.take<double>(h.p);
+      c.Gpart = cv.take<double>((size_t)c.nchunk * h.k * h.k);
+      c.bpart = cv.take<double>((size_t)c.nchunk * h.k);
+      c.T = cv.take<double>((size_t)h.k * h.k);
+      c.Y32 = c.d32 = c.rinv32 = c.Gp32 = c.bp32 = c.V1 = c.T32 = nullptr;
+    }
   }
   b->dcases = cv.take<DevCase>(b->ncases);
   b->items = cv.take<WorkItem>(all.size());
   b->counters = cv.take<unsigned long long>(b->ncases);
   b->times = cv.take<unsigned long long>(b->ncases + 1);
   b->status = cv.take<int>(4);
+  int* order = cv.take<int>(b->ncases);
+  b->order = order;
+  std::vector<int> ord(b->ncases);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return dc[x].k > dc[y].k; });
   MG_TRY_CUDA(cudaMemcpy(b->dcases, dc.data(), sizeof(DevCase) * dc.size(), cudaMemcpyHostToDevice));
   MG_TRY_CUDA(cudaMemcpy(b->items, all.data(), sizeof(WorkItem) * all.size(), cudaMemcpyHostToDevice));
+  MG_TRY_CUDA(cudaMemcpy(order, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
@@ -624,11 +906,6 @@ int build(mg_context* ctx, mg_etkf_batch* b) {
   return MG_OK;
 }
 
-// The mixed path with the symmetric square root runs the FP32 two-stage
-// solve; with the Cholesky square root it keeps the FP64 Gram and solve.
-bool mixed_hunt(const mg_etkf_batch* b) {
-  return b->precision == MG_PREC_MIXED && !(b->flags & MG_SQRT_CHOLESKY);
-}
 
 constexpr size_t rebuild_bytes(int kmax) { return sizeof(float) * ((size_t)kmax * (kmax + 1) + 2 * 32 * (size_t)kmax); }
 
@@ -645,12 +922,17 @@ int enqueue(mg_context* ctx, mg_etkf_batch* b) {
       batch_prep_state_kernel<float><<<(unsigned)b->n_state_items, kStateTile, 0, s>>>(b->dcases, b->items + b->state_off, b->times);
     MG_COUNT_LAUNCH();
   }
+  const bool mh = mixed_hunt(b);
   if (b->n_obs_items) {
-    batch_prep_obs_kernel<<<(unsigned)b->n_obs_items, kObsTile * 32, 0, s>>>(b->dcases, b->items + b->obs_off);
+    if (mh)
+      batch_prep_obs_mixed_kernel<<<(unsigned)b->n_obs_items, kThreads, 0, s>>>(b->dcases, b->items + b->obs_off,
+                                                                                 b->times);
+    else
+      batch_prep_obs_kernel<<<(unsigned)b->n_obs_items, kObsTile * 32, 0, s>>>(b->dcases, b->items + b->obs_off);
     MG_COUNT_LAUNCH();
   }
   const int kp = b->maxk + (b->maxk & 1);
-  if (mixed_hunt(b)) {
+  if (mh) {
     if (b->gram_cnt[0]) {
       batch_gram_kernel<float, 32><<<(unsigned)b->gram_cnt[0], kThreads, 0, s>>>(b->dcases, b->items + b->gram_off[0]);
       MG_COUNT_LAUNCH();
@@ -664,7 +946,7 @@ int enqueue(mg_context* ctx, mg_etkf_batch* b) {
                                                                                   b->items + b->gram_off[2]);
       MG_COUNT_LAUNCH();
     }
-    batch_solve1_kernel<<<(unsigned)b->ncases, kThreads, sizeof(float) * solve1_floats(kp), s>>>(b->dcases, b->flags);
+    batch_solve1_kernel<<<(unsigned)b->ncases, kThreads, sizeof(float) * solve1_floats(kp), s>>>(b->dcases, b->order, b->flags);
     MG_COUNT_LAUNCH();
     if (b->gram_cnt[0]) {
       batch_rebuild_kernel<32><<<(unsigned)b->gram_cnt[0], kThreads, rebuild_bytes(32), s>>>(b->dcases,
@@ -681,12 +963,11 @@ int enqueue(mg_context* ctx, mg_etkf_batch* b) {
           b->dcases, b->items + b->gram_off[2]);
       MG_COUNT_LAUNCH();
     }
-    batch_solve2_kernel<<<(unsigned)b->ncases, kThreads, sizeof(float) * solve2_floats(kp), s>>>(b->dcases, b->flags,
+    batch_solve2_kernel<<<(unsigned)b->ncases, kThreads, sizeof(float) * solve2_floats(kp), s>>>(b->dcases, b->order, b->flags,
                                                                                                 b->status);
     MG_COUNT_LAUNCH();
-    const size_t usmem = sizeof(float) * ((size_t)b->maxk * b->maxk + 32 * (size_t)(b->maxk + 1));
-    batch_update_kernel<float><<<(unsigned)b->n_update_items, kThreads, usmem, s>>>(b->dcases, b->items + b->update_off,
-                                                                                    b->counters, b->times);
+    batch_update_mixed_kernel<<<(unsigned)b->n_update_items, kThreads, upd_bytes(b->maxk), s>>>(
+        b->dcases, b->items + b->update_off, b->maxk, b->counters, b->times);
     MG_COUNT_LAUNCH();
     MG_TRY_CUDA(cudaGetLastError());
     return MG_OK;
@@ -704,7 +985,7 @@ int enqueue(mg_context* ctx, mg_etkf_batch* b) {
     MG_COUNT_LAUNCH();
   }
   const size_t smem = sizeof(double) * (2 * (size_t)kp * (kp + 1) + 6 * (size_t)kp) + sizeof(int) * (kp + 8) + 64;
-  batch_solve_kernel<<<(unsigned)b->ncases, kThreads, smem, s>>>(b->dcases, b->flags, b->status);
+  batch_solve_kernel<<<(unsigned)b->ncases, kThreads, smem, s>>>(b->dcases, b->order, b->flags, b->status);
   MG_COUNT_LAUNCH();
   const size_t te = f64 ? 8 : 4;
   const size_t usmem = te * ((size_t)b->maxk * b->maxk + 32 * (size_t)(b->maxk + 1));
@@ -737,6 +1018,9 @@ int set_attributes(mg_context* ctx, const mg_etkf_batch* b) {
                                      (int)rebuild_bytes(64)));
     MG_TRY_CUDA(cudaFuncSetAttribute(batch_rebuild_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)rebuild_bytes(128)));
+    MG_TRY_CUDA(cudaFuncSetAttribute(batch_update_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)upd_bytes(b->maxk)));
+    return MG_OK;
   }
   if (te == 8)
     MG_TRY_CUDA(cudaFuncSetAttribute(batch_update_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)usmem));

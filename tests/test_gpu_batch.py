@@ -84,3 +84,26 @@ def test_batch_mixed_within_tolerance_and_graph_replays(dev, cases):
             ma, mw = a.mean(0), w.mean(0)
             assert rel_err(ma, mw) <= 1e-5
             assert rel_err(a - ma, w - mw) <= 1e-5
+
+
+def test_batch_mixed_large_offset_values(dev):
+    """Members and obs around 280 with unit spread (temperatures in K): the
+    mixed path's FP32 perturbations must keep 1e-5 of the spread, which
+    rounding the FP64 values to FP32 alone would not."""
+    sub = syn.uneven_batch(ncases=12, n_range=(2_000, 30_000), p_range=(200, 4_000), case=91)
+    for c in sub:
+        c.X += 280.0
+        c.yo += 280.0
+    d64 = _device_cases(sub, dev)
+    b64 = K.EtkfBatch(d64, flags=0, precision=_lib.MG_PREC_FP64)
+    b64.run(graph=False)
+    b64.finish()
+    dmx = _device_cases(sub, dev)
+    bmx = K.EtkfBatch(dmx, flags=0, precision=_lib.MG_PREC_MIXED)
+    bmx.run(graph=False)
+    bmx.finish()
+    for c, r in zip(dmx, d64):
+        a, w = c["X"].cpu().numpy(), r["X"].cpu().numpy()
+        ma, mw = a.mean(0), w.mean(0)
+        assert rel_err(ma, mw) <= 1e-5
+        assert rel_err(a - ma, w - mw) <= 1e-5
