@@ -53,10 +53,11 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-points", type=int, default=40000, help="local analyses in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["latlon", "uneven", "column"], default="latlon",
+    ap.add_argument("--workload", choices=["latlon", "uneven", "column", "next"], default="latlon",
                     help="latlon: the headline LETKF configuration; uneven: 512 global-ETKF cases of "
                          "uneven sizes in one captured graph (reports analyses/s and p50/p99 latency); "
-                         "column: the learned column operator (training, H(x) plain vs surrogate, LETKF)")
+                         "column: the learned column operator (training, H(x) plain vs surrogate, LETKF); "
+                         "next: the rows beside the analysis (EnKF, diagnostics, nearest node, text I/O)")
     ap.add_argument("--train-steps", type=int, default=6000, help="column workload: Adam steps")
     ap.add_argument("--train-batch", type=int, default=4096, help="column workload: columns per Adam step")
     ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
@@ -363,6 +364,181 @@ def run_uneven(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_next(args) -> None:
+    """The rows beside the analysis, each on device-resident inputs, timed per
+    call (CUDA-synchronised wall clock over --steps calls after --warmup),
+    with the oracle timed on a bounded host sample:
+      enkf     stochastic EnKF, lat-lon state 360x180x10x4 (2.59M values),
+               k=64, 500k obs at state nodes (mixed and FP64)
+      metrics  Metrics::CalculateAll of the same ensemble against a truth
+      nearest  nearest node of 500k obs on a 1000x1000 curvilinear grid
+               (with the vertical index among 40 levels)
+      io       GridObservation text (500k lines) and the state written as
+               SimpleState text ("%12.6f") and read back
+    Bandwidths are algorithmic bytes per call over the call time, against the
+    measured HBM copy rate."""
+    import torch
+
+    import oracle.bind as ob
+    from metada_gb300 import _lib
+    from metada_gb300 import kernels as K
+
+    dev = torch.device("cuda", 0)
+    ctx = K.context(0)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234)
+
+    def per_call(fn, reset=None):
+        for _ in range(args.warmup):
+            if reset:
+                reset()
+            fn()
+        ts = []
+        for _ in range(args.steps):
+            if reset:
+                reset()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return statistics.mean(ts)
+
+    def cpu_time(fn, min_s=2.0):
+        t0 = time.perf_counter()
+        reps = 0
+        while True:
+            fn()
+            reps += 1
+            if time.perf_counter() - t0 >= min_s:
+                return (time.perf_counter() - t0) / reps
+
+    rows = {}
+    threads = ob.load().orc_num_threads()
+    # ---------------------------------------------------------------- EnKF
+    nlon, nlat, nlev, nvar, k, p = 360, 180, 10, 4, 64, 500_000
+    n = nlon * nlat * nlev * nvar
+    truth = torch.randn(n, generator=g, device=dev, dtype=torch.float64)
+    X0 = truth[None, :] + torch.randn((k, n), generator=g, device=dev, dtype=torch.float64)
+    nodes = torch.randint(0, n, (p,), generator=g, device=dev)
+    sigma = 0.5
+    yo = truth[nodes] + sigma * torch.randn(p, generator=g, device=dev, dtype=torch.float64)
+    rvar = torch.full((p,), sigma * sigma, dtype=torch.float64, device=dev)
+    eps = sigma * torch.randn((p, k), generator=g, device=dev, dtype=torch.float64)
+    X = torch.empty_like(X0)
+    HX = X0[:, nodes].T.contiguous()
+    enkf_bytes = 2 * n * k * 8 + 2 * p * k * 8 + 2 * p * 8
+    res = {}
+    for name, prec in (("mixed", _lib.MG_PREC_MIXED), ("fp64", _lib.MG_PREC_FP64)):
+        l0 = ctx.launches()
+        t = per_call(lambda: K.enkf(X, HX, yo, rvar, eps, 1.05, precision=prec), reset=lambda: X.copy_(X0))
+        launches = (ctx.launches() - l0) // (args.warmup + args.steps)
+        res[name] = {"ms_per_call": 1e3 * t, "analyses_per_s": 1.0 / t, "hbm_gbs": enkf_bytes / t / 1e9,
+                     "frac_of_hbm": enkf_bytes / t / 1e9 / hbm, "gpu_launches": int(launches)}
+    # like-for-like at the reference's tutorial-sized ETKF configuration (64x64, k=32, p=1024)
+    from metada_gb300 import synthetic as syn
+    c1 = syn.global_etkf_grid(case=1)
+    HX1 = ob.hx_idw4(c1.X, 64, 64, c1.obs_xy)
+    eps1 = c1.sigma_o * np.random.default_rng(1).standard_normal((len(c1.yo), c1.X.shape[0]))
+    tc = cpu_time(lambda: ob.enkf(c1.X, HX1, c1.yo, c1.rvar, eps1, c1.rho))
+    X1 = torch.tensor(c1.X, device=dev)
+    X10 = X1.clone()
+    d1 = [torch.tensor(a, device=dev) for a in (HX1, c1.yo, c1.rvar, eps1)]
+    tg1 = per_call(lambda: K.enkf(X1, *d1, c1.rho, precision=_lib.MG_PREC_FP64), reset=lambda: X1.copy_(X10))
+    rows["enkf"] = {"metric": "global EnKF analyses/s", "unit": "analyses/s", "value": res["mixed"]["analyses_per_s"],
+                    "config": f"{nlon}x{nlat}x{nlev}x{nvar} state ({n} values), k={k}, p={p}, obs at nodes",
+                    "bound": "hbm", "algorithmic_bytes_per_call": enkf_bytes, **res,
+                    "small_case": {"config": "64x64, k=32, p=1024 (FP64)", "gpu_analyses_per_s": 1.0 / tg1,
+                                   "cpu_analyses_per_s": 1.0 / tc},
+                    "cpu_baseline": {"value": 1.0 / tc, "unit": "analyses/s", "cores": threads, "kind": "port",
+                                     "sample": "the oracle's dense p x p EnKF (the reference's algorithm) on the "
+                                               "64x64, k=32, p=1024 case; the full-size case has a 500k x 500k S"}}
+    del X, HX, eps, yo, rvar, nodes
+    # ------------------------------------------------------------- metrics
+    met_bytes = n * k * 8 + n * 8 + 2 * n * 8
+    l0 = ctx.launches()
+    t = per_call(lambda: K.ens_metrics(X0, truth))
+    launches = (ctx.launches() - l0) // (args.warmup + args.steps)
+    ns = 65_536
+    Xs, ts_ = X0[:, :ns].cpu().numpy(), truth[:ns].cpu().numpy()
+    tcm = cpu_time(lambda: ob.ens_metrics(Xs, ts_))
+    rows["metrics"] = {"metric": "member values/s (Metrics::CalculateAll)", "unit": "values/s", "value": n * k / t,
+                       "ms_per_call": 1e3 * t, "bound": "hbm", "algorithmic_bytes_per_call": met_bytes,
+                       "hbm_gbs": met_bytes / t / 1e9, "frac_of_hbm": met_bytes / t / 1e9 / hbm,
+                       "gpu_launches": int(launches), "config": f"k={k}, n={n}",
+                       "cpu_baseline": {"value": ns * k / tcm, "unit": "values/s", "cores": threads, "kind": "port",
+                                        "sample": f"the oracle on the first {ns} state values"}}
+    del X0, truth
+    torch.cuda.empty_cache()
+    # ------------------------------------------------------------- nearest
+    nx = ny = 1000
+    ii = torch.arange(nx, device=dev, dtype=torch.float64)[None, :].expand(ny, nx)
+    jj = torch.arange(ny, device=dev, dtype=torch.float64)[:, None].expand(ny, nx)
+    nlon_ = (-100.0 + 0.05 * ii + 0.01 * torch.sin(0.1 * jj)).contiguous().reshape(-1)
+    nlat_ = (20.0 + 0.04 * jj + 0.01 * torch.cos(0.1 * ii)).contiguous().reshape(-1)
+    po = 500_000
+    olon = -100.0 + 50.0 * torch.rand(po, generator=g, device=dev, dtype=torch.float64)
+    olat = 20.0 + 40.0 * torch.rand(po, generator=g, device=dev, dtype=torch.float64)
+    vc = torch.linspace(1.0, 0.0, 40, device=dev, dtype=torch.float64)
+    olev = torch.rand(po, generator=g, device=dev, dtype=torch.float64)
+    l0 = ctx.launches()
+    t = per_call(lambda: K.nearest_node(nlat_, nlon_, nx, ny, olat, olon, vc, olev))
+    launches = (ctx.launches() - l0) // (args.warmup + args.steps)
+    xy, kk = K.nearest_node(nlat_, nlon_, nx, ny, olat, olon, vc, olev)
+    pc = 500
+    hl, hn = nlat_.cpu().numpy(), nlon_.cpu().numpy()
+    ola, olo, ole, vch = olat[:pc].cpu().numpy(), olon[:pc].cpu().numpy(), olev[:pc].cpu().numpy(), vc.cpu().numpy()
+    tcn = cpu_time(lambda: ob.nearest_node(hl, hn, nx, ny, ola, olo, vch, ole))
+    wxy, wk = ob.nearest_node(hl, hn, nx, ny, ola, olo, vch, ole)
+    same = bool(np.array_equal(wxy, xy[:pc].cpu().numpy()) and np.array_equal(wk, kk[:pc].cpu().numpy()))
+    rows["nearest"] = {"metric": "geographic obs located/s", "unit": "obs/s", "value": po / t, "ms_per_call": 1e3 * t,
+                       "bound": "latency (hash ring search; nodes and hash fit in L2)", "gpu_launches": int(launches),
+                       "config": f"{nx}x{ny} curvilinear grid, {po} obs, 40 levels",
+                       "sample_identical_to_oracle": same,
+                       "cpu_baseline": {"value": pc / tcn, "unit": "obs/s", "cores": threads, "kind": "port",
+                                        "sample": f"the reference's scan over all nodes for the first {pc} obs"}}
+    # ------------------------------------------------------------------ io
+    rng = np.random.default_rng(5)
+    lines = ["-" * 80, "Time Z   Y   X   ZNU      XLONG_U    XLAT_U     Simple", "-" * 80]
+    zz, yy, xx = rng.integers(1, 40, po), rng.integers(0, 360, po), rng.integers(0, 720, po)
+    vals = rng.standard_normal((po, 4)) * [0.3, 50.0, 30.0, 2.0]
+    lines += [f"0 {a:4d} {b:4d} {c:4d} {v0:8.4f} {v1:10.4f} {v2:10.4f} {v3:10.4f}"
+              for a, b, c, (v0, v1, v2, v3) in zip(zz, yy, xx, vals)]
+    obs_text = ("\n".join(lines) + "\n").encode()
+    l0 = ctx.launches()
+    t_obs = per_call(lambda: K.parse_grid_obs(obs_text))
+    launches_obs = (ctx.launches() - l0) // (args.warmup + args.steps)
+    xyz, ov = K.parse_grid_obs(obs_text)
+    ok_obs = bool(xyz.shape[0] == po and np.array_equal(xyz[:, 0].cpu().numpy(), xx))
+    state = (torch.randn(n, generator=g, device=dev, dtype=torch.float64) * 15.0 + 280.0)
+    t_fmt = per_call(lambda: K.format_state(state, nlon, n // nlon))
+    st_text = K.format_state(state, nlon, n // nlon)
+    t_par = per_call(lambda: K.parse_values(st_text))
+    back = K.parse_values(st_text).cpu().numpy()
+    sample = st_text[: 2_000_000]
+    sample = sample[: sample.rfind(b"\n") + 1]
+    tco = cpu_time(lambda: ob.parse_values(sample))
+    ok_state = bool(np.array_equal(back[: 10_000], ob.parse_values(st_text[: 200_000])[: 10_000]) and
+                    np.abs(back - state.cpu().numpy()).max() <= 5e-7)
+    rows["io"] = {"metric": "text MB/s (parse, host text in; format, host text out)", "unit": "MB/s",
+                  "value": len(st_text) / t_par / 1e6, "bound": "host link + latency of the line index scan",
+                  "parse_grid_obs": {"mb_per_s": len(obs_text) / t_obs / 1e6, "ms_per_call": 1e3 * t_obs,
+                                     "bytes": len(obs_text), "lines": po, "gpu_launches": int(launches_obs),
+                                     "ok": ok_obs},
+                  "parse_values": {"mb_per_s": len(st_text) / t_par / 1e6, "ms_per_call": 1e3 * t_par,
+                                   "bytes": len(st_text), "values": n, "ok": ok_state},
+                  "format_state": {"mb_per_s": len(st_text) / t_fmt / 1e6, "ms_per_call": 1e3 * t_fmt,
+                                   "bytes": len(st_text), "values": n},
+                  "cpu_baseline": {"value": len(sample) / tco / 1e6, "unit": "MB/s", "cores": 1, "kind": "port",
+                                   "sample": f"the reference's getline + istringstream >> double loop "
+                                             f"(SimpleState::readFromFile) over the first {len(sample)} bytes"}}
+    line = {"metric": "rows beside the analysis (EnKF, diagnostics, nearest node, text I/O)", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "data": "synthetic (seeded)", "rows": rows}
+    print(json.dumps(line), flush=True)
+
+
 def run_column(args) -> None:
     """Learned column operator on the 720 x 360 column grid (30 levels, T and
     ln q, 64 members, 200k single-channel column obs): train the surrogate
@@ -491,6 +667,9 @@ def main():
         return
     if args.workload == "column":
         run_column(args)
+        return
+    if args.workload == "next":
+        run_next(args)
         return
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":

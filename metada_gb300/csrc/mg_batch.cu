@@ -30,6 +30,7 @@
 
 #include "mg_dense.cuh"
 #include "mg_ffloat.cuh"
+#include "mg_update.cuh"
 #include "mg_internal.h"
 
 struct DevCase {
@@ -230,126 +231,9 @@ __global__ void __launch_bounds__(kThreads) batch_prep_obs_mixed_kernel(const De
   }
 }
 
-// Mixed path update, fused with the member mean: for each tile of kUpdS
-// states of one case, split the members into FP32 pairs, take the FP32 mean
-// m, X' = (hi - m) + lo in shared memory, Xa' = T^T X' by a register-tiled
-// FP32 product (thread: R consecutive members x 4 states), and write
-// m + Xa' back in place as FP64 through a TwoSum pair.  The transform is
-// staged once per item of kUpdItemS states.
-constexpr int kUpdS = 64;
+// Mixed path update (mg_update.cuh): items of kUpdItemS states, the
+// transform staged once per item.
 constexpr int kUpdItemS = 512;
-
-__host__ __device__ constexpr int upd_kmax(int k) { return k <= 32 ? 32 : (k <= 64 ? 64 : 128); }
-__host__ __device__ constexpr size_t upd_ts_floats(int maxk) { return (size_t)maxk * upd_kmax(maxk); }
-__host__ __device__ constexpr size_t upd_bytes(int maxk) {
-  return sizeof(float) * (upd_ts_floats(maxk) + (size_t)maxk * kUpdS + 5 * kUpdS);
-}
-
-template <int R>
-__device__ __forceinline__ void load_row(const float* p, float (&v)[R]) {
-  if constexpr (R % 4 == 0) {
-#pragma unroll
-    for (int a = 0; a < R; a += 4) {
-      const float4 t = *reinterpret_cast<const float4*>(p + a);
-      v[a] = t.x;
-      v[a + 1] = t.y;
-      v[a + 2] = t.z;
-      v[a + 3] = t.w;
-    }
-  } else {
-#pragma unroll
-    for (int a = 0; a < R; a += 2) {
-      const float2 t = *reinterpret_cast<const float2*>(p + a);
-      v[a] = t.x;
-      v[a + 1] = t.y;
-    }
-  }
-}
-
-template <int KMAX>
-__device__ __forceinline__ void update_mixed_item(const DevCase& c, const WorkItem& it, float* Ts, float* Xs,
-                                                  float* part, float* ms) {
-  constexpr int R = KMAX / 16, JQ = KMAX / 4;
-  const int k = c.k, tid = threadIdx.x;
-  for (int e = tid; e < k * KMAX; e += kThreads) {
-    const int j = e / KMAX, i = e % KMAX;
-    Ts[e] = i < k ? c.T32[j * k + i] : 0.0f;
-  }
-  const float inv_k = 1.0f / (float)k;
-  const int s = tid % kUpdS, q = tid / kUpdS;        // mean phase: state, member quarter
-  const int ti = tid / 16, ts = tid % 16, i0 = ti * R;  // product: members i0.., states 4 ts..
-  for (int64_t s0 = it.a; s0 < it.b; s0 += kUpdS) {
-    const int cnt = (int)(it.b - s0 < kUpdS ? it.b - s0 : kUpdS);
-    float lo[JQ];
-    float sum = 0.0f;
-    const double* xs = c.X + s0 + s;
-    // all loads of a batch are issued before any is split (the split branches)
-    constexpr int LB = JQ < 16 ? JQ : 16;
-#pragma unroll
-    for (int u0 = 0; u0 < JQ; u0 += LB) {
-      double raw[LB];
-#pragma unroll
-      for (int v = 0; v < LB; ++v) {
-        const int j = q + 4 * (u0 + v);
-        raw[v] = (j < k && s < cnt) ? __ldcs(xs + (int64_t)j * c.ld) : 0.0;
-      }
-#pragma unroll
-      for (int v = 0; v < LB; ++v) {
-        const int j = q + 4 * (u0 + v);
-        float h, l;
-        mg::split_double(raw[v], h, l);
-        lo[u0 + v] = l;
-        if (j < k) Xs[j * kUpdS + s] = h;
-        sum += h + l;
-      }
-    }
-    part[q * kUpdS + s] = sum;
-    __syncthreads();
-    const float mf = (((part[s] + part[kUpdS + s]) + part[2 * kUpdS + s]) + part[3 * kUpdS + s]) * inv_k;
-    if (q == 0) ms[s] = mf;
-#pragma unroll
-    for (int u = 0; u < JQ; ++u) {
-      const int j = q + 4 * u;
-      if (j < k) Xs[j * kUpdS + s] = __fadd_rn(__fsub_rn(Xs[j * kUpdS + s], mf), lo[u]);
-    }
-    __syncthreads();
-    float acc[R][4];
-#pragma unroll
-    for (int a = 0; a < R; ++a) acc[a][0] = acc[a][1] = acc[a][2] = acc[a][3] = 0.0f;
-    if (i0 < k) {
-#pragma unroll 4
-      for (int j = 0; j < k; ++j) {
-        const float4 xv = *reinterpret_cast<const float4*>(Xs + j * kUpdS + 4 * ts);
-        float tv[R];
-        load_row<R>(Ts + j * KMAX + i0, tv);
-#pragma unroll
-        for (int a = 0; a < R; ++a) {
-          acc[a][0] = fmaf(tv[a], xv.x, acc[a][0]);
-          acc[a][1] = fmaf(tv[a], xv.y, acc[a][1]);
-          acc[a][2] = fmaf(tv[a], xv.z, acc[a][2]);
-          acc[a][3] = fmaf(tv[a], xv.w, acc[a][3]);
-        }
-      }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int a = 0; a < R; ++a)
-      if (i0 + a < k)
-        *reinterpret_cast<float4*>(Xs + (i0 + a) * kUpdS + 4 * ts) = make_float4(acc[a][0], acc[a][1], acc[a][2],
-                                                                                 acc[a][3]);
-    __syncthreads();
-    for (int e = tid; e < k * kUpdS; e += kThreads) {
-      const int i = e / kUpdS, ss = e % kUpdS;
-      if (ss < cnt) {
-        float y, ye;
-        mg::two_sum(ms[ss], Xs[e], y, ye);
-        c.X[(int64_t)i * c.ld + s0 + ss] = mg::pair_to_double(y, ye);
-      }
-    }
-    if (c.mean_out && tid < cnt) c.mean_out[s0 + tid] = mg::pair_to_double(ms[tid], 0.0f);
-    __syncthreads();
-  }
-}
 
 __global__ void __launch_bounds__(kThreads, 2) batch_update_mixed_kernel(const DevCase* __restrict__ cases,
                                                                          const WorkItem* __restrict__ items,
@@ -358,17 +242,9 @@ __global__ void __launch_bounds__(kThreads, 2) batch_update_mixed_kernel(const D
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const WorkItem it = items[blockIdx.x];
   const DevCase& c = cases[it.c];
-  float* Ts = reinterpret_cast<float*>(smem_raw);
-  float* Xs = Ts + upd_ts_floats(maxk);
-  float* part = Xs + (size_t)maxk * kUpdS;
-  float* ms = part + 4 * kUpdS;
-  const int km = upd_kmax(c.k);
-  if (km == 32)
-    update_mixed_item<32>(c, it, Ts, Xs, part, ms);
-  else if (km == 64)
-    update_mixed_item<64>(c, it, Ts, Xs, part, ms);
-  else
-    update_mixed_item<128>(c, it, Ts, Xs, part, ms);
+  float bg = 0.0f, an = 0.0f;
+  mg::update_mixed<false>(c.X, c.ld, c.k, it.a, it.b, c.T32, c.mean_out, reinterpret_cast<float*>(smem_raw), maxk,
+                          bg, an);
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned long long done = atomicAdd(&counters[it.c], 1ull) + 1ull;
@@ -460,7 +336,8 @@ __host__ __device__ constexpr size_t solve2_floats(int kp) { return 3 * (size_t)
 
 // Stage 1 of one case: A = (k-1)/rho I + G (FP32 from the partials), loose
 // Jacobi, V1 back to orthogonal, V1 to global memory.
-__global__ void __launch_bounds__(kThreads) batch_solve1_kernel(const DevCase* __restrict__ cases,
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) batch_solve1_kernel(const DevCase* __restrict__ cases,
                                                                 const int* __restrict__ order, int flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const DevCase& c = cases[order[blockIdx.x]];
@@ -471,7 +348,7 @@ __global__ void __launch_bounds__(kThreads) batch_solve1_kernel(const DevCase* _
   float4* rot = reinterpret_cast<float4*>(tmp + 32 * 128);
   const int tid = threadIdx.x;
   const float diagf = (flags & MG_INFL_COMPAT) ? (float)(k - 1) : (float)(k - 1) / (float)c.rho;
-  for (int e = tid; e < kp * kp; e += kThreads) {
+  for (int e = tid; e < kp * kp; e += NT) {
     const int i = e / kp, j = e - i * kp;
     float s = 0.0f;
     if (i < k && j < k) {
@@ -483,14 +360,14 @@ __global__ void __launch_bounds__(kThreads) batch_solve1_kernel(const DevCase* _
     A[i * lda + j] = s;
   }
   __syncthreads();
-  mg::cta_jacobi_tri<128, kThreads>(A, lda, Vt, ldv, kp, kStage1Tol, 30, rot);
-  for (int e = tid; e < kp * kp; e += kThreads) {  // eigenvector rows -> row-major V1 in the A region
+  mg::cta_jacobi_tri<128, NT>(A, lda, Vt, ldv, kp, kStage1Tol, 30, rot);
+  for (int e = tid; e < kp * kp; e += NT) {  // eigenvector rows -> row-major V1 in the A region
     const int j = e / kp, i = e - j * kp;
     A[i * lda + j] = Vt[j * ldv + i];
   }
   __syncthreads();
   mg::cta_reorthonormalize<float, 128>(A, kp, lda, Vt, tmp, 32);
-  for (int e = tid; e < k * k; e += kThreads) c.V1[e] = A[(e / k) * lda + e % k];
+  for (int e = tid; e < k * k; e += NT) c.V1[e] = A[(e / k) * lda + e % k];
 }
 
 // Gram of the factor B = diag(sqrt(1/sigma^2)) Y' V1 over one obs chunk:
@@ -532,16 +409,22 @@ __global__ void __launch_bounds__(kThreads) batch_rebuild_kernel(const DevCase* 
     for (int x = 0; x < RW; ++x)
 #pragma unroll
       for (int q = 0; q < CW; ++q) sacc[x][q] = 0.0f;
-    for (int m = 0; m < k; ++m) {
-      float yv[RW], vv[CW];
+    for (int m0 = 0; m0 < k; m0 += 4) {  // rows of Ys and V1s are zero from k to KMAX
+      float4 yv[RW];
 #pragma unroll
-      for (int x = 0; x < RW; ++x) yv[x] = Ys[(wrp * RW + x) * KMAX + m];
+      for (int x = 0; x < RW; ++x) yv[x] = *reinterpret_cast<const float4*>(Ys + (wrp * RW + x) * KMAX + m0);
 #pragma unroll
-      for (int q = 0; q < CW; ++q) vv[q] = V1s[m * LDW + ln + 32 * q];
+      for (int mm = 0; mm < 4; ++mm) {
+        float vv[CW];
 #pragma unroll
-      for (int x = 0; x < RW; ++x)
+        for (int q = 0; q < CW; ++q) vv[q] = V1s[(m0 + mm) * LDW + ln + 32 * q];
 #pragma unroll
-        for (int q = 0; q < CW; ++q) sacc[x][q] += yv[x] * vv[q];
+        for (int x = 0; x < RW; ++x) {
+          const float y = mm == 0 ? yv[x].x : (mm == 1 ? yv[x].y : (mm == 2 ? yv[x].z : yv[x].w));
+#pragma unroll
+          for (int q = 0; q < CW; ++q) sacc[x][q] += y * vv[q];
+        }
+      }
     }
 #pragma unroll
     for (int x = 0; x < RW; ++x) {
@@ -823,7 +706,17 @@ int build(mg_context* ctx, mg_etkf_batch* b) {
     return wx > wy;
   };
   for (auto& g : gr_items) std::stable_sort(g.begin(), g.end(), by_k);
-  std::stable_sort(up_items.begin(), up_items.end(), by_k);
+  if (mh) {
+    // Mixed update items (all of one size) run shortest case first, a case's
+    // items together, so that small cases finish early in the batch.
+    auto work = [&](int ci) { return (double)dc[ci].n * dc[ci].k * dc[ci].k; };
+    std::stable_sort(up_items.begin(), up_items.end(), [&](const WorkItem& x, const WorkItem& y) {
+      if (work(x.c) != work(y.c)) return work(x.c) < work(y.c);
+      return x.c != y.c ? x.c < y.c : x.a < y.a;
+    });
+  } else {
+    std::stable_sort(up_items.begin(), up_items.end(), by_k);
+  }
   std::vector<WorkItem> all;
   b->state_off = (int64_t)all.size();
   all.insert(all.end(), st_items.begin(), st_items.end());
@@ -946,7 +839,12 @@ int enqueue(mg_context* ctx, mg_etkf_batch* b) {
                                                                                   b->items + b->gram_off[2]);
       MG_COUNT_LAUNCH();
     }
-    batch_solve1_kernel<<<(unsigned)b->ncases, kThreads, sizeof(float) * solve1_floats(kp), s>>>(b->dcases, b->order, b->flags);
+    if (b->maxk > 64)  // more threads per rotation round for the large cases
+      batch_solve1_kernel<512><<<(unsigned)b->ncases, 512, sizeof(float) * solve1_floats(kp), s>>>(b->dcases, b->order,
+                                                                                              b->flags);
+    else
+      batch_solve1_kernel<kThreads><<<(unsigned)b->ncases, kThreads, sizeof(float) * solve1_floats(kp), s>>>(
+          b->dcases, b->order, b->flags);
     MG_COUNT_LAUNCH();
     if (b->gram_cnt[0]) {
       batch_rebuild_kernel<32><<<(unsigned)b->gram_cnt[0], kThreads, rebuild_bytes(32), s>>>(b->dcases,
@@ -966,7 +864,7 @@ int enqueue(mg_context* ctx, mg_etkf_batch* b) {
     batch_solve2_kernel<<<(unsigned)b->ncases, kThreads, sizeof(float) * solve2_floats(kp), s>>>(b->dcases, b->order, b->flags,
                                                                                                 b->status);
     MG_COUNT_LAUNCH();
-    batch_update_mixed_kernel<<<(unsigned)b->n_update_items, kThreads, upd_bytes(b->maxk), s>>>(
+    batch_update_mixed_kernel<<<(unsigned)b->n_update_items, kThreads, mg::upd_bytes(b->maxk), s>>>(
         b->dcases, b->items + b->update_off, b->maxk, b->counters, b->times);
     MG_COUNT_LAUNCH();
     MG_TRY_CUDA(cudaGetLastError());
@@ -1008,7 +906,9 @@ int set_attributes(mg_context* ctx, const mg_etkf_batch* b) {
   if (smem > 227 * 1024 || usmem > 227 * 1024) return mg::fail(ctx, MG_ERR_ARG, "mg_etkf_batch: k too large");
   MG_TRY_CUDA(cudaFuncSetAttribute(batch_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (mixed_hunt(b)) {
-    MG_TRY_CUDA(cudaFuncSetAttribute(batch_solve1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    MG_TRY_CUDA(cudaFuncSetAttribute(batch_solve1_kernel<kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(sizeof(float) * solve1_floats(kp))));
+    MG_TRY_CUDA(cudaFuncSetAttribute(batch_solve1_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)(sizeof(float) * solve1_floats(kp))));
     MG_TRY_CUDA(cudaFuncSetAttribute(batch_solve2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)(sizeof(float) * solve2_floats(kp))));
@@ -1019,7 +919,7 @@ int set_attributes(mg_context* ctx, const mg_etkf_batch* b) {
     MG_TRY_CUDA(cudaFuncSetAttribute(batch_rebuild_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)rebuild_bytes(128)));
     MG_TRY_CUDA(cudaFuncSetAttribute(batch_update_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)upd_bytes(b->maxk)));
+                                     (int)mg::upd_bytes(b->maxk)));
     return MG_OK;
   }
   if (te == 8)

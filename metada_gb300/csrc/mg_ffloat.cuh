@@ -19,8 +19,8 @@ namespace mg {
 // The rare FP64 fallbacks live in calls so that they stay real branches: an
 // if-converted (predicated) FP64 instruction still occupies the FP64 pipe
 // for every element, taken or not.
-__device__ __noinline__ float d2f_slow(double x) { return __double2float_rn(x); }
-__device__ __noinline__ double pair_sum_slow(float s, float e) { return (double)s + (double)e; }
+static __device__ __noinline__ float d2f_slow(double x) { return __double2float_rn(x); }
+static __device__ __noinline__ double pair_sum_slow(float s, float e) { return (double)s + (double)e; }
 
 // hi = x with its significand truncated to 24 bits (exact in FP32); lo = the
 // next 23 significand bits, also exact in FP32.

@@ -11,28 +11,49 @@
 // taken per CTA, then over the CTAs in a fixed order by one CTA:
 // deterministic, and equal to the reference's sequential sums to rounding.
 //
-// A CTA stages a tile of 32 state elements x k members in shared memory;
-// the k^2 pair sum of an element is split over the 8 threads of its group.
+// A CTA stages a tile of 32 state elements x k members in shared memory,
+// with an order-preserving integer key per value; each element has a group
+// of 8 threads.  GB300 runs FP64 at about 2 operations per clock per SM, so
+// the CRPS pair term is not the k^2 sum of |x_j - x_l| but its sorted form
+//     sum_j sum_l |x_j - x_l| = 2 sum_j (2 r_j - k + 1) x_j,
+// r_j the rank of x_j (ties broken by member index), with the ranks counted
+// by 32-bit integer comparisons of the keys' top halves (exact recount on
+// the full keys where two members share them): k FP64 FMAs per element
+// instead of 2 k^2 FP64 operations.  Member order of the mean and spread is
+// kept; they are computed by one full warp, a lane per element.
 #include "mg_internal.h"
 
 namespace {
 
 constexpr int kThreads = 256;
 constexpr int kTile = 32;     // state elements per tile
-constexpr int kGroup = kThreads / kTile;  // threads per element in the pair sum
+constexpr int kGroup = kThreads / kTile;  // threads per element
 constexpr int kSums = 9;
 // sums: m - t, (m - t)^2, m, t, m t, m^2, t^2, crps_i, spread_i
 constexpr int kMaxBlocks = 152 * 8;
+constexpr int kOwn = 8;  // members ranked at once by one thread
+
+// Signed 64-bit keys that order like the doubles (NaN aside; -0 < +0 only
+// separates values whose difference is zero).
+__device__ __forceinline__ long long order_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
 
 __global__ void __launch_bounds__(kThreads) metrics_elem_kernel(const double* __restrict__ X, int64_t n, int k,
                                                                 int64_t ld, const double* __restrict__ truth,
                                                                 double* __restrict__ mean_out,
                                                                 double* __restrict__ spread_out,
                                                                 double* __restrict__ partial) {
-  extern __shared__ double xs[];  // k x kTile
+  extern __shared__ double xs[];  // k x kTile values, then k x kTile top-32-bit keys
+  int* ks = reinterpret_cast<int*>(xs + (size_t)k * kTile);
+  __shared__ double coef[256];     // 2 r - k + 1 for rank r
+  __shared__ double sd_sh[kTile], st_sh[kTile];
   __shared__ double red[kSums][kThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int e = tid / kGroup, g = tid % kGroup;  // element of the tile, thread within its group
+  for (int r = tid; r < k; r += kThreads) coef[r] = (double)(2 * r - k + 1);
+  const double inv_k = 1.0 / (double)k, inv_k2 = inv_k * inv_k;
   double acc[kSums];
 #pragma unroll
   for (int s = 0; s < kSums; ++s) acc[s] = 0.0;
@@ -40,21 +61,55 @@ __global__ void __launch_bounds__(kThreads) metrics_elem_kernel(const double* __
     const int cnt = (int)(n - t0 < kTile ? n - t0 : kTile);
     for (int q = tid; q < k * kTile; q += kThreads) {
       const int j = q / kTile, c = q - j * kTile;
-      xs[q] = (c < cnt) ? X[(int64_t)j * ld + t0 + c] : 0.0;
+      const double v = (c < cnt) ? X[(int64_t)j * ld + t0 + c] : 0.0;
+      xs[q] = v;
+      ks[q] = (int)(order_key(v) >> 32);
     }
     __syncthreads();
     const bool valid = e < cnt;
     const int64_t i = t0 + e;
-    double m = 0.0, tr = 0.0, sd = 0.0, st = 0.0;
+    double tr = 0.0, sd = 0.0, st = 0.0;
     if (valid) {
       tr = truth[i];
-      for (int j = 0; j < k; ++j) m = __dadd_rn(m, xs[j * kTile + e]);
-      m = __ddiv_rn(m, (double)k);
-      // pair sum over rows j = g, g + kGroup, ...; truth term likewise
-      for (int j = g; j < k; j += kGroup) {
-        const double xj = xs[j * kTile + e];
-        for (int l = 0; l < k; ++l) sd += fabs(xj - xs[l * kTile + e]);
-        st += fabs(xj - tr);
+      // ranks of members j = g + kGroup u, kOwn at a time, counted on the top
+      // 32 bits of the keys (ordered like the keys); a member that shares
+      // them with another member is recounted on the full keys with ties
+      // broken by member index.  Then the sorted-form sum.
+      for (int u0 = 0; g + kGroup * u0 < k; u0 += kOwn) {
+        int hk[kOwn], lt[kOwn], eq[kOwn];
+#pragma unroll
+        for (int u = 0; u < kOwn; ++u) {
+          const int j = g + kGroup * (u0 + u);
+          hk[u] = j < k ? ks[j * kTile + e] : 0x7fffffff;
+          lt[u] = 0;
+          eq[u] = 0;
+        }
+        for (int l = 0; l < k; ++l) {
+          const int hl = ks[l * kTile + e];
+#pragma unroll
+          for (int u = 0; u < kOwn; ++u) {
+            lt[u] += hl < hk[u] ? 1 : 0;
+            eq[u] += hl == hk[u] ? 1 : 0;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kOwn; ++u) {
+          const int j = g + kGroup * (u0 + u);
+          if (j < k) {
+            const double xj = xs[j * kTile + e];
+            int r = lt[u];
+            if (eq[u] > 1) {  // another member with the same top 32 bits: exact count
+              const long long kj = order_key(xj);
+              r = 0;
+              for (int l = 0; l < k; ++l) {
+                const long long kl = order_key(xs[l * kTile + e]);
+                r += (kl < kj || (kl == kj && l < j)) ? 1 : 0;
+              }
+            }
+            sd = fma(coef[r], xj, sd);
+            st += fabs(xj - tr);
+          }
+        }
       }
     }
 #pragma unroll
@@ -62,24 +117,36 @@ __global__ void __launch_bounds__(kThreads) metrics_elem_kernel(const double* __
       sd += __shfl_down_sync(0xffffffffu, sd, off, kGroup);
       st += __shfl_down_sync(0xffffffffu, st, off, kGroup);
     }
-    if (valid && g == 0) {
+    if (g == 0) {
+      sd_sh[e] = sd;
+      st_sh[e] = st;
+    }
+    __syncthreads();
+    // Mean, spread and the sums: one full warp, a lane per element (an FP64
+    // instruction costs the FP64 pipe the same with one active lane or 32).
+    if (warp == 0 && lane < cnt) {
+      const int64_t il = t0 + lane;
+      const double trl = truth[il];
+      double m = 0.0;
+      for (int j = 0; j < k; ++j) m = __dadd_rn(m, xs[j * kTile + lane]);
+      m = __ddiv_rn(m, (double)k);
       double sp = 0.0;
       for (int j = 0; j < k; ++j) {
-        const double d = __dsub_rn(xs[j * kTile + e], m);
+        const double d = __dsub_rn(xs[j * kTile + lane], m);
         sp = __dadd_rn(sp, __dmul_rn(d, d));
       }
       sp = __dsqrt_rn(__ddiv_rn(sp, (double)(k - 1)));
-      if (mean_out) mean_out[i] = m;
-      if (spread_out) spread_out[i] = sp;
-      const double dm = m - tr;
+      if (mean_out) mean_out[il] = m;
+      if (spread_out) spread_out[il] = sp;
+      const double dm = m - trl;
       acc[0] += dm;
       acc[1] += dm * dm;
       acc[2] += m;
-      acc[3] += tr;
-      acc[4] += m * tr;
+      acc[3] += trl;
+      acc[4] += m * trl;
       acc[5] += m * m;
-      acc[6] += tr * tr;
-      acc[7] += st / (double)k - sd / (2.0 * (double)k * (double)k);
+      acc[6] += trl * trl;
+      acc[7] += st_sh[lane] * inv_k - sd_sh[lane] * inv_k2;  // sum_j sum_l |x_j - x_l| = 2 sd
       acc[8] += sp;
     }
     __syncthreads();
@@ -123,7 +190,7 @@ extern "C" int mg_ens_metrics(mg_context* ctx, const double* X, int64_t n, int32
   MG_CHECK_ARG(X && truth && out && n > 0 && k >= 2 && k <= 256 && ld >= n, "mg_ens_metrics: bad arguments");
   const int64_t tiles = (n + kTile - 1) / kTile;
   const int nblocks = (int)(tiles < kMaxBlocks ? tiles : kMaxBlocks);
-  const size_t smem = sizeof(double) * (size_t)k * kTile;
+  const size_t smem = (sizeof(double) + sizeof(int)) * (size_t)k * kTile;
   void* ws = mg::workspace(ctx, sizeof(double) * ((size_t)nblocks * kSums + 8));
   if (!ws) return MG_ERR_NOMEM;
   double* partial = static_cast<double*>(ws);

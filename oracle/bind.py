@@ -57,6 +57,7 @@ def load() -> ctypes.CDLL:
             "orc_ens_metrics": ([vp, c_int64, c_int32, c_int64, vp, vp, vp, vp], None),
             "orc_nearest_node": ([vp, vp, c_int32, c_int32, vp, vp, c_int64, vp, c_int32, vp, vp, vp], None),
             "orc_enkf": ([vp, c_int64, c_int32, c_int64, vp, vp, vp, vp, c_int64, c_double, vp, vp, vp], ctypes.c_int),
+            "orc_parse_values": ([ctypes.c_char_p, c_int64, vp, c_int64], c_int64),
             "orc_num_threads": ([], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
@@ -260,3 +261,16 @@ def enkf(X, HX, yo, rvar, eps, rho):
 
 def num_threads() -> int:
     return load().orc_num_threads()
+
+
+def parse_values(text: bytes) -> np.ndarray:
+    """SimpleState::readFromFile: the doubles std::istringstream extracts from
+    each line of the text."""
+    lib = load()
+    cap = max(1, text.count(b" ") + text.count(b"\n") + text.count(b"\t") + 1)
+    out = np.empty(cap)
+    n = lib.orc_parse_values(text, len(text), _p(out), cap)
+    if n > cap:
+        out = np.empty(n)
+        n = lib.orc_parse_values(text, len(text), _p(out), n)
+    return out[:n]

@@ -12,6 +12,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <sstream>
+#include <string>
 #include <vector>
 
 #ifdef _OPENMP
@@ -787,6 +789,22 @@ void orc_column_op(const float* T, const float* q, int64_t ncol, int32_t nlev, c
       y[c * nch + ch] = (float)acc;
     }
   }
+}
+
+// SimpleState.hpp:255-261: getline, then `iss >> value` until it fails.
+int64_t orc_parse_values(const char* text, int64_t nbytes, double* out, int64_t cap) {
+  std::istringstream file(std::string(text, (size_t)nbytes));
+  std::string line;
+  int64_t n = 0;
+  while (std::getline(file, line)) {
+    std::istringstream iss(line);
+    double value;
+    while (iss >> value) {
+      if (n < cap) out[n] = value;
+      ++n;
+    }
+  }
+  return n;
 }
 
 }  // extern "C"

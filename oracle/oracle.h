@@ -146,6 +146,11 @@ void orc_nearest_node(const double* node_lat, const double* node_lon, int32_t nx
                       const double* obs_lat, const double* obs_lon, int64_t p, const double* vcoord, int32_t nz,
                       const double* obs_level, int32_t* out_xy, int32_t* out_k);
 
+/* SimpleState::readFromFile (SimpleState.hpp:248-263): every double that
+ * std::istringstream extracts from each line, in order.  Writes at most cap
+ * values and returns the count found. */
+int64_t orc_parse_values(const char* text, int64_t nbytes, double* out, int64_t cap);
+
 /* Symmetric eigen-decomposition by cyclic Jacobi (FP64), A = V diag(w) V^T.
  * A (k x k, row-major) is overwritten.  Returns the number of sweeps. */
 int orc_sym_eig(double* A, int32_t k, double* w, double* V);

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 import torch
 
+import oracle.bind as ob
 from metada_gb300 import kernels as K
 from metada_gb300 import synthetic as syn
 
@@ -113,6 +114,7 @@ def test_state_round_trip(dev, nx, ny):
     assert text == want
     back = K.parse_values(text).cpu().numpy()
     assert np.array_equal(back, np.array([float(t) for t in want.split()]))
+    assert np.array_equal(back, ob.parse_values(text))  # the reference's own extraction loop
 
 
 def test_parse_values_stops_a_line_at_the_first_failed_extraction(dev):
@@ -120,3 +122,4 @@ def test_parse_values_stops_a_line_at_the_first_failed_extraction(dev):
     got = K.parse_values(text).cpu().numpy()
     want = [1.5, 2.5, 4.0, 50.0, -0.25, 0.75, 7.0] + [float(i) for i in range(1, 12)] + [12.000000000000000000001]
     assert np.array_equal(got, np.array(want))
+    assert np.array_equal(got, ob.parse_values(text))

@@ -237,3 +237,12 @@ def test_nearest_node_scan_matches_numpy(built):
     d = np.sqrt((ol[:, None] - lon.ravel()[None]) ** 2 + (oa[:, None] - lat.ravel()[None]) ** 2)
     idx = np.argmin(d, axis=1)  # first minimum, as the scan
     assert np.array_equal(xy[:, 0], idx % nx) and np.array_equal(xy[:, 1], idx // nx)
+
+
+def test_parse_values_is_the_istringstream_loop(built):
+    """SimpleState::readFromFile: a line's extraction stops at the first
+    token that is not a double; the next line starts afresh."""
+    text = b"  1.5 2.25\n-3e2\t4.000000\nbad 5\n7 .5 8x 9\n\n+.25e1 -0.0\n"
+    got = ob.parse_values(text)
+    assert np.array_equal(got, [1.5, 2.25, -300.0, 4.0, 7.0, 0.5, 8.0, 2.5, -0.0])
+    assert np.signbit(got[-1])
