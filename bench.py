@@ -60,9 +60,12 @@ def parse():
                          "next: the rows beside the analysis (EnKF, diagnostics, nearest node, text I/O)")
     ap.add_argument("--train-steps", type=int, default=6000, help="column workload: Adam steps")
     ap.add_argument("--train-batch", type=int, default=4096, help="column workload: columns per Adam step")
-    ap.add_argument("--profile-case", choices=["mixed", "fp64"], default=None,
-                    help="run one batched LETKF on the reduced 180x90x10x4 case (125k obs) and exit; "
-                         "the case ncu captures of the analysis kernel use")
+    ap.add_argument("--profile-case", default=None,
+                    choices=["mixed", "fp64", "uneven", "uneven-small", "enkf", "metrics"],
+                    help="run a profiler case and exit: mixed/fp64 = one batched LETKF on the reduced "
+                         "180x90x10x4 case (125k obs); uneven = the 512-case mixed batch run twice without "
+                         "the graph; uneven-small = its first 64 cases; enkf = the mixed EnKF (2.59M values, "
+                         "k=64, 500k obs) twice; metrics = Metrics::CalculateAll of that ensemble twice")
     return ap.parse_args()
 
 
@@ -286,14 +289,65 @@ def run_reference(args, rank, world):
 
 def profile_case(precision_name: str) -> None:
     """One analysis of a reduced configuration (inputs ~170 MB, above L2; a
-    few hundred MB on the device) for profiler captures."""
+    few hundred MB on the device) for profiler captures, or one of the other
+    workloads' cases."""
     import torch
 
     from metada_gb300 import _lib
+    from metada_gb300 import kernels as K
     from metada_gb300 import synthetic as syn
 
+    dev = torch.device("cuda", 0)
+    if precision_name.startswith("uneven"):
+        cases = syn.uneven_batch(ncases=64 if precision_name == "uneven-small" else 512)
+        dc = [{"X": torch.tensor(c.X, device=dev), "obs_node": torch.tensor(c.obs_node, device=dev),
+               "yo": torch.tensor(c.yo, device=dev),
+               "rvar": torch.full((len(c.yo),), c.sigma_o ** 2, dtype=torch.float64, device=dev), "rho": c.rho}
+              for c in cases]
+        b = K.EtkfBatch(dc, flags=0, precision=_lib.MG_PREC_MIXED)
+        ms = []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.run(graph=False)
+            b.finish()
+            ms.append(1e3 * (time.perf_counter() - t0))
+        b.close()
+        print(json.dumps({"profile_case": precision_name, "cases": len(cases), "ms": ms}))
+        return
+    if precision_name in ("enkf", "metrics"):
+        g = torch.Generator(device=dev)
+        g.manual_seed(1234)
+        n, k, p = 360 * 180 * 10 * 4, 64, 500_000
+        truth = torch.randn(n, generator=g, device=dev, dtype=torch.float64)
+        X0 = truth[None, :] + torch.randn((k, n), generator=g, device=dev, dtype=torch.float64)
+        ms = []
+        if precision_name == "metrics":
+            for _ in range(2):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                K.ens_metrics(X0, truth)
+                torch.cuda.synchronize()
+                ms.append(1e3 * (time.perf_counter() - t0))
+        else:
+            nodes = torch.randint(0, n, (p,), generator=g, device=dev)
+            yo = truth[nodes] + 0.5 * torch.randn(p, generator=g, device=dev, dtype=torch.float64)
+            rvar = torch.full((p,), 0.25, dtype=torch.float64, device=dev)
+            eps = 0.5 * torch.randn((p, k), generator=g, device=dev, dtype=torch.float64)
+            HX = X0[:, nodes].T.contiguous()
+            X = X0.clone()
+            for _ in range(2):
+                X.copy_(X0)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                K.enkf(X, HX, yo, rvar, eps, 1.05, precision=_lib.MG_PREC_MIXED)
+                torch.cuda.synchronize()
+                ms.append(1e3 * (time.perf_counter() - t0))
+        print(json.dumps({"profile_case": precision_name, "ms": ms}))
+        return
+
     c = syn.latlon_letkf_case(nlon=180, nlat=90, nlev=10, nvar=4, k=64, p=125_000, T=45, case=40)
-    w = Workload(c, torch.device("cuda", 0))
+    w = Workload(c, dev)
     st = w.step(_lib.MG_PREC_MIXED if precision_name == "mixed" else _lib.MG_PREC_FP64)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": precision_name, "analyses": st.n_points, "ms_analysis": st.ms_analysis,

@@ -58,6 +58,63 @@ __global__ void node_scatter_kernel(const double* __restrict__ lat, const double
   }
 }
 
+// Bounding box of the nodes: per-CTA (min lon, max lon, min lat, max lat,
+// non-finite count), then one CTA over the CTAs.
+constexpr int kBoxBlocks = 152 * 4;
+
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((__double2hiint(x) >> 20) & 0x7ff) != 0x7ff;
+}
+
+__global__ void __launch_bounds__(kThreads) node_box_kernel(const double* __restrict__ lat,
+                                                            const double* __restrict__ lon, int64_t nn,
+                                                            double* __restrict__ part) {
+  __shared__ double red[5][kThreads / 32];
+  double v[5] = {INFINITY, -INFINITY, INFINITY, -INFINITY, 0.0};
+  for (int64_t t = (int64_t)blockIdx.x * kThreads + threadIdx.x; t < nn; t += (int64_t)gridDim.x * kThreads) {
+    const double x = lon[t], y = lat[t];
+    if (!finite_bits(x) || !finite_bits(y)) {
+      v[4] += 1.0;
+      continue;
+    }
+    v[0] = fmin(v[0], x);
+    v[1] = fmax(v[1], x);
+    v[2] = fmin(v[2], y);
+    v[3] = fmax(v[3], y);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    v[0] = fmin(v[0], __shfl_xor_sync(0xffffffffu, v[0], off));
+    v[1] = fmax(v[1], __shfl_xor_sync(0xffffffffu, v[1], off));
+    v[2] = fmin(v[2], __shfl_xor_sync(0xffffffffu, v[2], off));
+    v[3] = fmax(v[3], __shfl_xor_sync(0xffffffffu, v[3], off));
+    v[4] += __shfl_xor_sync(0xffffffffu, v[4], off);
+  }
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < 5; ++q) red[q][warp] = v[q];
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    const int q = threadIdx.x;
+    double r = red[q][0];
+    for (int w = 1; w < kThreads / 32; ++w)
+      r = (q == 0 || q == 2) ? fmin(r, red[q][w]) : (q == 4 ? r + red[q][w] : fmax(r, red[q][w]));
+    part[(int64_t)blockIdx.x * 5 + q] = r;
+  }
+}
+
+__global__ void node_box_final_kernel(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  const int q = threadIdx.x;
+  if (q >= 5) return;
+  double r = part[q];
+  for (int b = 1; b < nb; ++b) {
+    const double x = part[(int64_t)b * 5 + q];
+    r = (q == 0 || q == 2) ? fmin(r, x) : (q == 4 ? r + x : fmax(r, x));
+  }
+  out[q] = r;
+}
+
 __device__ __forceinline__ double node_dist(double lat, double lon, double glat, double glon) {
   const double dx = __dsub_rn(lon, glon), dy = __dsub_rn(lat, glat);
   return __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
@@ -138,20 +195,24 @@ extern "C" int mg_nearest_node(mg_context* ctx, const double* node_lat, const do
   if (p == 0) return MG_OK;
   const int64_t nn = (int64_t)nx * ny;
   cudaStream_t s = ctx->stream;
-  // Bounding box of the nodes (host: one copy of the coordinates).
-  std::vector<double> hlat(nn), hlon(nn);
-  MG_TRY_CUDA(cudaMemcpyAsync(hlat.data(), node_lat, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
-  MG_TRY_CUDA(cudaMemcpyAsync(hlon.data(), node_lon, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
-  MG_TRY_CUDA(cudaStreamSynchronize(s));
-  double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
-  for (int64_t t = 0; t < nn; ++t) {
-    if (!std::isfinite(hlat[t]) || !std::isfinite(hlon[t]))
-      return mg::fail(ctx, MG_ERR_ARG, "mg_nearest_node: node coordinates must be finite");
-    xmin = std::min(xmin, hlon[t]);
-    xmax = std::max(xmax, hlon[t]);
-    ymin = std::min(ymin, hlat[t]);
-    ymax = std::max(ymax, hlat[t]);
+  // Bounding box of the nodes (device reduction, five values back).
+  const int nbox = (int)std::min<int64_t>(kBoxBlocks, (nn + kThreads - 1) / kThreads);
+  double box[5];
+  {
+    void* wsb = mg::workspace(ctx, sizeof(double) * (5 * (size_t)nbox + 8));
+    if (!wsb) return MG_ERR_NOMEM;
+    double* part = static_cast<double*>(wsb);
+    double* dbox = part + 5 * (size_t)nbox;
+    node_box_kernel<<<nbox, kThreads, 0, s>>>(node_lat, node_lon, nn, part);
+    MG_COUNT_LAUNCH();
+    node_box_final_kernel<<<1, 32, 0, s>>>(part, nbox, dbox);
+    MG_COUNT_LAUNCH();
+    MG_TRY_CUDA(cudaGetLastError());
+    MG_TRY_CUDA(cudaMemcpyAsync(box, dbox, sizeof(box), cudaMemcpyDeviceToHost, s));
+    MG_TRY_CUDA(cudaStreamSynchronize(s));
   }
+  if (box[4] != 0.0) return mg::fail(ctx, MG_ERR_ARG, "mg_nearest_node: node coordinates must be finite");
+  const double xmin = box[0], xmax = box[1], ymin = box[2], ymax = box[3];
   NodeHash g;
   const double span_x = std::max(xmax - xmin, 1e-9), span_y = std::max(ymax - ymin, 1e-9);
   const double cells = std::max(1.0, (double)nn / 4.0);
