@@ -61,11 +61,15 @@ def parse():
     ap.add_argument("--train-steps", type=int, default=6000, help="column workload: Adam steps")
     ap.add_argument("--train-batch", type=int, default=4096, help="column workload: columns per Adam step")
     ap.add_argument("--profile-case", default=None,
-                    choices=["mixed", "fp64", "uneven", "uneven-small", "enkf", "metrics"],
+                    choices=["mixed", "fp64", "uneven", "uneven-small", "enkf", "metrics", "column",
+                             "column-small"],
                     help="run a profiler case and exit: mixed/fp64 = one batched LETKF on the reduced "
                          "180x90x10x4 case (125k obs); uneven = the 512-case mixed batch run twice without "
                          "the graph; uneven-small = its first 64 cases; enkf = the mixed EnKF (2.59M values, "
-                         "k=64, 500k obs) twice; metrics = Metrics::CalculateAll of that ensemble twice")
+                         "k=64, 500k obs) twice; metrics = Metrics::CalculateAll of that ensemble twice; column = "
+                         "H(x) of 200k column obs x 64 members (720x360 columns, 30 levels), plain and "
+                         "surrogate (untrained weights), twice each; column-small = the same on 360x180 columns with "
+                         "50k obs (2 GB state)")
     return ap.parse_args()
 
 
@@ -314,6 +318,33 @@ def profile_case(precision_name: str) -> None:
             ms.append(1e3 * (time.perf_counter() - t0))
         b.close()
         print(json.dumps({"profile_case": precision_name, "cases": len(cases), "ms": ms}))
+        return
+    if precision_name.startswith("column"):
+        g = torch.Generator(device=dev)
+        g.manual_seed(7)
+        ncol, nlev, k, p = (360 * 180, 30, 64, 50_000) if precision_name == "column-small" else (720 * 360, 30, 64,
+                                                                                              200_000)
+        Tm = (255.0 + 15.0 * torch.randn((k, nlev * ncol), generator=g, device=dev, dtype=torch.float64)).clamp(200, 310)
+        lq = (np.log(2e-3) + torch.randn((k, nlev * ncol), generator=g, device=dev, dtype=torch.float64)).clamp(
+            np.log(1e-6), np.log(2e-2))
+        X = torch.cat([Tm, lq], dim=1).contiguous()
+        del Tm, lq
+        oc = torch.randint(0, ncol, (p,), generator=g, device=dev)
+        och = torch.randint(0, 16, (p,), generator=g, device=dev).to(torch.int32)
+        op = syn.column_operator()
+        w, tau = torch.tensor(op.w, device=dev), torch.tensor(op.tau, device=dev)
+        mlp = K.MLP(64, 256, 16)
+        mlp.set_params(mlp.init_params(seed=7), torch.zeros(16, device=dev), torch.ones(16, device=dev))
+        ms = {"plain": [], "surrogate": []}
+        for _ in range(2):
+            for name, fn in (("plain", lambda: K.hx_column(X, ncol, nlev, oc, och, w, tau)),
+                             ("surrogate", lambda: mlp.hx_column(X, ncol, nlev, oc, och))):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                ms[name].append(1e3 * (time.perf_counter() - t0))
+        print(json.dumps({"profile_case": precision_name, "ms": ms}))
         return
     if precision_name in ("enkf", "metrics"):
         g = torch.Generator(device=dev)

@@ -15,6 +15,8 @@
 // standardised per channel (y - out_shift)/out_scale.
 #include <cuda_bf16.h>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include <memory>
 #include <vector>
 
@@ -254,15 +256,31 @@ __global__ void column_features_kernel(const float* __restrict__ T, const float*
 // v = 0: T (K), v = 1: ln q.  One thread per (obs, member): the column of
 // member i at obs o, either labelled by the plain operator (channel obs_ch[o]
 // into HX) or turned into MLP features (row o*k + i of X).
+// Obs in column order: keys = obs_col (as 32-bit), values = obs index.
+__global__ void obs_sort_keys_kernel(const int64_t* __restrict__ obs_col, int64_t p, uint32_t* __restrict__ keys,
+                                     int32_t* __restrict__ vals) {
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p; o += (int64_t)gridDim.x * blockDim.x) {
+    keys[o] = (uint32_t)obs_col[o];
+    vals[o] = (int32_t)o;
+  }
+}
+
+// One thread per (member, obs) of a slice of p obs taken in column order
+// (perm: slice rank -> obs index): consecutive threads read the same member
+// at neighbouring columns, so a warp's loads share sectors (a thread per
+// (obs, member) in obs order read one 32-byte sector per value).  The plain
+// operator writes HX[o k + i]; the feature rows are slice-local, rank-major
+// (row r k + i).
 __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t ld, int64_t ncol, int nlev,
                                  const int64_t* __restrict__ obs_col, const int32_t* __restrict__ obs_ch,
-                                 int64_t p, const float* __restrict__ w, const float* __restrict__ tau,
-                                 double* __restrict__ HX, float* __restrict__ feat, int nin,
-                                 __nv_bfloat16* __restrict__ featb = nullptr) {
+                                 int64_t p, const int32_t* __restrict__ perm, const float* __restrict__ w,
+                                 const float* __restrict__ tau, double* __restrict__ HX, float* __restrict__ feat,
+                                 int nin, __nv_bfloat16* __restrict__ featb = nullptr) {
   const int64_t total = p * k;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t o = e / k;
-    const int i = (int)(e - o * k);
+    const int i = (int)(e / p);
+    const int64_t r = e - (int64_t)i * p;
+    const int64_t o = perm[r];
     const double* x = Xs + (int64_t)i * ld + obs_col[o];
     if (HX) {
       const int ch = obs_ch[o];
@@ -272,16 +290,26 @@ __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t l
         Q += expf((float)x[(int64_t)(nlev + l) * ncol]);
         acc += w[ch * nlev + l] * expf(-tau[ch] * Q) * ((t * t) * (t * t) / 1e8f);
       }
-      HX[e] = acc;
+      HX[o * k + i] = acc;
     } else if (featb) {
-      __nv_bfloat16* f = featb + e * nin;
-      for (int l = 0; l < nlev; ++l) {
-        f[l] = __float2bfloat16_rn(((float)x[(int64_t)l * ncol] - 255.0f) / 30.0f);
-        f[nlev + l] = __float2bfloat16_rn(100.0f * expf((float)x[(int64_t)(nlev + l) * ncol]));
+      // the row in registers, written as 16-byte chunks (nin % 8 == 0 here)
+      __nv_bfloat16* f = featb + (r * k + i) * nin;
+      for (int c0 = 0; c0 < nin; c0 += 8) {
+        __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int j = c0 + u;
+          float val = 0.0f;
+          if (j < nlev)
+            val = ((float)x[(int64_t)j * ncol] - 255.0f) / 30.0f;
+          else if (j < 2 * nlev)
+            val = 100.0f * expf((float)x[(int64_t)j * ncol]);
+          v[u] = __float2bfloat16_rn(val);
+        }
+        *reinterpret_cast<uint4*>(f + c0) = *reinterpret_cast<const uint4*>(v);
       }
-      for (int j = 2 * nlev; j < nin; ++j) f[j] = __float2bfloat16_rn(0.0f);
     } else {
-      float* f = feat + e * nin;
+      float* f = feat + (r * k + i) * nin;
       for (int l = 0; l < nlev; ++l) {
         f[l] = ((float)x[(int64_t)l * ncol] - 255.0f) / 30.0f;
         f[nlev + l] = 100.0f * expf((float)x[(int64_t)(nlev + l) * ncol]);
@@ -291,14 +319,17 @@ __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t l
   }
 }
 
-// HX[o*k + i] = Y[(o*k + i)*nout + obs_ch[o]] * scale + shift (de-standardise).
+// HX[o k + i] = Y[(r k + i) nout + obs_ch[o]] * scale + shift (de-standardise),
+// o = perm[r] for the slice's rank-major network output rows.
 __global__ void pick_channel_kernel(const float* __restrict__ Y, int64_t p, int k, int nout,
-                                    const int32_t* __restrict__ obs_ch, const float* __restrict__ shift,
-                                    const float* __restrict__ scale, double* __restrict__ HX) {
+                                    const int32_t* __restrict__ perm, const int32_t* __restrict__ obs_ch,
+                                    const float* __restrict__ shift, const float* __restrict__ scale,
+                                    double* __restrict__ HX) {
   const int64_t total = p * k;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int ch = obs_ch[e / k];
-    HX[e] = (double)(Y[e * nout + ch] * scale[ch] + shift[ch]);
+    const int64_t r = e / k, o = perm[r];
+    const int ch = obs_ch[o];
+    HX[o * k + (e - r * k)] = (double)(Y[e * nout + ch] * scale[ch] + shift[ch]);
   }
 }
 
@@ -407,6 +438,30 @@ int backward(mg_context* ctx, mg_mlp* m, const float* X, const float* Yt, int64_
   return MG_OK;
 }
 
+// perm[r] = the obs at rank r in column order (CUB radix sort on the
+// column index); tmp is column_sort_bytes(p) bytes of device workspace.
+size_t column_sort_bytes(int64_t p) {
+  size_t b = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, b, (const uint32_t*)nullptr, (uint32_t*)nullptr, (const int32_t*)nullptr,
+                                  (int32_t*)nullptr, (int)p);
+  return b + 256 + 2 * sizeof(uint32_t) * (size_t)p + sizeof(int32_t) * (size_t)p + 1024;
+}
+
+cudaError_t sort_obs_by_column(const int64_t* obs_col, int64_t p, int32_t* perm, void* tmp, cudaStream_t s) {
+  char* t = static_cast<char*>(tmp);
+  auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  uint32_t* keys = reinterpret_cast<uint32_t*>(t);
+  uint32_t* keys_out = reinterpret_cast<uint32_t*>(t + align(sizeof(uint32_t) * p));
+  int32_t* vals = reinterpret_cast<int32_t*>(t + 2 * align(sizeof(uint32_t) * p));
+  void* sort_tmp = t + 2 * align(sizeof(uint32_t) * p) + align(sizeof(int32_t) * p);
+  size_t sb = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, sb, (const uint32_t*)nullptr, (uint32_t*)nullptr, (const int32_t*)nullptr,
+                                  (int32_t*)nullptr, (int)p);
+  obs_sort_keys_kernel<<<grid_for(p), kThreads, 0, s>>>(obs_col, p, keys, vals);
+  MG_COUNT_LAUNCH();
+  return cub::DeviceRadixSort::SortPairs(sort_tmp, sb, keys, keys_out, vals, perm, (int)p, 0, 32, s);
+}
+
 }  // namespace
 
 extern "C" {
@@ -442,8 +497,18 @@ int mg_hx_column(mg_context* ctx, const double* X, int32_t k, int64_t ld, int64_
                    ld >= 2 * (int64_t)nlev * ncol,
                "mg_hx_column: bad arguments");
   if (p == 0) return MG_OK;
-  hx_column_kernel<<<grid_for(p * k), kThreads, 0, ctx->stream>>>(X, k, ld, ncol, nlev, obs_col, obs_ch, p, w, tau,
-                                                                   HX, nullptr, 0);
+  MG_CHECK_ARG(p < ((int64_t)1 << 31) && ncol < ((int64_t)1 << 32), "mg_hx_column: too many obs or columns");
+  mg::Carver cv;
+  cv.reserve<int32_t>(p);
+  cv.reserve<char>(column_sort_bytes(p));
+  void* ws = mg::workspace(ctx, cv.off);
+  if (!ws) return MG_ERR_NOMEM;
+  cv = mg::Carver{static_cast<char*>(ws), 0};
+  int32_t* perm = cv.take<int32_t>(p);
+  void* stmp = cv.take<char>(column_sort_bytes(p));
+  MG_TRY_CUDA(sort_obs_by_column(obs_col, p, perm, stmp, ctx->stream));
+  hx_column_kernel<<<grid_for(p * k), kThreads, 0, ctx->stream>>>(X, k, ld, ncol, nlev, obs_col, obs_ch, p, perm, w,
+                                                                   tau, HX, nullptr, 0);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   return MG_OK;
@@ -586,21 +651,35 @@ int mg_hx_column_mlp(mg_context* ctx, mg_mlp* m, const double* X, int32_t k, int
                    ld >= 2 * (int64_t)nlev * ncol,
                "mg_hx_column_mlp: bad arguments");
   if (p == 0) return MG_OK;
-  // Columns are run through the network in slices so activations stay bounded.
+  MG_CHECK_ARG(p < ((int64_t)1 << 31) && ncol < ((int64_t)1 << 32), "mg_hx_column_mlp: too many obs or columns");
+  // Columns are run through the network in slices so activations stay
+  // bounded; the obs are taken in column order (sorted once per call).
   const int64_t total = p * k;
   const int64_t slice = std::min<int64_t>(total, (int64_t)1 << 20);
-  if (tc_shapes_ok(m)) {
+  const bool tc = tc_shapes_ok(m);
+  mg::Carver cv;
+  cv.reserve<int32_t>(p);
+  cv.reserve<char>(column_sort_bytes(p));
+  if (!tc) cv.reserve<float>((size_t)slice * m->nin);
+  void* ws = mg::workspace(ctx, cv.off);
+  if (!ws) return MG_ERR_NOMEM;
+  cv = mg::Carver{static_cast<char*>(ws), 0};
+  int32_t* perm = cv.take<int32_t>(p);
+  void* stmp = cv.take<char>(column_sort_bytes(p));
+  float* feat = tc ? nullptr : cv.take<float>((size_t)slice * m->nin);
+  MG_TRY_CUDA(sort_obs_by_column(obs_col, p, perm, stmp, ctx->stream));
+  if (tc) {
     int rc = ensure_capacity(ctx, m, slice);
     if (rc != MG_OK || (rc = ensure_tc_capacity(ctx, m, slice)) != MG_OK) return rc;
     MG_TRY_CUDA(cudaMemsetAsync(m->tc_err, 0, sizeof(int), ctx->stream));
     for (int64_t o0 = 0; o0 < p; o0 += slice / k) {
       const int64_t np = std::min<int64_t>(p - o0, slice / k);
       hx_column_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(
-          X, k, ld, ncol, nlev, obs_col + o0, obs_ch + o0, np, nullptr, nullptr, nullptr, nullptr, m->nin, m->Xb);
+          X, k, ld, ncol, nlev, obs_col, obs_ch, np, perm + o0, nullptr, nullptr, nullptr, nullptr, m->nin, m->Xb);
       MG_COUNT_LAUNCH();
       if ((rc = forward_tc(ctx, m, np * k)) != MG_OK) return rc;
-      pick_channel_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(m->Y, np, k, m->nout, obs_ch + o0,
-                                                                          m->out_shift, m->out_scale, HX + o0 * k);
+      pick_channel_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(m->Y, np, k, m->nout, perm + o0, obs_ch,
+                                                                          m->out_shift, m->out_scale, HX);
       MG_COUNT_LAUNCH();
       MG_TRY_CUDA(cudaGetLastError());
     }
@@ -612,17 +691,15 @@ int mg_hx_column_mlp(mg_context* ctx, mg_mlp* m, const double* X, int32_t k, int
   }
   int rc = ensure_capacity(ctx, m, slice);
   if (rc != MG_OK) return rc;
-  void* ws = mg::workspace(ctx, sizeof(float) * (size_t)slice * m->nin);
-  if (!ws) return MG_ERR_NOMEM;
-  float* feat = static_cast<float*>(ws);
   for (int64_t o0 = 0; o0 < p; o0 += slice / k) {
     const int64_t np = std::min<int64_t>(p - o0, slice / k);
-    hx_column_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(X, k, ld, ncol, nlev, obs_col + o0, obs_ch + o0,
-                                                                     np, nullptr, nullptr, nullptr, feat, m->nin);
+    hx_column_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(X, k, ld, ncol, nlev, obs_col, obs_ch, np,
+                                                                     perm + o0, nullptr, nullptr, nullptr, feat,
+                                                                     m->nin);
     MG_COUNT_LAUNCH();
     if ((rc = forward(ctx, m, feat, np * k)) != MG_OK) return rc;
-    pick_channel_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(m->Y, np, k, m->nout, obs_ch + o0,
-                                                                        m->out_shift, m->out_scale, HX + o0 * k);
+    pick_channel_kernel<<<grid_for(np * k), kThreads, 0, ctx->stream>>>(m->Y, np, k, m->nout, perm + o0, obs_ch,
+                                                                        m->out_shift, m->out_scale, HX);
     MG_COUNT_LAUNCH();
     MG_TRY_CUDA(cudaGetLastError());
   }

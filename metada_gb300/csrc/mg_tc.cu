@@ -98,6 +98,10 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 }
 
 __device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
+// SiLU for BF16-only outputs (hidden activations): the hardware exp2-based
+// exponential and the approximate division, a few ulp, far below BF16's
+// 2^-8; for z < -88 the denominator is +inf and the result 0, the limit.
+__device__ __forceinline__ float silu_bf16(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -117,6 +121,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ uint64_t done_bar;            // all MMAs drained
   __shared__ uint32_t tmem_base_s;
   __shared__ int failed;
+  __shared__ float sbias[BN];  // bias (0 past N or without one)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kBM;
   const int nk = (K + kBK - 1) / kBK;
@@ -130,6 +135,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  for (int n = threadIdx.x; n < BN; n += kThreads) sbias[n] = (bias && n < N) ? bias[n] : 0.0f;
   if (warp == 0) {  // TMEM: BN FP32 columns x 128 lanes
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
                  "r"(kTmemCols));
@@ -200,8 +206,43 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int rbase = m0 + warp * 32;
     const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
     const bool pairs16 = C16 && (ldc % 2 == 0) && (((uintptr_t)C16 & 3) == 0);
+    // BF16-only output with 16-byte aligned rows: each lane packs its row's
+    // 32 columns and stores them directly (no staging).
+    const bool direct16 = C16 && !C32 && (ldc % 8 == 0) && (((uintptr_t)C16 & 15) == 0);
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 32) {
+      if (direct16 && c0 + 32 <= N) {
+        uint32_t v[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+              "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+              "=r"(v[30]), "=r"(v[31])
+            : "r"(trow + (uint32_t)c0));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        uint32_t pk[16];
+#pragma unroll
+        for (int j = 0; j < 32; j += 2) {
+          float x0 = __uint_as_float(v[j]) + sbias[c0 + j];
+          float x1 = __uint_as_float(v[j + 1]) + sbias[c0 + j + 1];
+          if (act) {
+            x0 = silu_bf16(x0);
+            x1 = silu_bf16(x1);
+          }
+          const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+          pk[j / 2] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+        const int row = rbase + lane;
+        if (row < M) {
+          uint4* dst = reinterpret_cast<uint4*>(C16 + (int64_t)row * ldc + c0);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) dst[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+        }
+        continue;
+      }
       uint32_t v[32];
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -216,8 +257,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int n = c0 + j;
-        float x = __uint_as_float(v[j]) + ((bias && n < N) ? bias[n] : 0.0f);
-        if (act) x = silu_f(x);
+        float x = __uint_as_float(v[j]) + sbias[n];
+        if (act) x = C32 ? silu_f(x) : silu_bf16(x);
         stg[lane * 33 + j] = x;
       }
       __syncwarp();
