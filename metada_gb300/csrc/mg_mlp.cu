@@ -269,8 +269,8 @@ __global__ void obs_sort_keys_kernel(const int64_t* __restrict__ obs_col, int64_
 // (perm: slice rank -> obs index): consecutive threads read the same member
 // at neighbouring columns, so a warp's loads share sectors (a thread per
 // (obs, member) in obs order read one 32-byte sector per value).  The plain
-// operator writes HX[o k + i]; the feature rows are slice-local, rank-major
-// (row r k + i).
+// operator writes HX[o k + i]; the feature rows are slice-local in thread
+// order (row i p + r), so a warp writes neighbouring rows.
 __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t ld, int64_t ncol, int nlev,
                                  const int64_t* __restrict__ obs_col, const int32_t* __restrict__ obs_ch,
                                  int64_t p, const int32_t* __restrict__ perm, const float* __restrict__ w,
@@ -293,7 +293,7 @@ __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t l
       HX[o * k + i] = acc;
     } else if (featb) {
       // the row in registers, written as 16-byte chunks (nin % 8 == 0 here)
-      __nv_bfloat16* f = featb + (r * k + i) * nin;
+      __nv_bfloat16* f = featb + e * nin;
       for (int c0 = 0; c0 < nin; c0 += 8) {
         __align__(16) __nv_bfloat16 v[8];
 #pragma unroll
@@ -309,7 +309,7 @@ __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t l
         *reinterpret_cast<uint4*>(f + c0) = *reinterpret_cast<const uint4*>(v);
       }
     } else {
-      float* f = feat + (r * k + i) * nin;
+      float* f = feat + e * nin;
       for (int l = 0; l < nlev; ++l) {
         f[l] = ((float)x[(int64_t)l * ncol] - 255.0f) / 30.0f;
         f[nlev + l] = 100.0f * expf((float)x[(int64_t)(nlev + l) * ncol]);
@@ -319,17 +319,17 @@ __global__ void hx_column_kernel(const double* __restrict__ Xs, int k, int64_t l
   }
 }
 
-// HX[o k + i] = Y[(r k + i) nout + obs_ch[o]] * scale + shift (de-standardise),
-// o = perm[r] for the slice's rank-major network output rows.
+// HX[o k + i] = Y[(i p + r) nout + obs_ch[o]] * scale + shift (de-standardise),
+// o = perm[r], for the slice's network output rows (feature row order).
 __global__ void pick_channel_kernel(const float* __restrict__ Y, int64_t p, int k, int nout,
                                     const int32_t* __restrict__ perm, const int32_t* __restrict__ obs_ch,
                                     const float* __restrict__ shift, const float* __restrict__ scale,
                                     double* __restrict__ HX) {
   const int64_t total = p * k;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = e / k, o = perm[r];
+    const int64_t i = e / p, r = e - i * p, o = perm[r];
     const int ch = obs_ch[o];
-    HX[o * k + (e - r * k)] = (double)(Y[e * nout + ch] * scale[ch] + shift[ch]);
+    HX[o * k + i] = (double)(Y[e * nout + ch] * scale[ch] + shift[ch]);
   }
 }
 
