@@ -299,6 +299,15 @@ int mg_hx_column_mlp(mg_context* ctx, mg_mlp* mlp, const double* X, int32_t k, i
 int mg_gemm_bf16_tc(mg_context* ctx, const void* A, const void* B, int32_t M, int32_t N, int32_t K,
                     const float* bias, int32_t silu, float* C);
 
+/* Self-test of the kernel's bounded waits: the same GEMM with one k-block
+ * of every CTA's first tile never loaded, so a wait runs out (after about a
+ * second) and the kernel returns instead of hanging.  *observed receives the
+ * status the launch reports (MG_ERR_TIMEOUT when the waits work); returns
+ * MG_OK when the kernel came back.  C is scratch.  No counterpart in the
+ * reference. */
+int mg_gemm_bf16_tc_wait_selftest(mg_context* ctx, const void* A, const void* B, int32_t M, int32_t N,
+                                  int32_t K, float* C, int32_t* observed);
+
 /* Text I/O of the analysis path on the device (text and output buffers
  * on the host; parsed arrays on the device).
  *

@@ -174,6 +174,7 @@ _SIGNATURES = {
     "mg_ens_metrics": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p,
                        POINTER(EnsMetrics)],
     "mg_gemm_bf16_tc": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_int32, c_void_p],
+    "mg_gemm_bf16_tc_wait_selftest": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p],
     "mg_etkf_noalloc": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
                         c_double, c_int32, c_int32, c_void_p],
 }

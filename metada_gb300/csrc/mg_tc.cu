@@ -33,7 +33,7 @@ constexpr int kThreads = 64 + 32 * kEpiWarps;  // TMA warp, MMA warp, epilogue w
 // Shared-memory ring of A and B k-blocks (the widest tile keeps three so the
 // ring and the epilogue staging fit in 227 KB).
 __host__ __device__ constexpr int ring_stages(int bn) { return bn >= 256 ? 3 : 4; }
-constexpr unsigned kSpinLimit = 1u << 26;
+constexpr uint64_t kWaitNs = 1000000000ull;  // one wait gives up after 1 s (a legitimate one takes microseconds)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -47,39 +47,44 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
-// Bounded wait for the given phase parity; false if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  const uint32_t addr = smem_u32(bar);
-  for (unsigned it = 0; it < kSpinLimit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
 
-// Bounded wait that also gives up once another role has raised *abort.
+__device__ __forceinline__ bool mbar_test(uint32_t addr, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Wait for the given phase parity, bounded by elapsed time (kWaitNs, checked
+// every 64 polls; try_wait itself may suspend for a hardware-defined time, so
+// a poll count would not bound the wall time) and, for mbar_wait_ab, by
+// another role raising *abort.  False if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  const uint64_t t0 = global_ns();
+  for (unsigned it = 1;; ++it) {
+    if (mbar_test(addr, parity)) return true;
+    if ((it & 63u) == 0u && global_ns() - t0 > kWaitNs) return false;
+  }
+}
+
 __device__ __forceinline__ bool mbar_wait_ab(uint64_t* bar, uint32_t parity, volatile int* abort) {
   const uint32_t addr = smem_u32(bar);
-  for (unsigned it = 0; it < kSpinLimit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((it & 1023u) == 1023u && *abort) return false;
+  const uint64_t t0 = global_ns();
+  for (unsigned it = 1;; ++it) {
+    if (mbar_test(addr, parity)) return true;
+    if ((it & 63u) == 0u && (*abort || global_ns() - t0 > kWaitNs)) return false;
   }
-  return false;
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -143,7 +148,9 @@ template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int M,
                    int N, int K, const float* __restrict__ bias, int act, float* __restrict__ C32,
-                   __nv_bfloat16* __restrict__ C16, int ldc, int* __restrict__ err) {
+                   __nv_bfloat16* __restrict__ C16, int ldc, int* __restrict__ err, int skip_kb) {
+  // skip_kb >= 0 (the wait self-test only): the producer never issues that
+  // k-block of the CTA's first tile, so the MMA warp's wait for it runs out.
   static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "N tile");
   constexpr int kStages = ring_stages(BN);
   constexpr uint32_t kABytes = kBM * kBK * 2, kBBytes = BN * kBK * 2, kStageBytes = kABytes + kBBytes;
@@ -195,6 +202,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     if (lane == 0) {  // TMA producer
       uint32_t g = 0;  // k-blocks issued
+      uint32_t skipped = 0xffffffffu;
       bool ok = true;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
         const int m0 = t * kBM;
@@ -204,6 +212,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (!mbar_wait_ab(&empty_bar[s], ph ^ 1u, abort)) {
             ok = false;
             break;
+          }
+          if (t == (int)blockIdx.x && kb == skip_kb) {
+            skipped = g++;
+            continue;
           }
           mbar_expect_tx(&full_bar[s], kStageBytes);
           tma_load_2d(sA + s * kABytes, &mapA, &full_bar[s], kb * kBK, m0);
@@ -218,7 +230,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       // Copies into this CTA's shared memory must land before it exits: wait
       // (bounded) for the last issue of every stage.
       for (uint32_t j = g > (uint32_t)kStages ? g - kStages : 0u; j < g; ++j)
-        mbar_wait(&full_bar[j % kStages], (j / kStages) & 1u);
+        if (j != skipped) mbar_wait(&full_bar[j % kStages], (j / kStages) & 1u);
     }
   } else if (warp == 1) {
     if (lane == 0) {  // MMA issuer
@@ -408,13 +420,14 @@ bool make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t cols, int
 
 template <int BN>
 int launch(mg_context* ctx, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int K, const float* bias,
-           int act, float* C32, __nv_bfloat16* C16, int ldc, int* err) {
+           int act, float* C32, __nv_bfloat16* C16, int ldc, int* err, int skip_kb) {
   const size_t smem =
       1024 + (size_t)ring_stages(BN) * (kBM * kBK * 2 + BN * kBK * 2) + sizeof(float) * kEpiWarps * 32 * 33;
   MG_TRY_CUDA(cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int tiles = (M + kBM - 1) / kBM;
   const int grid = std::max(1, std::min(tiles, ctx->num_sms));
-  tc_gemm_kernel<BN><<<(unsigned)grid, kThreads, smem, ctx->stream>>>(ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
+  tc_gemm_kernel<BN><<<(unsigned)grid, kThreads, smem, ctx->stream>>>(ma, mb, M, N, K, bias, act, C32, C16, ldc, err,
+                                                                      skip_kb);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   return MG_OK;
@@ -425,8 +438,8 @@ int launch(mg_context* ctx, const CUtensorMap& ma, const CUtensorMap& mb, int M,
 namespace mg {
 
 // Internal entry used by the MLP inference path as well.
-int tc_gemm_bf16(mg_context* ctx, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K,
-                 const float* bias, int act, float* C32, __nv_bfloat16* C16, int ldc, int* err) {
+int tc_gemm_run(mg_context* ctx, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K,
+                const float* bias, int act, float* C32, __nv_bfloat16* C16, int ldc, int* err, int skip_kb) {
   if (N < 1 || N > 256 || K % 8 != 0 || M <= 0 || K <= 0)
     return fail(ctx, MG_ERR_ARG, "tensor-core GEMM: need 1 <= N <= 256, K > 0, K % 8 == 0");
   if (((uintptr_t)A | (uintptr_t)B) & 15)
@@ -436,12 +449,17 @@ int tc_gemm_bf16(mg_context* ctx, const __nv_bfloat16* A, const __nv_bfloat16* B
   if (!make_map(&ma, A, M, K, kBM) || !make_map(&mb, B, N, K, bn))
     return fail(ctx, MG_ERR_CUDA, "tensor-core GEMM: cuTensorMapEncodeTiled failed");
   switch (bn) {
-    case 16: return launch<16>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
-    case 32: return launch<32>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
-    case 64: return launch<64>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
-    case 128: return launch<128>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
-    default: return launch<256>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err);
+    case 16: return launch<16>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err, skip_kb);
+    case 32: return launch<32>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err, skip_kb);
+    case 64: return launch<64>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err, skip_kb);
+    case 128: return launch<128>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err, skip_kb);
+    default: return launch<256>(ctx, ma, mb, M, N, K, bias, act, C32, C16, ldc, err, skip_kb);
   }
+}
+
+int tc_gemm_bf16(mg_context* ctx, const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K,
+                 const float* bias, int act, float* C32, __nv_bfloat16* C16, int ldc, int* err) {
+  return tc_gemm_run(ctx, A, B, M, N, K, bias, act, C32, C16, ldc, err, -1);
 }
 
 }  // namespace mg
@@ -460,5 +478,27 @@ extern "C" int mg_gemm_bf16_tc(mg_context* ctx, const void* A, const void* B, in
   MG_TRY_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   MG_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
   if (h) return mg::fail(ctx, MG_ERR_TIMEOUT, "mg_gemm_bf16_tc: a bounded mbarrier wait gave up");
+  return MG_OK;
+}
+
+// Self-test of the bounded waits: the same GEMM with one k-block of every
+// CTA's first tile never loaded, so the MMA warp's wait for it gives up
+// after its time limit and the others follow the abort.  *observed is the
+// status the launch reports (MG_ERR_TIMEOUT when the waits work); the call
+// returns MG_OK when the kernel came back and the context is usable.
+extern "C" int mg_gemm_bf16_tc_wait_selftest(mg_context* ctx, const void* A, const void* B, int32_t M, int32_t N,
+                                             int32_t K, float* C, int32_t* observed) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(A && B && C && observed, "mg_gemm_bf16_tc_wait_selftest: null argument");
+  int* err = static_cast<int*>(mg::workspace(ctx, 256));
+  if (!err) return MG_ERR_NOMEM;
+  MG_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  const int rc = mg::tc_gemm_run(ctx, static_cast<const __nv_bfloat16*>(A), static_cast<const __nv_bfloat16*>(B), M,
+                                 N, K, nullptr, 0, C, nullptr, N, err, 0);
+  if (rc != MG_OK) return rc;
+  int h = 0;
+  MG_TRY_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MG_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
+  *observed = h ? MG_ERR_TIMEOUT : MG_OK;
   return MG_OK;
 }

@@ -373,6 +373,19 @@ def gemm_bf16_tc(A: torch.Tensor, B: torch.Tensor, bias: torch.Tensor | None = N
     return C
 
 
+def gemm_bf16_tc_wait_selftest(A: torch.Tensor, B: torch.Tensor) -> int:
+    """Runs the tensor-core GEMM with one k-block never loaded; returns the
+    status its bounded waits report (MG_ERR_TIMEOUT when they work)."""
+    _need(A, torch.bfloat16, "A")
+    _need(B, torch.bfloat16, "B")
+    M, K = A.shape
+    N = B.shape[0]
+    C = torch.empty((M, N), dtype=torch.float32, device=A.device)
+    obs = ctypes.c_int32(-1)
+    context(A.device.index).call("mg_gemm_bf16_tc_wait_selftest", _ptr(A), _ptr(B), M, N, K, _ptr(C), byref(obs))
+    return obs.value
+
+
 # ----------------------------------------------------- column operator ----
 def column_op(T: torch.Tensor, q: torch.Tensor, w: torch.Tensor, tau: torch.Tensor) -> torch.Tensor:
     """Plain column operator: T, q (ncol x nlev float32) -> y (ncol x nch)."""

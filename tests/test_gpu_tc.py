@@ -83,3 +83,17 @@ def test_surrogate_tensor_core_path_matches_simt_forward(dev):
     # BF16 rounding of the features and hidden activations (2^-9 relative).
     assert rel_err(HX, want) <= 1e-2
     assert np.isfinite(HX).all()
+
+
+def test_tc_gemm_bounded_wait_gives_up_and_context_stays_usable(dev):
+    """A wait that can never complete (one k-block never loaded) runs out and
+    the kernel returns MG_ERR_TIMEOUT instead of hanging; the next GEMM on
+    the same context is correct."""
+    from metada_gb300 import _lib
+
+    g = torch.Generator().manual_seed(11)
+    A = torch.randn(2048, 128, generator=g).to(torch.bfloat16).to(dev)
+    B = torch.randn(256, 128, generator=g).to(torch.bfloat16).to(dev)
+    assert K.gemm_bf16_tc_wait_selftest(A, B) == _lib.MG_ERR_TIMEOUT
+    C = K.gemm_bf16_tc(A, B).cpu().numpy()
+    assert rel_err(C, _ref(A, B, None, False)) <= 1e-5
