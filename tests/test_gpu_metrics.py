@@ -29,7 +29,7 @@ def test_metrics_known_answers(dev):
     assert abs(u["correlation"] - 0.34105511573854358) <= 1e-6
 
 
-@pytest.mark.parametrize("n,k", [(1, 2), (31, 3), (100_003, 64), (20_000, 100)])
+@pytest.mark.parametrize("n,k", [(1, 2), (31, 3), (100_003, 64), (20_000, 100), (7_001, 200)])
 def test_metrics_match_oracle(dev, n, k):
     g = np.random.default_rng(n + k)
     truth = g.standard_normal(n) * 3.0 + 1.0
@@ -51,3 +51,20 @@ def test_metrics_python_mirror(dev):
     r = A.Metrics.CalculateAll(ens, METRICS_TRUTH, state_dim=4, ens_size=3)
     assert abs(r["crps"] - 0.022222222222222227) <= 1e-6
     np.testing.assert_allclose(r["spread"], 0.1, atol=1e-6)
+
+
+def test_metrics_ties_and_shared_key_halves(dev):
+    """Members on a coarse grid (many exact ties) and members a few ulp
+    apart (same top 32 bits of the order key): the CRPS ranks take the exact
+    recount, and the result still matches the pairwise sum."""
+    g = np.random.default_rng(3)
+    n, k = 4_099, 48
+    truth = g.standard_normal(n)
+    X = np.round(truth[None] + g.standard_normal((k, n)), 1)
+    X[5:9] = X[4] + np.arange(1, 5)[:, None] * np.spacing(X[4])  # a few ulp above member 4
+    mean, spread, m = _gpu(X, truth, dev)
+    wmean, wspread, wm = ob.ens_metrics(X, truth)
+    assert np.array_equal(mean.cpu().numpy(), wmean)
+    assert np.array_equal(spread.cpu().numpy(), wspread)
+    for key in ("rmse", "bias", "crps", "avg_spread"):
+        assert abs(m[key] - wm[key]) <= 1e-12 * max(1.0, abs(wm[key])), key
