@@ -9,7 +9,7 @@
 // band bound plus a longitude bound from the haversine inequality
 // a >= cos(lat_c) cos(lat_o) sin^2(dlon/2)); the reachable cells of one
 // latitude band are one or two contiguous runs of the cell-sorted obs, which
-// the whole CTA sweeps.  The test on a candidate is the squared chord
+// the whole CTA sweeps after one warp has planned them (a lane per band).  The test on a candidate is the squared chord
 // |u_c - u_o|^2 between unit vectors (u_o stored with the hash), compared
 // with the chord of the radius: haversine <= r  <=>  chord^2 <= 4 sin^2(r/2R),
 // with an absolute error near 1e-16 against a band of 2e-9 relative in
@@ -107,9 +107,12 @@ struct CellObs {
   double* uz;
 };
 
+// Obs into their cells (positions from the cell starts), with unit vectors
+// both cell-sorted and in obs order (the latter for the list distances).
 __global__ void cell_scatter_kernel(const double* __restrict__ lat, const double* __restrict__ lon,
                                     int64_t p, const int64_t* __restrict__ start,
-                                    unsigned long long* __restrict__ cursor, CellObs co) {
+                                    unsigned long long* __restrict__ cursor, CellObs co, double* __restrict__ oux,
+                                    double* __restrict__ ouy, double* __restrict__ ouz) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p; o += stride) {
     const int c = cell_of(lat[o], lon[o]);
@@ -121,30 +124,54 @@ __global__ void cell_scatter_kernel(const double* __restrict__ lat, const double
     co.ux[pos] = u.x;
     co.uy[pos] = u.y;
     co.uz[pos] = u.z;
+    oux[o] = u.x;
+    ouy[o] = u.y;
+    ouz[o] = u.z;
   }
 }
 
-// Visits every candidate obs of column (la, lo) with the whole CTA and calls
-// f(t, cls) for the candidates at cell-sorted position t with cls = +1
-// (inside) or 0 (within 1e-9 relative of the radius).
-template <typename F>
-__device__ void visit_candidates(double la, double lo, double radius_km, const int64_t* __restrict__ start,
-                                 const CellObs& co, F&& f) {
+// Search plan of one column in shared memory, made by warp 0: the chord
+// thresholds, the column's unit vector, and per reachable latitude band the
+// one or two contiguous runs of cell-sorted obs its longitude window covers
+// (slots 2 b and 2 b + 1, the second empty where one run suffices).  The
+// FP64 transcendentals run once per band on one lane, not on every thread
+// of the CTA (GB300's FP64 pipe does about 2 operations per clock per SM).
+constexpr int kMaxRuns = 2 * kNBand;
+
+struct ColPlan {
+  double la, lo, rlo, rhi, c2lo, c2hi, ux, uy, uz;
+  int chord, nrun;
+};
+
+__device__ void plan_column(double la, double lo, double radius_km, const int64_t* __restrict__ start,
+                            ColPlan& pl, int64_t* run_lo, int64_t* run_hi) {
+  const int lane = threadIdx.x & 31;
   const double theta = radius_km / kEarthKm;  // radians
   const double theta_deg = theta * 180.0 / kPi;
-  const double sh = sin(0.5 * theta);
-  const double a_r = sh * sh;
-  const bool chord = radius_km >= 50.0;
-  const double rlo = radius_km * (1.0 - kBorderRel), rhi = radius_km * (1.0 + kBorderRel);
-  const double slo = sin(0.5 * rlo / kEarthKm), shi = sin(0.5 * rhi / kEarthKm);
-  const double c2lo = 4.0 * slo * slo, c2hi = 4.0 * shi * shi;
-  const double3 uc = unit_vec(la, lo);
   int b0 = (int)floor(la + 90.0 - theta_deg - 1e-6);
   int b1 = (int)floor(la + 90.0 + theta_deg + 1e-6);
   b0 = b0 < 0 ? 0 : b0;
   b1 = b1 >= kNBand ? kNBand - 1 : b1;
+  if (lane == 0) {
+    const double rlo = radius_km * (1.0 - kBorderRel), rhi = radius_km * (1.0 + kBorderRel);
+    const double slo = sin(0.5 * rlo / kEarthKm), shi = sin(0.5 * rhi / kEarthKm);
+    const double3 uc = unit_vec(la, lo);
+    pl.la = la;
+    pl.lo = lo;
+    pl.rlo = rlo;
+    pl.rhi = rhi;
+    pl.c2lo = 4.0 * slo * slo;
+    pl.c2hi = 4.0 * shi * shi;
+    pl.ux = uc.x;
+    pl.uy = uc.y;
+    pl.uz = uc.z;
+    pl.chord = radius_km >= 50.0;
+    pl.nrun = 2 * (b1 - b0 + 1);
+  }
+  const double sh = sin(0.5 * theta);
+  const double a_r = sh * sh;
   const double cosc = cos(la * kPi / 180.0);
-  for (int band = b0; band <= b1; ++band) {
+  for (int band = b0 + lane; band <= b1; band += 32) {
     const double e0 = (double)band - 90.0, e1 = e0 + 1.0;
     const double emax = fmax(fabs(e0), fabs(e1));
     const double cmin = cos(emax * kPi / 180.0);
@@ -161,40 +188,48 @@ __device__ void visit_candidates(double la, double lo, double radius_km, const i
       }
     }
     // The cells c0..c1 (mod 360) as at most two contiguous runs of obs.
-    int64_t run_lo[2], run_hi[2];
-    int nrun = 0;
-    const int bb = band * kNLonCell;
+    const int bb = band * kNLonCell, slot = 2 * (band - b0);
+    run_lo[slot + 1] = run_hi[slot + 1] = 0;
     if (c1 - c0 + 1 >= kNLonCell) {
-      run_lo[0] = start[bb];
-      run_hi[0] = start[bb + kNLonCell];
-      nrun = 1;
+      run_lo[slot] = start[bb];
+      run_hi[slot] = start[bb + kNLonCell];
     } else {
       const int a0 = ((c0 % kNLonCell) + kNLonCell) % kNLonCell;
       const int a1 = ((c1 % kNLonCell) + kNLonCell) % kNLonCell;
       if (a0 <= a1) {
-        run_lo[0] = start[bb + a0];
-        run_hi[0] = start[bb + a1 + 1];
-        nrun = 1;
+        run_lo[slot] = start[bb + a0];
+        run_hi[slot] = start[bb + a1 + 1];
       } else {
-        run_lo[0] = start[bb + a0];
-        run_hi[0] = start[bb + kNLonCell];
-        run_lo[1] = start[bb];
-        run_hi[1] = start[bb + a1 + 1];
-        nrun = 2;
+        run_lo[slot] = start[bb + a0];
+        run_hi[slot] = start[bb + kNLonCell];
+        run_lo[slot + 1] = start[bb];
+        run_hi[slot + 1] = start[bb + a1 + 1];
       }
     }
-    for (int rr = 0; rr < nrun; ++rr) {
-      for (int64_t t = run_lo[rr] + threadIdx.x; t < run_hi[rr]; t += blockDim.x) {
-        if (chord) {
-          const double dx = co.ux[t] - uc.x, dy = co.uy[t] - uc.y, dz = co.uz[t] - uc.z;
-          const double c2 = dx * dx + dy * dy + dz * dz;
-          if (c2 <= c2lo) f(t, 1);
-          else if (c2 <= c2hi) f(t, 0);
-        } else {
-          const double d = haversine_dev(la, lo, co.lat[t], co.lon[t]);
-          if (d <= rlo) f(t, 1);
-          else if (d <= rhi) f(t, 0);
-        }
+  }
+}
+
+// Visits every candidate obs of a planned column with the whole CTA and
+// calls f(t, cls) for the candidates at cell-sorted position t with
+// cls = +1 (inside) or 0 (within 1e-9 relative of the radius).
+template <typename F>
+__device__ void visit_candidates(const ColPlan& pl, const int64_t* run_lo, const int64_t* run_hi,
+                                 const CellObs& co, F&& f) {
+  const int nrun = pl.nrun;
+  const bool chord = pl.chord;
+  const double ux = pl.ux, uy = pl.uy, uz = pl.uz, c2lo = pl.c2lo, c2hi = pl.c2hi;
+  for (int r = 0; r < nrun; ++r) {
+    const int64_t hi = run_hi[r];
+    for (int64_t t = run_lo[r] + threadIdx.x; t < hi; t += blockDim.x) {
+      if (chord) {
+        const double dx = co.ux[t] - ux, dy = co.uy[t] - uy, dz = co.uz[t] - uz;
+        const double c2 = dx * dx + dy * dy + dz * dz;
+        if (c2 <= c2lo) f(t, 1);
+        else if (c2 <= c2hi) f(t, 0);
+      } else {
+        const double d = haversine_dev(pl.la, pl.lo, co.lat[t], co.lon[t]);
+        if (d <= pl.rlo) f(t, 1);
+        else if (d <= pl.rhi) f(t, 0);
       }
     }
   }
@@ -215,12 +250,15 @@ __global__ void __launch_bounds__(256) geo_count_kernel(
     double radius_km, const int64_t* __restrict__ start, CellObs co, int64_t* __restrict__ counts,
     BorderRec* __restrict__ border, unsigned long long* __restrict__ nborder) {
   __shared__ unsigned long long scount;
+  __shared__ ColPlan pl;
+  __shared__ int64_t run_lo[kMaxRuns], run_hi[kMaxRuns];
   const int64_t col = blockIdx.x;
   if (threadIdx.x == 0) scount = 0;
-  __syncthreads();
   const double la = col_lat[col], lo = col_lon[col];
+  if (threadIdx.x < 32) plan_column(la, lo, radius_km, start, pl, run_lo, run_hi);
+  __syncthreads();
   unsigned long long mine = 0;
-  visit_candidates(la, lo, radius_km, start, co, [&](int64_t t, int cls) {
+  visit_candidates(pl, run_lo, run_hi, co, [&](int64_t t, int cls) {
     ++mine;
     if (cls == 0) {
       const unsigned long long slot = atomicAdd(nborder, 1ull);
@@ -244,10 +282,13 @@ __global__ void __launch_bounds__(256) geo_fill_kernel(
     const double* __restrict__ col_lat, const double* __restrict__ col_lon, int64_t ncol,
     double radius_km, const int64_t* __restrict__ start, CellObs co,
     const int64_t* __restrict__ offsets, const unsigned long long* __restrict__ rej, int nrej,
-    const double* __restrict__ obs_lat, const double* __restrict__ obs_lon,
-    int32_t* __restrict__ idx, double* __restrict__ dist, int* __restrict__ overflow) {
+    const double* __restrict__ obs_lat, const double* __restrict__ obs_lon, const double* __restrict__ oux,
+    const double* __restrict__ ouy, const double* __restrict__ ouz, int32_t* __restrict__ idx,
+    double* __restrict__ dist, int* __restrict__ overflow) {
   extern __shared__ int32_t slist[];  // capacity: next power of two >= kMaxList
   __shared__ int scount;
+  __shared__ ColPlan pl;
+  __shared__ int64_t run_lo[kMaxRuns], run_hi[kMaxRuns];
   const int64_t col = blockIdx.x;
   const int64_t base = offsets[col];
   const int64_t n = offsets[col + 1] - base;
@@ -257,9 +298,10 @@ __global__ void __launch_bounds__(256) geo_fill_kernel(
     return;
   }
   if (threadIdx.x == 0) scount = 0;
-  __syncthreads();
   const double la = col_lat[col], lo = col_lon[col];
-  visit_candidates(la, lo, radius_km, start, co, [&](int64_t t, int cls) {
+  if (threadIdx.x < 32) plan_column(la, lo, radius_km, start, pl, run_lo, run_hi);
+  __syncthreads();
+  visit_candidates(pl, run_lo, run_hi, co, [&](int64_t t, int cls) {
     const int32_t o = co.obs[t];
     if (cls == 0 && nrej > 0 && key_rejected(rej, nrej, ((unsigned long long)col << 32) | (unsigned)o)) return;
     const int pos = atomicAdd(&scount, 1);
@@ -291,15 +333,13 @@ __global__ void __launch_bounds__(256) geo_fill_kernel(
       __syncthreads();
     }
   }
-  const double3 uc = unit_vec(la, lo);
-  const bool chord = radius_km >= 50.0;
+  const bool chord = pl.chord;
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     const int o = slist[t];
     idx[base + t] = o;
     if (dist) {
       if (chord) {  // d = 2R asin(chord / 2): well conditioned for chords up to the radius
-        const double3 u = unit_vec(obs_lat[o], obs_lon[o]);
-        const double dx = u.x - uc.x, dy = u.y - uc.y, dz = u.z - uc.z;
+        const double dx = oux[o] - pl.ux, dy = ouy[o] - pl.uy, dz = ouz[o] - pl.uz;
         const double h = 0.5 * sqrt(dx * dx + dy * dy + dz * dz);
         dist[base + t] = 2.0 * kEarthKm * asin(h < 1.0 ? h : 1.0);
       } else {
@@ -377,7 +417,7 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
   cv.reserve<unsigned long long>(kNCell + 1);
   cv.reserve<int64_t>(kNCell + 1);             // cell start
   cv.reserve<int32_t>(p + 1);
-  for (int a = 0; a < 5; ++a) cv.reserve<double>(p + 1);  // lat, lon, unit vector
+  for (int a = 0; a < 8; ++a) cv.reserve<double>(p + 1);  // lat, lon, unit vector; unit vector in obs order
   cv.reserve<int64_t>(ncol + 1);               // column counts
   cv.reserve<BorderRec>(kBorderCap);
   cv.reserve<unsigned long long>(kBorderCap);  // rejected keys
@@ -397,6 +437,9 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
   co.ux = cv.take<double>(p + 1);
   co.uy = cv.take<double>(p + 1);
   co.uz = cv.take<double>(p + 1);
+  double* oux = cv.take<double>(p + 1);
+  double* ouy = cv.take<double>(p + 1);
+  double* ouz = cv.take<double>(p + 1);
   auto* counts = cv.take<int64_t>(ncol + 1);
   auto* border = cv.take<BorderRec>(kBorderCap);
   auto* rej = cv.take<unsigned long long>(kBorderCap);
@@ -418,7 +461,7 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
     MG_TRY_CUDA(cudaGetLastError());
     MG_TRY_CUDA(mg::exclusive_scan(reinterpret_cast<const int64_t*>(ccount), cstart, kNCell, tmp,
                                    tmpb, s));
-    cell_scatter_kernel<<<gb, 256, 0, s>>>(obs_lat, obs_lon, p, cstart, ccursor, co);
+    cell_scatter_kernel<<<gb, 256, 0, s>>>(obs_lat, obs_lon, p, cstart, ccursor, co, oux, ouy, ouz);
     MG_COUNT_LAUNCH();
     MG_TRY_CUDA(cudaGetLastError());
   } else {
@@ -465,7 +508,7 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
   MG_TRY_CUDA(cudaFuncSetAttribute(geo_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
   geo_fill_kernel<<<(unsigned)ncol, 256, smem, s>>>(col_lat, col_lon, ncol, radius_km, cstart, co, offsets, rej,
-                                                    nrej, obs_lat, obs_lon, idx, dist_km, overflow);
+                                                    nrej, obs_lat, obs_lon, oux, ouy, ouz, idx, dist_km, overflow);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   int ovf = 0;
