@@ -31,9 +31,13 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kNVarMax = 8;
 // Off-diagonal threshold of the loose first Jacobi stage (relative to
-// sqrt(a_pp a_qq)); the first-order finish below leaves a remainder of
-// about k * kStage1Tol^2.
-constexpr double kStage1Tol = 3e-4;
+// sqrt(a_pp a_qq)); the second-order finish below leaves a remainder of
+// order k^2 kStage1Tol^3.
+constexpr double kStage1Tol = 1e-3;
+
+// a / b by the hardware reciprocal for FP32 (a few ulp), exact for FP64.
+__device__ __forceinline__ float fast_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
 
 struct LetkfParams {
   int k, kp, n_var, nlev;
@@ -381,13 +385,19 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
       __syncthreads();
       // Stage 3: A2 = D + E is nearly diagonal (|E_ij| <= kStage1Tol
       // sqrt(d_i d_j) after stage 1, V1 orthonormal to FP32 rounding), so
-      // f(A2) for f = x^-1/2 and x^-1 is taken to first order by the
-      // Daleckii-Krein formula,
-      //   f(D + E) = f(D) + [E_ij f[d_i, d_j]] + O(|E|^2),
-      // with the divided differences in closed form (no cancellation):
-      //   x^-1/2: -1 / (s_i s_j (s_i + s_j)), s = sqrt(d);  x^-1: -1 / (d_i d_j).
-      // The second-order remainder is ~k kStage1Tol^2 relative (a few 1e-6
-      // at k = 64), and no tight Jacobi is needed.
+      // f(A2) for f = x^-1/2 and x^-1 is taken to second order by the
+      // Daleckii-Krein expansion
+      //   f(D + E)_ij = f(d_i) delta_ij + f[d_i, d_j] E_ij
+      //                 + sum_m f[d_i, d_m, d_j] E_im E_mj + O(|E|^3),
+      // with the divided differences in closed form (no cancellation),
+      // s = sqrt(d):
+      //   x^-1/2: f[a,b] = -1 / (s_a s_b (s_a + s_b)),
+      //           f[a,b,c] = (s_a + s_b + s_c) / (s_a s_b s_c (s_a + s_b) (s_b + s_c) (s_a + s_c));
+      //   x^-1:   f[a,b] = -1 / (a b),  f[a,b,c] = 1 / (a b c).
+      // For x^-1/2 the second-order sum splits by partial fractions into
+      //   h_ij S_ij,  h_ij = 1 / (s_i s_j (s_i + s_j)),
+      //   S_ij = sum_m [P_im E_mj + E_im P_mj] / s_m - P_im P_mj,  P_im = E_im / (s_i + s_m),
+      // two k^3 products, run register-tiled (no eigen-sweep barriers).
       for (int i = tid; i < k; i += kThreads) {
         const TE l = A[i * LDA + i];
         lam[i] = l;
@@ -396,18 +406,32 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
       __syncthreads();
       have_basis = true;
       const TE sc = infl_compat ? (TE)prm.rho : TE(1);
+      TE* gvec = rot;        // k values; the Jacobi rotation buffer is free now
+      TE* sv = rot + KMAX;   // s = sqrt(d)
+      TE* yv = Bc;           // D^-1 u; the rebuild buffer is free now
+      TE* zv = Bc + KMAX;    // z = E D^-1 u
+      TE* zq = Bc + 2 * KMAX;  // D^-1 z
       for (int i = tid; i < k; i += kThreads) {  // u = V1^T b
         TE s = TE(0);
         for (int j = 0; j < k; ++j) s += V[j * LDA + i] * bvec[j];
         uvec[i] = s;
+        yv[i] = s / lam[i];
+        sv[i] = mg::dsqrt<TE>(lam[i]);
       }
       __syncthreads();
-      TE* gvec = rot;  // k values; the Jacobi rotation buffer is free now
-      for (int i = tid; i < k; i += kThreads) {  // g = (sc x^-1)(A2) u
-        TE s = uvec[i];
+      for (int i = tid; i < k; i += kThreads) {
+        TE z = TE(0);
         for (int j = 0; j < k; ++j)
-          if (j != i) s -= A[i * LDA + j] * (uvec[j] / lam[j]);
-        gvec[i] = s * sc / lam[i];
+          if (j != i) z += A[i * LDA + j] * yv[j];
+        zv[i] = z;
+        zq[i] = z / lam[i];
+      }
+      __syncthreads();
+      for (int i = tid; i < k; i += kThreads) {  // g = (sc x^-1)(A2) u = sc D^-1 (u - z + E D^-1 z)
+        TE w = TE(0);
+        for (int m = 0; m < k; ++m)
+          if (m != i) w += A[i * LDA + m] * zq[m];
+        gvec[i] = (uvec[i] - zv[i] + w) * sc / lam[i];
       }
       __syncthreads();
       for (int i = tid; i < k; i += kThreads) {  // wa = V1 g
@@ -415,18 +439,55 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
         for (int m = 0; m < k; ++m) s += V[i * LDA + m] * gvec[m];
         wa[i] = s;
       }
-      // A <- Wb = (c x^-1/2)(A2), c = sqrt((k-1) sc); W = V1 Wb V1^T is never
-      // formed: the update applies X' V1, then Wb, then V1^T.
-      const TE cw = mg::dsqrt<TE>(TE(k - 1) * sc);
-      for (int e = tid; e < k * k; e += kThreads) {
-        const int i = e / k, j = e - i * k;
-        const TE si = mg::dsqrt<TE>(lam[i]);
-        if (i == j) {
-          A[i * LDA + i] = cw / si;
-        } else {
-          const TE sj = mg::dsqrt<TE>(lam[j]);
-          A[i * LDA + j] = -cw * A[i * LDA + j] / (si * sj * (si + sj));
+      {
+        // S (second-order sum) for the thread's R x R block: rows
+        // i = ti + 16 a, columns j = tj + 16 b, as the Gram tiles.
+#pragma unroll
+        for (int a = 0; a < R; ++a)
+#pragma unroll
+          for (int b = 0; b < R; ++b) acc[a][b] = TE(0);
+        TE si_[R], sj_[R];
+#pragma unroll
+        for (int a = 0; a < R; ++a) {
+          const int i = ti + 16 * a, j = tj + 16 * a;
+          si_[a] = i < k ? sv[i] : TE(1);
+          sj_[a] = j < k ? sv[j] : TE(1);
         }
+        // (approximate divisions: these scale a correction of order
+        // kStage1Tol^2, a few ulp of it is far below the result's rounding)
+        for (int m = 0; m < k; ++m) {
+          const TE sm = sv[m], ism = fast_div(TE(1), sm);
+          TE emj[R], pmj[R];
+#pragma unroll
+          for (int b = 0; b < R; ++b) {
+            const int j = tj + 16 * b;
+            emj[b] = (j < k && j != m) ? A[m * LDA + j] : TE(0);
+            pmj[b] = fast_div(emj[b], sm + sj_[b]);
+          }
+#pragma unroll
+          for (int a = 0; a < R; ++a) {
+            const int i = ti + 16 * a;
+            const TE eim = (i < k && i != m) ? A[i * LDA + m] : TE(0);
+            const TE pim = fast_div(eim, si_[a] + sm);
+#pragma unroll
+            for (int b = 0; b < R; ++b) acc[a][b] += (pim * emj[b] + eim * pmj[b]) * ism - pim * pmj[b];
+          }
+        }
+        __syncthreads();  // every read of E done
+        // A <- Wb = (c x^-1/2)(A2), c = sqrt((k-1) sc); W = V1 Wb V1^T is
+        // never formed: the update applies X' V1, then Wb, then V1^T.
+        const TE cw = mg::dsqrt<TE>(TE(k - 1) * sc);
+#pragma unroll
+        for (int a = 0; a < R; ++a)
+#pragma unroll
+          for (int b = 0; b < R; ++b) {
+            const int i = ti + 16 * a, j = tj + 16 * b;
+            if (i < k && j < k) {
+              const TE h = TE(1) / (si_[a] * sj_[b] * (si_[a] + sj_[b]));
+              const TE first = (i == j) ? TE(1) / si_[a] : -A[i * LDA + j] * h;
+              A[i * LDA + j] = cw * (first + acc[a][b] * h);
+            }
+          }
       }
       __syncthreads();
       if (upd_compat) {  // row sums of W = V1 Wb V1^T 1, kept in uvec
