@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(kThreads) metrics_elem_kernel(const double* __
       }
     } else if (t >= 1) {
       // Warp 0: mean, spread and the sums of tile t - 1, a lane per element
-      // (an FP64 instruction costs the pipe the same for 1 active lane or 32).
+      // (every FP64 warp instruction carries 32 lanes of work).
       const int tp = t - 1, b = tp % 3, cnt = tile_cnt(tp);
       const double* xs = xs_all + b * tile_vals;
       if (lane < cnt) {
