@@ -6,7 +6,8 @@
 //
 // The text is copied to the device once; lines are indexed in parallel
 // (per-4 KB chunk counts, a scan, then the line starts), and every line is
-// scanned by one thread with the extraction rules of std::istream:
+// scanned with the extraction rules of std::istream (one thread per line, or
+// for long lines of values one warp per line, below):
 //   * int: skip white space, optional sign, at least one digit;
 //   * double: skip white space, [sign] (digits [. digits] | . digits)
 //     [(e|E) [sign] digits]; no inf/nan/hex (libstdc++ rejects them);
@@ -103,11 +104,11 @@ __device__ bool extract_int(const char* t, int64_t& pos, int64_t end, int& out) 
   return true;
 }
 
-__device__ __forceinline__ double pow10_exact(int e) {  // 10^e, 0 <= e <= 22, exact in binary64
-  const double p[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
-                        1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
-  return p[e];
-}
+// 10^e, 0 <= e <= 22, exact in binary64 (a global table: a local one would
+// be rebuilt on the thread's stack at every call).
+__device__ const double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                                      1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+__device__ __forceinline__ double pow10_exact(int e) { return kPow10[e]; }
 
 // Returns 1 on success, 0 on a failed extraction, 2 if the number is valid
 // but outside the exact fast path (the host converts it).
@@ -193,7 +194,8 @@ struct ObsLines {
 };
 
 __global__ void obs_lines_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
-                                 int64_t L, ObsLines ol, unsigned long long* __restrict__ first_header) {
+                                 int64_t L, ObsLines ol, unsigned long long* __restrict__ first_header,
+                                 int32_t* __restrict__ nhost) {
   const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (l >= L) return;
   const int64_t s = starts[l];
@@ -228,6 +230,7 @@ __global__ void obs_lines_kernel(const char* __restrict__ t, int64_t n, const in
         if (r == 2) host = 1;
       }
       ty = !ok ? kBad : (host ? kHost : kData);
+      if (ty == kHost) atomicAdd(nhost, 1);
       if (ty == kData) {
         for (int f = 0; f < 4; ++f) {
           ol.ival[l * 4 + f] = iv[f];
@@ -266,35 +269,158 @@ __global__ void obs_write_kernel(const ObsLines ol, int64_t L, const int64_t* __
 }
 
 // ---- SimpleState values: per line, doubles until the first failed extraction ----
-__global__ void values_count_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
-                                    int64_t L, int64_t* __restrict__ counts, int32_t* __restrict__ host) {
-  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= L) return;
-  const int64_t s = starts[l];
-  const int64_t e = (l + 1 < L) ? starts[l + 1] - 1 : ((n > 0 && t[n - 1] == '\n') ? n - 1 : n);
+// Per-line mode after the count pass: 0 = read on the device token-parallel
+// (or by the thread-per-line kernels), 1 = read on the host (a number outside
+// the fast path), 2 = read on the device by the sequential extraction loop.
+enum ValueMode : int32_t { kValFast = 0, kValHost = 1, kValSeq = 2 };
+
+__device__ __forceinline__ void line_span(const char* t, int64_t n, const int64_t* starts, int64_t L, int64_t l,
+                                          int64_t& s, int64_t& e) {
+  s = starts[l];
+  e = (l + 1 < L) ? starts[l + 1] - 1 : ((n > 0 && t[n - 1] == '\n') ? n - 1 : n);
+}
+
+// The extraction loop of one line: count, whether a number needs the host,
+// and (with out) the values.
+__device__ int64_t line_values_seq(const char* t, int64_t s, int64_t e, int& h, double* out) {
   int64_t pos = s, c = 0;
-  int h = 0;
+  h = 0;
   double v;
   for (;;) {
     const int r = extract_double(t, pos, e, v);
     if (r == 0) break;
     if (r == 2) h = 1;
+    if (out && !h) out[c] = v;
     ++c;
   }
-  counts[l] = c;
-  host[l] = h;
+  return c;
+}
+
+// Thread per line (short lines).
+__global__ void values_count_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
+                                    int64_t L, int64_t* __restrict__ counts, int32_t* __restrict__ mode,
+                                    int32_t* __restrict__ nhost) {
+  const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= L) return;
+  int64_t s, e;
+  line_span(t, n, starts, L, l, s, e);
+  int h;
+  counts[l] = line_values_seq(t, s, e, h, nullptr);
+  mode[l] = h ? kValHost : kValFast;
+  if (h) atomicAdd(nhost, 1);
 }
 
 __global__ void values_write_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
-                                    int64_t L, const int64_t* __restrict__ offs, const int32_t* __restrict__ host,
+                                    int64_t L, const int64_t* __restrict__ offs, const int32_t* __restrict__ mode,
                                     double* __restrict__ out) {
   const int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= L || host[l]) return;
-  const int64_t s = starts[l];
-  const int64_t e = (l + 1 < L) ? starts[l + 1] - 1 : ((n > 0 && t[n - 1] == '\n') ? n - 1 : n);
-  int64_t pos = s, o = offs[l];
-  double v;
-  while (extract_double(t, pos, e, v) == 1) out[o++] = v;
+  if (l >= L || mode[l] == kValHost) return;
+  int64_t s, e;
+  line_span(t, n, starts, L, l, s, e);
+  int h;
+  line_values_seq(t, s, e, h, out + offs[l]);
+}
+
+// Warp per line (long lines).  A line whose white-space separated tokens are
+// each one number that extract_double consumes whole is "regular": for it
+// the extraction sequence is the token sequence (each extraction skips white
+// space to the next token start and ends at the token's end; after the last
+// token it meets only white space and fails), so the tokens can be read in
+// parallel.  Each 512-byte round of the line gives lane i the token starts in
+// bytes [16 i, 16 i + 16); a warp prefix sum of the lanes' token counts
+// places the values.  Other lines go to the sequential loop (lane 0).
+constexpr int kWin = 16;
+constexpr int kRound = 32 * kWin;
+constexpr int64_t kWarpLineBytes = 256;  // mean line length from which a warp reads each line
+
+__device__ __forceinline__ bool token_start(const char* t, int64_t s, int64_t p) {
+  return !is_ws(t[p]) && (p == s || is_ws(t[p - 1]));
+}
+
+__global__ void values_count_warp_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
+                                         int64_t L, int64_t* __restrict__ counts, int32_t* __restrict__ mode,
+                                         int32_t* __restrict__ nhost) {
+  const int64_t l = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one line per warp
+  const int lane = threadIdx.x & 31;
+  if (l >= L) return;
+  int64_t s, e;
+  line_span(t, n, starts, L, l, s, e);
+  int c = 0;
+  bool bad = false, host = false;
+  for (int64_t base = s; base < e; base += kRound) {
+    const int64_t w0 = base + (int64_t)lane * kWin;
+    const int64_t w1 = w0 + kWin < e ? w0 + kWin : e;
+    for (int64_t p = w0; p < w1; ++p) {
+      if (!token_start(t, s, p)) continue;
+      int64_t pos = p;
+      double v;
+      const int r = extract_double(t, pos, e, v);
+      if (r != 0 && (pos == e || is_ws(t[pos]))) {
+        ++c;
+        host |= (r == 2);
+      } else {
+        bad = true;
+      }
+    }
+  }
+  bad = __any_sync(0xffffffffu, bad);
+  host = __any_sync(0xffffffffu, host);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+  if (lane != 0) return;
+  int32_t m;
+  int64_t cnt = c;
+  if (bad) {
+    int h;
+    cnt = line_values_seq(t, s, e, h, nullptr);
+    m = h ? kValHost : kValSeq;
+  } else {
+    m = host ? kValHost : kValFast;
+  }
+  counts[l] = cnt;
+  mode[l] = m;
+  if (m == kValHost) atomicAdd(nhost, 1);
+}
+
+__global__ void values_write_warp_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
+                                         int64_t L, const int64_t* __restrict__ offs,
+                                         const int32_t* __restrict__ mode, double* __restrict__ out) {
+  const int64_t l = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (l >= L) return;
+  const int32_t m = mode[l];
+  if (m == kValHost) return;
+  int64_t s, e;
+  line_span(t, n, starts, L, l, s, e);
+  int64_t o = offs[l];
+  if (m == kValSeq) {
+    if (lane == 0) {
+      int h;
+      line_values_seq(t, s, e, h, out + o);
+    }
+    return;
+  }
+  for (int64_t base = s; base < e; base += kRound) {
+    const int64_t w0 = base + (int64_t)lane * kWin;
+    const int64_t w1 = w0 + kWin < e ? w0 + kWin : e;
+    int cnt = 0;
+    for (int64_t p = w0; p < w1; ++p) cnt += token_start(t, s, p) ? 1 : 0;
+    int inc = cnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc += y;
+    }
+    int64_t slot = o + inc - cnt;
+    for (int64_t p = w0; p < w1; ++p) {
+      if (!token_start(t, s, p)) continue;
+      int64_t pos = p;
+      double v;
+      extract_double(t, pos, e, v);
+      out[slot++] = v;
+    }
+    o += __shfl_sync(0xffffffffu, inc, 31);
+  }
 }
 
 // ---- "%12.6f" writer ----
@@ -355,12 +481,13 @@ __device__ int format_f6(double v, char* buf) {
 }
 
 __global__ void fmt_len_kernel(const double* __restrict__ v, int64_t count, int32_t nx, int64_t* __restrict__ len,
-                               int32_t* __restrict__ host) {
+                               int32_t* __restrict__ host, int32_t* __restrict__ nhost) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   char buf[40];
   const int n = format_f6(v[i], buf);
   host[i] = n < 0 ? 1 : 0;
+  if (n < 0) atomicAdd(nhost, 1);
   const int w = n < 0 ? 0 : (n < 12 ? 12 : n);
   len[i] = w + 1;  // the separator: " " inside a row, "\n" at its end
 }
@@ -416,11 +543,21 @@ int with_lines(mg_context* ctx, const char* text, int64_t nbytes, F&& body) {
   return rc;
 }
 
-// The lines a host istringstream must read (numbers outside the fast path).
-std::vector<int64_t> host_lines(mg_context* ctx, const int32_t* flags, int64_t L, int32_t want, int* rc) {
-  std::vector<int32_t> h(L);
+// The lines a host istringstream must read (numbers outside the fast path);
+// nflag is the device count of them, so the flags are copied only when some
+// are set.
+std::vector<int64_t> host_lines(mg_context* ctx, const int32_t* flags, int64_t L, int32_t want, const int32_t* nflag,
+                                int* rc) {
   *rc = MG_OK;
   if (L == 0) return {};
+  int32_t nf = 0;
+  if (cudaMemcpyAsync(&nf, nflag, sizeof(nf), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+    *rc = mg::fail(ctx, MG_ERR_CUDA, "text I/O: device copy failed");
+    return {};
+  }
+  if (nf == 0) return {};
+  std::vector<int32_t> h(L);
   if (cudaMemcpyAsync(h.data(), flags, sizeof(int32_t) * L, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
       cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
     *rc = mg::fail(ctx, MG_ERR_CUDA, "text I/O: device copy failed");
@@ -453,6 +590,7 @@ int mg_parse_grid_obs(mg_context* ctx, const char* text, int64_t nbytes, double 
   return with_lines(ctx, text, nbytes, [&](const char* t, int64_t L, int64_t* starts) -> int {
     ObsLines ol{};
     unsigned long long* marks = nullptr;  // first header, first separator after it
+    int32_t* nhost = nullptr;
     int64_t *keep = nullptr, *pos = nullptr;
     void* tmp = nullptr;
     const size_t tmpb = mg::scan_temp_bytes(L);
@@ -460,6 +598,7 @@ int mg_parse_grid_obs(mg_context* ctx, const char* text, int64_t nbytes, double 
     MG_TRY_CUDA(cudaMallocAsync(&ol.ival, sizeof(int32_t) * 4 * L, s));
     MG_TRY_CUDA(cudaMallocAsync(&ol.dval, sizeof(double) * 4 * L, s));
     MG_TRY_CUDA(cudaMallocAsync(&marks, sizeof(unsigned long long) * 2, s));
+    MG_TRY_CUDA(cudaMallocAsync(&nhost, sizeof(int32_t), s));
     MG_TRY_CUDA(cudaMallocAsync(&keep, sizeof(int64_t) * (L + 1), s));
     MG_TRY_CUDA(cudaMallocAsync(&pos, sizeof(int64_t) * (L + 1), s));
     MG_TRY_CUDA(cudaMallocAsync(&tmp, tmpb, s));
@@ -468,13 +607,15 @@ int mg_parse_grid_obs(mg_context* ctx, const char* text, int64_t nbytes, double 
       cudaFreeAsync(ol.ival, s);
       cudaFreeAsync(ol.dval, s);
       cudaFreeAsync(marks, s);
+      cudaFreeAsync(nhost, s);
       cudaFreeAsync(keep, s);
       cudaFreeAsync(pos, s);
       cudaFreeAsync(tmp, s);
     };
     MG_TRY_CUDA(cudaMemsetAsync(marks, 0xff, sizeof(unsigned long long) * 2, s));
+    MG_TRY_CUDA(cudaMemsetAsync(nhost, 0, sizeof(int32_t), s));
     const unsigned g = (unsigned)((L + kThreads - 1) / kThreads);
-    obs_lines_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, ol, marks);
+    obs_lines_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, ol, marks, nhost);
     MG_COUNT_LAUNCH();
     obs_sep_kernel<<<g, kThreads, 0, s>>>(ol.type, L, marks, marks + 1);
     MG_COUNT_LAUNCH();
@@ -482,7 +623,7 @@ int mg_parse_grid_obs(mg_context* ctx, const char* text, int64_t nbytes, double 
     // Lines with numbers outside the fast path: the reference's own
     // extraction on the host.
     int rc = MG_OK;
-    const std::vector<int64_t> hl = host_lines(ctx, ol.type, L, kHost, &rc);
+    const std::vector<int64_t> hl = host_lines(ctx, ol.type, L, kHost, nhost, &rc);
     if (rc != MG_OK) return release(), rc;
     if (!hl.empty()) {
       std::vector<int64_t> hs(L);
@@ -533,25 +674,34 @@ int mg_parse_values(mg_context* ctx, const char* text, int64_t nbytes, double* o
   cudaStream_t s = ctx->stream;
   return with_lines(ctx, text, nbytes, [&](const char* t, int64_t L, int64_t* starts) -> int {
     int64_t *counts = nullptr, *offs = nullptr;
-    int32_t* host = nullptr;
+    int32_t *mode = nullptr, *nhost = nullptr;
     void* tmp = nullptr;
     const size_t tmpb = mg::scan_temp_bytes(L);
     MG_TRY_CUDA(cudaMallocAsync(&counts, sizeof(int64_t) * (L + 1), s));
     MG_TRY_CUDA(cudaMallocAsync(&offs, sizeof(int64_t) * (L + 1), s));
-    MG_TRY_CUDA(cudaMallocAsync(&host, sizeof(int32_t) * L, s));
+    MG_TRY_CUDA(cudaMallocAsync(&mode, sizeof(int32_t) * L, s));
+    MG_TRY_CUDA(cudaMallocAsync(&nhost, sizeof(int32_t), s));
     MG_TRY_CUDA(cudaMallocAsync(&tmp, tmpb, s));
     auto release = [&]() {
       cudaFreeAsync(counts, s);
       cudaFreeAsync(offs, s);
-      cudaFreeAsync(host, s);
+      cudaFreeAsync(mode, s);
+      cudaFreeAsync(nhost, s);
       cudaFreeAsync(tmp, s);
     };
+    MG_TRY_CUDA(cudaMemsetAsync(nhost, 0, sizeof(int32_t), s));
+    // Long lines (a state row per line): a warp per line; short ones: a thread.
+    const bool by_warp = nbytes >= kWarpLineBytes * L;
     const unsigned g = (unsigned)((L + kThreads - 1) / kThreads);
-    values_count_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, counts, host);
+    const unsigned gw = (unsigned)((32 * L + kThreads - 1) / kThreads);
+    if (by_warp)
+      values_count_warp_kernel<<<gw, kThreads, 0, s>>>(t, nbytes, starts, L, counts, mode, nhost);
+    else
+      values_count_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, counts, mode, nhost);
     MG_COUNT_LAUNCH();
     MG_TRY_CUDA(cudaGetLastError());
     int rc = MG_OK;
-    const std::vector<int64_t> hl = host_lines(ctx, host, L, 1, &rc);
+    const std::vector<int64_t> hl = host_lines(ctx, mode, L, kValHost, nhost, &rc);
     if (rc != MG_OK) return release(), rc;
     std::vector<int64_t> hs;
     std::vector<std::vector<double>> hv(hl.size());
@@ -578,7 +728,10 @@ int mg_parse_values(mg_context* ctx, const char* text, int64_t nbytes, double* o
       return mg::fail(ctx, MG_ERR_CAPACITY, "mg_parse_values: output array too small");
     }
     if (total > 0) {
-      values_write_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, offs, host, out);
+      if (by_warp)
+        values_write_warp_kernel<<<gw, kThreads, 0, s>>>(t, nbytes, starts, L, offs, mode, out);
+      else
+        values_write_kernel<<<g, kThreads, 0, s>>>(t, nbytes, starts, L, offs, mode, out);
       MG_COUNT_LAUNCH();
       MG_TRY_CUDA(cudaGetLastError());
       for (size_t q = 0; q < hl.size(); ++q) {
@@ -603,25 +756,28 @@ int mg_format_state(mg_context* ctx, const double* values, int32_t nx, int32_t n
   const int64_t count = (int64_t)nx * ny;
   const size_t tmpb = mg::scan_temp_bytes(count);
   int64_t *len = nullptr, *off = nullptr;
-  int32_t* host = nullptr;
+  int32_t *host = nullptr, *nhost = nullptr;
   void* tmp = nullptr;
   MG_TRY_CUDA(cudaMallocAsync(&len, sizeof(int64_t) * (count + 1), s));
   MG_TRY_CUDA(cudaMallocAsync(&off, sizeof(int64_t) * (count + 1), s));
   MG_TRY_CUDA(cudaMallocAsync(&host, sizeof(int32_t) * count, s));
+  MG_TRY_CUDA(cudaMallocAsync(&nhost, sizeof(int32_t), s));
   MG_TRY_CUDA(cudaMallocAsync(&tmp, tmpb, s));
   auto release = [&]() {
     cudaFreeAsync(len, s);
     cudaFreeAsync(off, s);
     cudaFreeAsync(host, s);
+    cudaFreeAsync(nhost, s);
     cudaFreeAsync(tmp, s);
   };
+  MG_TRY_CUDA(cudaMemsetAsync(nhost, 0, sizeof(int32_t), s));
   const unsigned g = (unsigned)((count + kThreads - 1) / kThreads);
-  fmt_len_kernel<<<g, kThreads, 0, s>>>(values, count, nx, len, host);
+  fmt_len_kernel<<<g, kThreads, 0, s>>>(values, count, nx, len, host, nhost);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   // Values the device does not format: their text length comes from the host.
   int rc = MG_OK;
-  const std::vector<int64_t> hl = host_lines(ctx, host, count, 1, &rc);
+  const std::vector<int64_t> hl = host_lines(ctx, host, count, 1, nhost, &rc);
   if (rc != MG_OK) return release(), rc;
   std::vector<std::string> htxt(hl.size());
   for (size_t q = 0; q < hl.size(); ++q) {

@@ -104,15 +104,17 @@ __global__ void __launch_bounds__(kThreads) node_box_kernel(const double* __rest
   }
 }
 
+// One warp per quantity: lanes stride over the partials, then a shuffle
+// tree (the sum is of small integer counts, exact in any order).
 __global__ void node_box_final_kernel(const double* __restrict__ part, int nb, double* __restrict__ out) {
-  const int q = threadIdx.x;
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (q >= 5) return;
-  double r = part[q];
-  for (int b = 1; b < nb; ++b) {
-    const double x = part[(int64_t)b * 5 + q];
-    r = (q == 0 || q == 2) ? fmin(r, x) : (q == 4 ? r + x : fmax(r, x));
-  }
-  out[q] = r;
+  auto op = [q](double a, double b) { return (q == 0 || q == 2) ? fmin(a, b) : (q == 4 ? a + b : fmax(a, b)); };
+  double r = (q == 0 || q == 2) ? INFINITY : (q == 4 ? 0.0 : -INFINITY);
+  for (int b = lane; b < nb; b += 32) r = op(r, part[(int64_t)b * 5 + q]);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) r = op(r, __shfl_xor_sync(0xffffffffu, r, off));
+  if (lane == 0) out[q] = r;
 }
 
 __device__ __forceinline__ double node_dist(double lat, double lon, double glat, double glon) {
@@ -205,7 +207,7 @@ extern "C" int mg_nearest_node(mg_context* ctx, const double* node_lat, const do
     double* dbox = part + 5 * (size_t)nbox;
     node_box_kernel<<<nbox, kThreads, 0, s>>>(node_lat, node_lon, nn, part);
     MG_COUNT_LAUNCH();
-    node_box_final_kernel<<<1, 32, 0, s>>>(part, nbox, dbox);
+    node_box_final_kernel<<<1, 5 * 32, 0, s>>>(part, nbox, dbox);
     MG_COUNT_LAUNCH();
     MG_TRY_CUDA(cudaGetLastError());
     MG_TRY_CUDA(cudaMemcpyAsync(box, dbox, sizeof(box), cudaMemcpyDeviceToHost, s));

@@ -62,34 +62,57 @@ def ens_mean_pert(X: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
     return mean, Xp
 
 
+# Outputs sized by an upper bound up to this many bytes take one call; larger
+# ones are sized by a counting call first.
+_ONE_CALL_BYTES = 1 << 30
+
+
+def _trim(t: torch.Tensor, n: int) -> torch.Tensor:
+    """The first n rows, in their own allocation when the bound was loose."""
+    return t[:n].clone() if 2 * n < t.shape[0] else t[:n]
+
+
 def parse_grid_obs(text: bytes, missing_value: float = -999.0,
                    device: int = 0) -> tuple[torch.Tensor, torch.Tensor]:
     """GridObservation text -> (xyz int32 p x 3: x, y, z; vals float64 p x 4:
     znu, xlong_u, xlat_u, value) on the device."""
     ctx = context(device)
-    count = c_int64(0)
-    rc = ctx.lib.mg_parse_grid_obs(ctx.handle, text, len(text), float(missing_value), c_void_p(0), c_void_p(0), 0,
-                                   byref(count))
-    if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
-        ctx.check(rc)
     dev = torch.device("cuda", device)
-    xyz = torch.empty((max(count.value, 1), 3), dtype=torch.int32, device=dev)
-    vals = torch.empty((max(count.value, 1), 4), dtype=torch.float64, device=dev)
-    ctx.call("mg_parse_grid_obs", text, len(text), float(missing_value), _ptr(xyz), _ptr(vals), count.value,
-             byref(count))
-    return xyz[: count.value], vals[: count.value]
+    count = c_int64(0)
+    # A data line holds 8 numbers with a non-digit between each two: at least
+    # 15 characters and its newline.
+    bound = (len(text) + 1) // 16 + 1
+    cap = bound if 44 * bound <= _ONE_CALL_BYTES else 0
+    xyz = torch.empty((max(cap, 1), 3), dtype=torch.int32, device=dev)
+    vals = torch.empty((max(cap, 1), 4), dtype=torch.float64, device=dev)
+    rc = ctx.lib.mg_parse_grid_obs(ctx.handle, text, len(text), float(missing_value), _ptr(xyz), _ptr(vals), cap,
+                                   byref(count))
+    if rc == _lib.MG_ERR_CAPACITY:
+        xyz = torch.empty((max(count.value, 1), 3), dtype=torch.int32, device=dev)
+        vals = torch.empty((max(count.value, 1), 4), dtype=torch.float64, device=dev)
+        ctx.call("mg_parse_grid_obs", text, len(text), float(missing_value), _ptr(xyz), _ptr(vals), count.value,
+                 byref(count))
+    else:
+        ctx.check(rc)
+    return _trim(xyz, count.value), _trim(vals, count.value)
 
 
 def parse_values(text: bytes, device: int = 0) -> torch.Tensor:
     """SimpleState text -> its values (float64) on the device."""
     ctx = context(device)
+    dev = torch.device("cuda", device)
     count = c_int64(0)
-    rc = ctx.lib.mg_parse_values(ctx.handle, text, len(text), c_void_p(0), 0, byref(count))
-    if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
+    # Two extracted values need a non-digit between their digits.
+    bound = (len(text) + 1) // 2
+    cap = bound if 8 * bound <= _ONE_CALL_BYTES else 0
+    out = torch.empty(max(cap, 1), dtype=torch.float64, device=dev)
+    rc = ctx.lib.mg_parse_values(ctx.handle, text, len(text), _ptr(out), cap, byref(count))
+    if rc == _lib.MG_ERR_CAPACITY:
+        out = torch.empty(max(count.value, 1), dtype=torch.float64, device=dev)
+        ctx.call("mg_parse_values", text, len(text), _ptr(out), count.value, byref(count))
+    else:
         ctx.check(rc)
-    out = torch.empty(max(count.value, 1), dtype=torch.float64, device=torch.device("cuda", device))
-    ctx.call("mg_parse_values", text, len(text), _ptr(out), count.value, byref(count))
-    return out[: count.value]
+    return _trim(out, count.value)
 
 
 def format_state(values: torch.Tensor, nx: int, ny: int) -> bytes:
@@ -97,12 +120,18 @@ def format_state(values: torch.Tensor, nx: int, ny: int) -> bytes:
     _need(values, torch.float64, "values")
     ctx = context(values.device.index)
     nbytes = c_int64(0)
-    rc = ctx.lib.mg_format_state(ctx.handle, _ptr(values), nx, ny, c_void_p(0), 0, byref(nbytes))
-    if rc not in (_lib.MG_OK, _lib.MG_ERR_CAPACITY):
+    # A value the device formats (|v| < 2^53) takes at most 24 characters and
+    # its separator; others are formatted on the host and may need a second
+    # call.  The text lands in pinned memory (the host allocator reuses it).
+    cap = 25 * nx * ny + 1
+    buf = torch.empty(cap, dtype=torch.uint8, pin_memory=True)
+    rc = ctx.lib.mg_format_state(ctx.handle, _ptr(values), nx, ny, c_void_p(buf.data_ptr()), cap, byref(nbytes))
+    if rc == _lib.MG_ERR_CAPACITY:
+        buf = torch.empty(max(nbytes.value, 1), dtype=torch.uint8, pin_memory=True)
+        ctx.call("mg_format_state", _ptr(values), nx, ny, c_void_p(buf.data_ptr()), nbytes.value, byref(nbytes))
+    else:
         ctx.check(rc)
-    buf = ctypes.create_string_buffer(max(nbytes.value, 1))
-    ctx.call("mg_format_state", _ptr(values), nx, ny, buf, nbytes.value, byref(nbytes))
-    return buf.raw[: nbytes.value]
+    return buf[: nbytes.value].numpy().tobytes()
 
 
 def nearest_node(node_lat: torch.Tensor, node_lon: torch.Tensor, nx: int, ny: int, obs_lat: torch.Tensor,

@@ -117,6 +117,36 @@ def test_state_round_trip(dev, nx, ny):
     assert np.array_equal(back, ob.parse_values(text))  # the reference's own extraction loop
 
 
+def test_parse_values_long_lines_every_line_mode(dev):
+    # Lines of hundreds of values (one warp per line): regular lines, lines
+    # whose tokens are not whole numbers ("1.5-2.5", "1.5.5": read by the
+    # sequential loop), a failed extraction mid-line, a number for the host,
+    # CRLF endings, tabs and runs of blanks.
+    g = np.random.default_rng(7)
+
+    def vals(n):
+        return ["%.6f" % x for x in g.standard_normal(n) * 100.0]
+
+    lines = [
+        "  " + " ".join(vals(400)) + "   ",
+        " ".join(vals(300) + ["1.5-2.5"] + vals(200)),
+        " ".join(vals(250) + ["abc"] + vals(100)),
+        " ".join(vals(300) + ["12.000000000000000000001"] + vals(50)),
+        "\t".join(vals(300)) + "\r",
+        "  ".join(vals(100) + ["1e5", "-.5", "+3.", "5E-3", "1.5.5", "-0.0"] + vals(100)),
+        " ".join(vals(600) + ["1e"]),
+        " ".join(vals(200) + ["7.5e+"] + vals(20)),
+        "",
+        "42",
+    ]
+    text = ("\n".join(lines) + "\n").encode()
+    assert len(text) >= 256 * len(lines)
+    got = K.parse_values(text).cpu().numpy()
+    want = ob.parse_values(text)
+    assert got.shape == want.shape and np.array_equal(got, want)
+    assert np.array_equal(np.signbit(got), np.signbit(want))
+
+
 def test_parse_values_stops_a_line_at_the_first_failed_extraction(dev):
     text = b"1.5 2.5 x 3.5\n  4 5e1\n\n-0.25 .75 7.\n1 2 3 4 5 6 7 8 9 10 11 12.000000000000000000001\n"
     got = K.parse_values(text).cpu().numpy()
