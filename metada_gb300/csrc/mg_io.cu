@@ -327,14 +327,29 @@ __global__ void values_write_kernel(const char* __restrict__ t, int64_t n, const
 // space to the next token start and ends at the token's end; after the last
 // token it meets only white space and fails), so the tokens can be read in
 // parallel.  Each 512-byte round of the line gives lane i the token starts in
-// bytes [16 i, 16 i + 16); a warp prefix sum of the lanes' token counts
-// places the values.  Other lines go to the sequential loop (lane 0).
+// bytes [16 i, 16 i + 16) as a bit mask, and the lanes then walk their set
+// bits together, so that the warp runs one parse per token rank of the round
+// instead of one per byte offset at which some lane meets a token; a warp
+// prefix sum of the lanes' token counts places the values.  Other lines go
+// to the sequential loop (lane 0).
 constexpr int kWin = 16;
 constexpr int kRound = 32 * kWin;
 constexpr int64_t kWarpLineBytes = 256;  // mean line length from which a warp reads each line
 
-__device__ __forceinline__ bool token_start(const char* t, int64_t s, int64_t p) {
-  return !is_ws(t[p]) && (p == s || is_ws(t[p - 1]));
+// Bit j set: a token (a non-blank byte after a blank or at the line start)
+// starts at w0 + j, for w0 + j < w1 <= w0 + kWin.
+__device__ __forceinline__ unsigned token_mask(const char* t, int64_t s, int64_t w0, int64_t w1) {
+  unsigned m = 0;
+  bool prev_ws = w0 == s || (w0 < w1 && is_ws(t[w0 - 1]));
+#pragma unroll
+  for (int j = 0; j < kWin; ++j) {
+    if (w0 + j < w1) {
+      const bool ws = is_ws(t[w0 + j]);
+      m |= (!ws && prev_ws) ? (1u << j) : 0u;
+      prev_ws = ws;
+    }
+  }
+  return m;
 }
 
 __global__ void values_count_warp_kernel(const char* __restrict__ t, int64_t n, const int64_t* __restrict__ starts,
@@ -350,8 +365,8 @@ __global__ void values_count_warp_kernel(const char* __restrict__ t, int64_t n, 
   for (int64_t base = s; base < e; base += kRound) {
     const int64_t w0 = base + (int64_t)lane * kWin;
     const int64_t w1 = w0 + kWin < e ? w0 + kWin : e;
-    for (int64_t p = w0; p < w1; ++p) {
-      if (!token_start(t, s, p)) continue;
+    for (unsigned m = token_mask(t, s, w0, w1); m; m &= m - 1) {
+      const int64_t p = w0 + (__ffs(m) - 1);
       int64_t pos = p;
       double v;
       const int r = extract_double(t, pos, e, v);
@@ -403,8 +418,8 @@ __global__ void values_write_warp_kernel(const char* __restrict__ t, int64_t n, 
   for (int64_t base = s; base < e; base += kRound) {
     const int64_t w0 = base + (int64_t)lane * kWin;
     const int64_t w1 = w0 + kWin < e ? w0 + kWin : e;
-    int cnt = 0;
-    for (int64_t p = w0; p < w1; ++p) cnt += token_start(t, s, p) ? 1 : 0;
+    const unsigned mask = token_mask(t, s, w0, w1);
+    const int cnt = __popc(mask);
     int inc = cnt;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
@@ -412,9 +427,8 @@ __global__ void values_write_warp_kernel(const char* __restrict__ t, int64_t n, 
       if (lane >= off) inc += y;
     }
     int64_t slot = o + inc - cnt;
-    for (int64_t p = w0; p < w1; ++p) {
-      if (!token_start(t, s, p)) continue;
-      int64_t pos = p;
+    for (unsigned m = mask; m; m &= m - 1) {
+      int64_t pos = w0 + (__ffs(m) - 1);
       double v;
       extract_double(t, pos, e, v);
       out[slot++] = v;
