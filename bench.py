@@ -579,7 +579,7 @@ def run_next(args) -> None:
     wxy, wk = ob.nearest_node(hl, hn, nx, ny, ola, olo, vch, ole)
     same = bool(np.array_equal(wxy, xy[:pc].cpu().numpy()) and np.array_equal(wk, kk[:pc].cpu().numpy()))
     rows["nearest"] = {"metric": "geographic obs located/s", "unit": "obs/s", "value": po / t, "ms_per_call": 1e3 * t,
-                       "bound": "latency (hash ring search; nodes and hash fit in L2)", "gpu_launches": int(launches),
+                       "bound": "FP64 pipe (exact distance arithmetic per visited node; nodes and hash fit in L2)", "gpu_launches": int(launches),
                        "config": f"{nx}x{ny} curvilinear grid, {po} obs, 40 levels",
                        "sample_identical_to_oracle": same,
                        "cpu_baseline": {"value": pc / tcn, "unit": "obs/s", "cores": threads, "kind": "port",

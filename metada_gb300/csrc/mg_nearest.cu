@@ -12,7 +12,11 @@
 // (dist, index) minimum, and stops once no unvisited cell can hold a node at
 // a distance <= the best (a tie with a lower index is then impossible).
 // Distances use explicit round-to-nearest operations, so they and the
-// chosen nodes equal the reference's bit for bit.  The vertical index is
+// chosen nodes equal the reference's bit for bit.  The square root is taken
+// only near the running best: sqrt_rn maps s' and s to one value only if
+// s' <= s (1 + 2^-51), so a node whose sum of squares exceeds the best one's
+// times (1 + 2^-50), rounded up, is strictly farther and is skipped without
+// it.  The vertical index is
 // the first z minimising |level - vcoord[z]| (:491-500).
 #include <algorithm>
 #include <cmath>
@@ -117,9 +121,10 @@ __global__ void node_box_final_kernel(const double* __restrict__ part, int nb, d
   if (lane == 0) out[q] = r;
 }
 
-__device__ __forceinline__ double node_dist(double lat, double lon, double glat, double glon) {
+// dx^2 + dy^2 with the reference's roundings; the distance is its sqrt_rn.
+__device__ __forceinline__ double node_dist2(double lat, double lon, double glat, double glon) {
   const double dx = __dsub_rn(lon, glon), dy = __dsub_rn(lat, glat);
-  return __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+  return __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
 }
 
 __global__ void __launch_bounds__(kThreads) nearest_kernel(const double* __restrict__ olat,
@@ -135,7 +140,7 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const double* __restr
   if (o >= p) return;
   const double la = olat[o], lo = olon[o];
   const int cx0 = cell_x(g, lo), cy0 = cell_y(g, la);
-  double best = INFINITY;
+  double best = INFINITY, thr = INFINITY;  // thr: sums of squares above it cannot reach best
   int64_t bidx = INT64_MAX;
   const int rmax = g.cx > g.cy ? g.cx : g.cy;
   for (int r = 0; r <= rmax; ++r) {
@@ -147,11 +152,14 @@ __global__ void __launch_bounds__(kThreads) nearest_kernel(const double* __restr
         if (cxx < 0 || cxx >= g.cx) continue;
         const int64_t c = (int64_t)cyy * g.cx + cxx;
         for (int64_t t = start[c]; t < start[c + 1]; ++t) {
-          const double d = node_dist(la, lo, slat[t], slon[t]);
+          const double s2 = node_dist2(la, lo, slat[t], slon[t]);
+          if (!(s2 <= thr)) continue;  // strictly farther (or NaN, which the scan never takes)
+          const double d = __dsqrt_rn(s2);
           const int64_t id = sidx[t];
           if (d < best || (d == best && id < bidx)) {
             best = d;
             bidx = id;
+            thr = __dadd_ru(__dmul_ru(s2, 1.0 + 0x1p-50), 0x1p-1000);
           }
         }
       }

@@ -1,6 +1,8 @@
 """GPU: nearest-node search of geographic obs on a curvilinear grid (spatial
 hash) against the reference's scan restated in the oracle: bit-identical
 node choice, including ties, obs outside the grid and the vertical index."""
+import math
+
 import numpy as np
 import pytest
 import torch
@@ -50,3 +52,49 @@ def test_nearest_node_feeds_idw4(dev):
     HX = K.hx_idw4(T(X), nx, ny, xy).cpu().numpy()
     wxy, _ = ob.nearest_node(lat, lon, nx, ny, oa, ol)
     assert np.array_equal(HX, ob.hx_idw4(X, nx, ny, wxy))
+
+
+def _collapsed_pairs(n, seed):
+    """n obs, each with two nodes whose sums of squares dx^2 + dy^2 differ
+    while their rounded square roots are equal: the scan keeps the lower
+    index, which is given to the node with the larger sum."""
+    g = np.random.default_rng(seed)
+
+    def s_of(la, lo, gla, glo):
+        dx, dy = lo - glo, la - gla
+        return dx * dx + dy * dy
+
+    def step(x, k):
+        for _ in range(abs(k)):
+            x = float(np.nextafter(x, np.inf if k > 0 else -np.inf))
+        return x
+
+    lat, lon, oa, ol = np.empty(2 * n), np.empty(2 * n), np.empty(n), np.empty(n)
+    for j in range(n):
+        ola, olo, found = 0.0, 16.0 * j, None
+        while found is None:
+            t = g.uniform(0.0, 2.0 * np.pi)
+            A = (ola + 0.3 * math.sin(t), olo + 0.3 * math.cos(t))
+            sA = s_of(ola, olo, *A)
+            for a in range(-3, 4):
+                for b in range(-3, 4):
+                    B = (step(A[0], a), step(A[1], b))
+                    sB = s_of(ola, olo, *B)
+                    if sA != sB and math.sqrt(sA) == math.sqrt(sB):
+                        found = (A, B) if sA > sB else (B, A)
+                        break
+                if found is not None:
+                    break
+        (lat[2 * j], lon[2 * j]), (lat[2 * j + 1], lon[2 * j + 1]) = found
+        oa[j], ol[j] = ola, olo
+    return lat, lon, oa, ol
+
+
+def test_nearest_node_ties_of_rounded_square_roots(dev):
+    n = 200
+    lat, lon, oa, ol = _collapsed_pairs(n, 11)
+    want, _ = ob.nearest_node(lat, lon, 2, n, oa, ol)
+    assert np.all(want[:, 0] == 0) and np.array_equal(want[:, 1], np.arange(n))
+    T = lambda a: torch.tensor(a, device=dev)  # noqa: E731
+    xy, _ = K.nearest_node(T(lat), T(lon), 2, n, T(oa), T(ol))
+    assert np.array_equal(xy.cpu().numpy(), want)
