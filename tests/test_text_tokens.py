@@ -69,3 +69,17 @@ def test_irregular_token_defeats_a_token_wise_reading(built, tok):
     except ValueError:
         token_wise = None
     assert token_wise is None or not np.array_equal(got, token_wise)
+
+
+def test_value_count_bound(built):
+    """Two extracted values need a non-digit between their digits, so a text
+    of n bytes yields at most (n + 1) // 2 values (the output size the
+    parse wrapper allocates); dense texts reach it."""
+    for text in (b"1-1-1-1-1", b"1 1 1 1\n", b".5.5.5.5", b"1\n2\n3\n", b"1..5", b"7"):
+        assert len(ob.parse_values(text)) <= (len(text) + 1) // 2
+    assert len(ob.parse_values(b"1-1-1-1-1")) == 5
+    g = np.random.default_rng(5)
+    alphabet = np.frombuffer(b"0123456789.-+eE \n\t", dtype=np.uint8)
+    for _ in range(300):
+        text = g.choice(alphabet, int(g.integers(1, 200))).tobytes()
+        assert len(ob.parse_values(text)) <= (len(text) + 1) // 2
