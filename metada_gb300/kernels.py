@@ -124,6 +124,11 @@ def format_state(values: torch.Tensor, nx: int, ny: int) -> bytes:
     # its separator; others are formatted on the host and may need a second
     # call.  The text lands in pinned memory (the host allocator reuses it).
     cap = 25 * nx * ny + 1
+    if cap > _ONE_CALL_BYTES:  # too much pinned memory for a bound: count first
+        rc = ctx.lib.mg_format_state(ctx.handle, _ptr(values), nx, ny, c_void_p(0), 0, byref(nbytes))
+        if rc != _lib.MG_ERR_CAPACITY:
+            ctx.check(rc)
+        cap = max(nbytes.value, 1)
     buf = torch.empty(cap, dtype=torch.uint8, pin_memory=True)
     rc = ctx.lib.mg_format_state(ctx.handle, _ptr(values), nx, ny, c_void_p(buf.data_ptr()), cap, byref(nbytes))
     if rc == _lib.MG_ERR_CAPACITY:
