@@ -380,11 +380,11 @@ __global__ void values_count_warp_kernel(const char* __restrict__ t, int64_t n, 
   }
   bad = __any_sync(0xffffffffu, bad);
   host = __any_sync(0xffffffffu, host);
+  long long cnt = c;  // a line may hold more than 2^31 values
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+  for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
   if (lane != 0) return;
   int32_t m;
-  int64_t cnt = c;
   if (bad) {
     int h;
     cnt = line_values_seq(t, s, e, h, nullptr);
