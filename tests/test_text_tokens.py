@@ -83,3 +83,18 @@ def test_value_count_bound(built):
     for _ in range(300):
         text = g.choice(alphabet, int(g.integers(1, 200))).tobytes()
         assert len(ob.parse_values(text)) <= (len(text) + 1) // 2
+
+
+def test_exact_fast_path_is_correctly_rounded():
+    """The device conversion's fast path (Clinger 1990): for a decimal
+    mantissa m < 2^53 and exponent |e| <= 22, one IEEE multiplication or
+    division of float(m) (exact) by 10^|e| (exact in binary64) gives the
+    correctly rounded value of m * 10^e."""
+    g = np.random.default_rng(3)
+    cases = [(2 ** 53 - 1, 22), (2 ** 53 - 1, -22), (1, -22), (9007199254740991, -1), (1, 0), (0, 5)]
+    cases += [(int(g.integers(0, 2 ** 53)), int(g.integers(-22, 23))) for _ in range(20000)]
+    cases += [(int(g.integers(0, 10 ** int(g.integers(1, 16)))), int(g.integers(-22, 23))) for _ in range(5000)]
+    for m, e in cases:
+        p = float(f"1e{abs(e)}")
+        v = float(m) * p if e >= 0 else float(m) / p
+        assert v == float(f"{m}e{e}"), (m, e)
