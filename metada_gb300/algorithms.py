@@ -93,9 +93,13 @@ class Ensemble:
         self._mean = K.ens_mean(self.X)
 
     def Mean(self) -> np.ndarray:
+        return self.mean_tensor().cpu().numpy()
+
+    def mean_tensor(self) -> torch.Tensor:
+        """Ensemble::Mean() on the device (computed once, then cached)."""
         if self._mean is None:
             self.RecomputeMean()
-        return self._mean.cpu().numpy()
+        return self._mean
 
     def RecomputePerturbations(self) -> torch.Tensor:
         self._mean, Xp = K.ens_mean_pert(self.X)
@@ -180,15 +184,16 @@ def _flags(config: dict) -> int:
     return _lib.MG_RTPS if "rtps" in config else 0
 
 
-def _save_state(path: Path, values: np.ndarray, geometry) -> None:
+def _save_state(path: Path, values: torch.Tensor, geometry) -> None:
+    """One state of the ensemble (a float64 device vector) to a file: for a
+    SimpleGeometry the text of SimpleState::saveToFile ("%12.6f" rows,
+    SimpleState.hpp:160-188), formatted on the device; otherwise the exact
+    values as a binary .npy."""
     path.parent.mkdir(parents=True, exist_ok=True)
-    if isinstance(geometry, SimpleGeometry):  # SimpleState::saveToFile, "%12.6f" rows
-        nx, ny = geometry.x_dim, geometry.y_dim
-        with open(path, "w") as f:
-            for y in range(ny):
-                f.write(" ".join(f"{v:12.6f}" for v in values[y * nx:(y + 1) * nx]) + "\n")
+    if isinstance(geometry, SimpleGeometry):
+        path.write_bytes(K.format_state(values, geometry.x_dim, geometry.y_dim))
     else:
-        np.save(path.with_suffix(".npy"), values)
+        np.save(path.with_suffix(".npy"), values.cpu().numpy())
 
 
 class ETKF:
@@ -212,9 +217,9 @@ class ETKF:
 
     def saveEnsemble(self) -> None:
         base = Path(self.output_base_file)
-        _save_state(Path(f"{base}_mean.{self.format}"), self.ensemble.Mean(), self.ensemble.geometry)
+        _save_state(Path(f"{base}_mean.{self.format}"), self.ensemble.mean_tensor(), self.ensemble.geometry)
         for i in range(self.ensemble.Size()):
-            _save_state(Path(f"{base}_member_{i}.{self.format}"), self.ensemble.GetMember(i), self.ensemble.geometry)
+            _save_state(Path(f"{base}_member_{i}.{self.format}"), self.ensemble.X[i], self.ensemble.geometry)
 
 
 class EnKF:
@@ -256,9 +261,9 @@ class EnKF:
 
     def saveEnsemble(self) -> None:
         base = Path(self.output_base_file)
-        _save_state(Path(f"{base}_mean.{self.format}"), self.ensemble.Mean(), self.ensemble.geometry)
+        _save_state(Path(f"{base}_mean.{self.format}"), self.ensemble.mean_tensor(), self.ensemble.geometry)
         for i in range(self.ensemble.Size()):
-            _save_state(Path(f"{base}_member_{i}.{self.format}"), self.ensemble.GetMember(i), self.ensemble.geometry)
+            _save_state(Path(f"{base}_member_{i}.{self.format}"), self.ensemble.X[i], self.ensemble.geometry)
 
 
 class LETKF:
@@ -318,9 +323,9 @@ class LETKF:
 
     def saveEnsemble(self) -> None:
         base = Path(self.output_base_file)
-        _save_state(Path(f"{base}_mean.{self.format}"), self.ensemble.Mean(), self.ensemble.geometry)
+        _save_state(Path(f"{base}_mean.{self.format}"), self.ensemble.mean_tensor(), self.ensemble.geometry)
         for i in range(self.ensemble.Size()):
-            _save_state(Path(f"{base}_member_{i}.{self.format}"), self.ensemble.GetMember(i), self.ensemble.geometry)
+            _save_state(Path(f"{base}_member_{i}.{self.format}"), self.ensemble.X[i], self.ensemble.geometry)
 
 
 class Metrics:

@@ -153,3 +153,25 @@ def test_parse_values_stops_a_line_at_the_first_failed_extraction(dev):
     want = [1.5, 2.5, 4.0, 50.0, -0.25, 0.75, 7.0] + [float(i) for i in range(1, 12)] + [12.000000000000000000001]
     assert np.array_equal(got, np.array(want))
     assert np.array_equal(got, ob.parse_values(text))
+
+
+def test_save_ensemble_writes_the_reference_text(dev, tmp_path):
+    """saveEnsemble on a SimpleGeometry: the mean and every member as the
+    reference's "%12.6f" rows (SimpleState::saveToFile), from the device."""
+    from metada_gb300 import algorithms as A
+
+    nx, ny, k = 36, 18, 5
+    c = syn.global_etkf_grid(nx=nx, ny=ny, k=k, p=64, case=71)
+    X = c.X.copy()
+    X[0, :6] = [0.0078125, -0.0078125, -0.0, 2.5e-7, 2.0 ** 60, 1.0 / 3.0]  # ties, -0, host path
+    ens = A.Ensemble(X, A.SimpleGeometry(nx, ny), device=dev)
+    obs = A.Observation(c.yo, c.sigma_o, grid_xy=c.obs_xy, device=dev)
+    base = tmp_path / "out" / "analysis"
+    A.ETKF(ens, obs, A.ObsOperator(), {"inflation": 1.05, "output_base_file": str(base)}).saveEnsemble()
+
+    def text(v):
+        return ("\n".join(" ".join("%12.6f" % x for x in v[y * nx:(y + 1) * nx]) for y in range(ny)) + "\n").encode()
+
+    assert (tmp_path / "out" / "analysis_mean.txt").read_bytes() == text(ens.Mean())
+    for i in range(k):
+        assert (tmp_path / "out" / f"analysis_member_{i}.txt").read_bytes() == text(X[i])
