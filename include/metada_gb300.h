@@ -53,6 +53,9 @@ extern "C" {
 #define MG_WARM_START 32 /* batched LETKF: the levels of a column run in sequence, each
                             eigen-solve warm-started from the previous level's eigenvectors
                             (default: every eigen-solve starts from the identity) */
+#define MG_SOLVE_SIMT 64 /* batched LETKF, mixed precision: the SIMT Jacobi solve instead of
+                            the tensor-core Newton-Schulz route (which serves k <= 64 with the
+                            Hunt transform and update) */
 
 /* Arithmetic of the analysis. */
 #define MG_PREC_FP64 0  /* every step in IEEE double */
@@ -144,14 +147,16 @@ int mg_letkf_compat_grid(mg_context* ctx, double* X, int32_t k, int64_t ld, int3
                          double* mean_out);
 
 /* Allocation-free variant of mg_etkf, for callers that cannot allocate device
- * memory when they run the analysis: code running while its stream is being
- * captured into a CUDA graph (allocation is not allowed there), real-time
- * loops whose memory is fixed at start-up, and host frameworks that own every
- * device allocation through their own pool.  No counterpart in the reference
- * (its analysis is host code).
+ * memory when they run the analysis: real-time assimilation loops whose
+ * device memory is fixed at start-up (an allocation in the cycle could fail
+ * or stall it), and host frameworks that own every device allocation through
+ * their own pool (a cudaMalloc behind their back breaks their accounting, or
+ * fails because the pool already holds the memory).  No counterpart in the
+ * reference (its analysis is host code).
  *  - Same arguments and results as mg_etkf, but no context: work goes on
  *    `cuda_stream` (a cudaStream_t, NULL = default stream) of the current
- *    device, and only a status code is returned.
+ *    device.  The call copies its status word to the host and waits for the
+ *    stream before it returns the status code.
  *  - Scratch comes from one fixed 32 MiB array that the library reserves on
  *    every GPU it is loaded on, until the process exits; the call performs no
  *    cudaMalloc, cudaFree or other allocating call.  A problem needs about
@@ -397,7 +402,13 @@ typedef struct mg_letkf_stats {
   double ms_prepare;     /* device time: perturbations, obs prior, ordering */
   double ms_analysis;    /* device time of the local-analysis kernel */
   double ms_writeback;   /* device time: write-back to members and mean */
-  int64_t total_sweeps;  /* Jacobi sweeps summed over all analyses */
+  int64_t total_sweeps;  /* Jacobi sweeps (tensor-core path: Newton-Schulz iterations)
+                            summed over all analyses */
+  int64_t n_fallback;    /* tensor-core path: analyses whose residual test failed and
+                            that the SIMT Jacobi kernel re-ran */
+  double max_residual;   /* tensor-core path: largest max |Z A Z - P| accepted */
+  int32_t tensor_path;   /* 1 when the tensor-core kernel ran the analyses */
+  int32_t reserved;
 } mg_letkf_stats;
 int mg_letkf_last_stats(const mg_context* ctx, mg_letkf_stats* stats);
 

@@ -25,6 +25,7 @@ MG_UPDATE_COMPAT = 8
 MG_COMPAT = 15
 MG_RTPS = 16
 MG_WARM_START = 32
+MG_SOLVE_SIMT = 64
 
 MG_PREC_FP64 = 0
 MG_PREC_MIXED = 1
@@ -105,6 +106,10 @@ class LetkfStats(Structure):
         ("ms_analysis", c_double),
         ("ms_writeback", c_double),
         ("total_sweeps", c_int64),
+        ("n_fallback", c_int64),
+        ("max_residual", c_double),
+        ("tensor_path", c_int32),
+        ("reserved", c_int32),
     ]
 
 

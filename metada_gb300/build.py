@@ -89,10 +89,24 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def build_reference_harness() -> Path | None:
-    """Build the reference-header harness when the reference tree is present."""
-    ref = Path(os.environ.get("METADA_REFERENCE", "/root/reference"))
+def reference_root() -> Path | None:
+    """The reference source tree named by METADA_REFERENCE (None when the
+    variable is unset).  A set variable that does not name a tree with a
+    ``src/`` directory is an error, not a silent skip."""
+    val = os.environ.get("METADA_REFERENCE")
+    if not val:
+        return None
+    ref = Path(val)
     if not (ref / "src").is_dir():
+        raise RuntimeError(f"METADA_REFERENCE={val} does not name the reference tree (no src/ there)")
+    return ref
+
+
+def build_reference_harness() -> Path | None:
+    """Build the reference-header harness (test infrastructure) from the tree
+    that METADA_REFERENCE names; None, with nothing built, when it is unset."""
+    ref = reference_root()
+    if ref is None:
         return None
     _run(["bash", str(ORACLE_DIR / "build_ref.sh"), str(ref)])
     return ORACLE_DIR / "_ref" / "ref_harness"

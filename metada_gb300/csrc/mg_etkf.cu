@@ -248,15 +248,14 @@ extern "C" int mg_etkf(mg_context* ctx, double* X, int64_t n, int32_t k, int64_t
 // Allocation-free global ETKF.
 //
 // Some callers cannot allocate device memory at the point where they run the
-// analysis: code executing while a CUDA stream is being captured into a graph
-// (a cudaMalloc there is illegal), real-time loops whose memory budget is
-// fixed at start-up, and host frameworks that own every device allocation
-// through their own pool.  mg_etkf_noalloc serves them: it runs the same
-// kernels as mg_etkf, but its scratch lives in one file-scope device array
-// of fixed size, so the call itself performs no cudaMalloc/cudaFree and no
-// allocating library call.  The array is part of this library's module:
-// every GPU that loads the library keeps kStaticScratchBytes reserved until
-// the process exits.
+// analysis: real-time loops whose memory budget is fixed at start-up, and
+// host frameworks that own every device allocation through their own pool.
+// mg_etkf_noalloc serves them: it runs the same kernels as mg_etkf, but its
+// scratch lives in one file-scope device array of fixed size, so the call
+// itself performs no cudaMalloc/cudaFree and no allocating library call.  It
+// ends by copying the status word to the host and synchronising the stream.
+// The array is part of this library's module: every GPU that loads the
+// library keeps kStaticScratchBytes reserved until the process exits.
 // ---------------------------------------------------------------------------
 namespace {
 

@@ -21,12 +21,17 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "mg_dense.cuh"
 #include "mg_internal.h"
+#include "mg_letkf.cuh"
 
 namespace {
+
+using mg::LetkfParams;
+using mg::gaspari_cohn;
 
 constexpr int kThreads = 256;
 constexpr int kNVarMax = 8;
@@ -38,46 +43,6 @@ constexpr double kStage1Tol = 1e-3;
 // a / b by the hardware reciprocal for FP32 (a few ulp), exact for FP64.
 __device__ __forceinline__ float fast_div(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
-
-struct LetkfParams {
-  int k, kp, n_var, nlev;
-  int64_t ncol, npoints;
-  const int64_t* col_base;
-  int64_t lev_stride, var_stride;
-  const void* Xp;        // point-major perturbations, TE, [s*k + i]
-  const double* xmean;   // n
-  double* Xa;            // point-major analysis, [s*k + i]
-  const void* Y;         // obs anomalies, TE, [o*k + i]
-  const double* dinn;    // innovation
-  const double* rinv;    // 1 / error variance
-  const double* obs_lev; // or null
-  const int64_t* loc_off;
-  const int32_t* loc_idx;
-  const double* loc_dist;  // or null
-  double hsupport, vsupport, rho;
-  int flags;
-  const int32_t* order;  // columns, longest list first
-  unsigned long long* next;
-  unsigned long long* n_empty;
-  unsigned long long* total_local;
-  unsigned long long* total_sweeps;
-  int* max_local;
-  int* max_sweeps;
-  int* status;
-  double tol;
-  int sweep_cap;
-  int warm_start;  // levels of a column run in sequence, each Jacobi warm-started
-};
-
-template <typename T>
-__device__ __forceinline__ T gaspari_cohn(T z) {
-  z = fabs(z);
-  if (z >= T(2)) return T(0);
-  if (z <= T(1))
-    return (((T(-0.25) * z + T(0.5)) * z + T(0.625)) * z - T(5.0 / 3.0)) * z * z + T(1);
-  return ((((z / T(12) - T(0.5)) * z + T(0.625)) * z + T(5.0 / 3.0)) * z - T(5)) * z + T(4) -
-         T(2) / (T(3) * z);
-}
 
 // Shared-memory plan of one CTA: A and V (k x k, padded rows), one chunk of
 // gathered Y' rows (Ys) and, for the FP32 two-stage eigen-solve (k <= 96),
@@ -242,7 +207,14 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
     // The two-stage path may exchange the roles of the A and V regions.
     TE* A = A0;
     TE* V = V0;
-    const int64_t col = warm_mode ? prm.order[item] : prm.order[item / prm.nlev];
+    int64_t col;
+    if (prm.redo_in) {
+      const int32_t pt = prm.redo_in[item];
+      col = pt / prm.nlev;
+      lev = pt % prm.nlev;
+    } else {
+      col = warm_mode ? prm.order[item] : prm.order[item / prm.nlev];
+    }
     const int64_t base = prm.col_base[col] + (int64_t)lev * prm.lev_stride;
     const int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
 
@@ -818,6 +790,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   cv.reserve<uint32_t>((size_t)d->ncol * 2);       // keys
   cv.reserve<int32_t>((size_t)d->ncol * 2);        // vals
   cv.reserve<unsigned long long>(8);               // counters
+  cv.reserve<int32_t>((size_t)npoints);            // points handed back by the tensor-core path
   cv.reserve<char>(sort_bytes);
   void* ws = mg::workspace(ctx, cv.off);
   if (!ws) return MG_ERR_NOMEM;
@@ -831,6 +804,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   uint32_t* keys = cv.take<uint32_t>((size_t)d->ncol * 2);
   int32_t* vals = cv.take<int32_t>((size_t)d->ncol * 2);
   auto* cnt = cv.take<unsigned long long>(8);
+  int32_t* redo = cv.take<int32_t>((size_t)npoints);
   void* sort_tmp = cv.take<char>(sort_bytes);
   cudaStream_t s = ctx->stream;
 
@@ -887,9 +861,35 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   prm.tol = fp64 ? 1e-14 : 1e-6;
   prm.sweep_cap = fp64 ? 30 : 20;
   prm.warm_start = (d->flags & MG_WARM_START) ? 1 : 0;
+  prm.redo_out = redo;
+  prm.n_redo = cnt + 6;
+  prm.max_resid_bits = reinterpret_cast<unsigned*>(cnt + 7);
+  prm.redo_in = nullptr;
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[1], s));
   int rc;
-  if (fp64) {
+  const bool tensor = !fp64 && !(d->flags & MG_SOLVE_SIMT) && mg::letkf_tc_supported(prm);
+  int64_t n_fallback = 0;
+  if (tensor) {
+    // Tensor-core local analyses; the few whose residual test fails are
+    // re-run by the SIMT kernel over the list the first kernel wrote.
+    const int e = mg::letkf_tc_launch(prm, ctx->num_sms, s);
+    if (e != 0)
+      return mg::fail(ctx, MG_ERR_CUDA, std::string("letkf_tc_kernel: ") + cudaGetErrorString((cudaError_t)e));
+    unsigned long long hr = 0;
+    MG_TRY_CUDA(cudaMemcpyAsync(&hr, cnt + 6, sizeof(hr), cudaMemcpyDeviceToHost, s));
+    MG_TRY_CUDA(cudaStreamSynchronize(s));
+    n_fallback = (int64_t)hr;
+    rc = MG_OK;
+    if (n_fallback > 0) {
+      LetkfParams fb = prm;
+      fb.redo_in = redo;
+      fb.npoints = n_fallback;
+      fb.warm_start = 0;
+      fb.next = cnt + 6;  // reused as the work counter of the re-run
+      MG_TRY_CUDA(cudaMemsetAsync(cnt + 6, 0, sizeof(unsigned long long), s));
+      rc = launch_batched<float, 64>(ctx, fb);
+    }
+  } else if (fp64) {
     if (k <= 32) rc = launch_batched<double, 32>(ctx, prm);
     else if (k <= 64) rc = launch_batched<double, 64>(ctx, prm);
     else rc = launch_batched<double, 96>(ctx, prm);
@@ -906,7 +906,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   if (d->mean_out)
     MG_TRY_CUDA(mg::launch_mean_pert_members(d->X, n, k, d->ld, d->mean_out, nullptr, nullptr, 0, s));
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[3], s));
-  unsigned long long host_cnt[6];
+  unsigned long long host_cnt[8];
   MG_TRY_CUDA(cudaMemcpyAsync(host_cnt, cnt, sizeof(host_cnt), cudaMemcpyDeviceToHost, s));
   MG_TRY_CUDA(cudaStreamSynchronize(s));
   float ms[3] = {0.f, 0.f, 0.f};
@@ -920,6 +920,16 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   ctx->stats.max_local = (int32_t)(host_cnt[3] & 0xffffffffull);
   ctx->stats.max_sweeps = (int32_t)(host_cnt[3] >> 32);
   ctx->stats.total_sweeps = (int64_t)host_cnt[5];
+  ctx->stats.n_fallback = n_fallback;
+  {
+    const unsigned bits = (unsigned)(host_cnt[7] & 0xffffffffull);
+    float r;
+    memcpy(&r, &bits, sizeof(r));
+    ctx->stats.max_residual = tensor ? (double)r : 0.0;
+  }
+  ctx->stats.tensor_path = tensor ? 1 : 0;
+  if ((int)(host_cnt[4] & 0xffffffffull) == 2)
+    return mg::fail(ctx, MG_ERR_TIMEOUT, "mg_letkf_batched: a bounded tensor-core wait gave up");
   if ((int)(host_cnt[4] & 0xffffffffull) != 0)
     return mg::fail(ctx, MG_ERR_NUMERIC, "mg_letkf_batched: a local k x k system was not positive definite");
   return MG_OK;

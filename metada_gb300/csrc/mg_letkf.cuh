@@ -1,0 +1,64 @@
+// Parameters of the batched local analyses, shared by the SIMT kernels
+// (mg_letkf.cu) and the tensor-core kernel (mg_letkf_tc.cu).
+#pragma once
+
+#include <stdint.h>
+
+namespace mg {
+
+struct LetkfParams {
+  int k, kp, n_var, nlev;
+  int64_t ncol, npoints;
+  const int64_t* col_base;
+  int64_t lev_stride, var_stride;
+  const void* Xp;        // point-major perturbations, TE, [s*k + i]
+  const double* xmean;   // n
+  double* Xa;            // point-major analysis, [s*k + i]
+  const void* Y;         // obs anomalies, TE, [o*k + i]
+  const double* dinn;    // innovation
+  const double* rinv;    // 1 / error variance
+  const double* obs_lev; // or null
+  const int64_t* loc_off;
+  const int32_t* loc_idx;
+  const double* loc_dist;  // or null
+  double hsupport, vsupport, rho;
+  int flags;
+  const int32_t* order;  // columns, longest list first
+  unsigned long long* next;
+  unsigned long long* n_empty;
+  unsigned long long* total_local;
+  unsigned long long* total_sweeps;
+  int* max_local;
+  int* max_sweeps;
+  int* status;
+  double tol;
+  int sweep_cap;
+  int warm_start;  // levels of a column run in sequence, each Jacobi warm-started
+  // Tensor-core path: analyses it hands back (points col * nlev + lev) and
+  // their count; the largest first-order residual seen (float bits).
+  int32_t* redo_out;
+  unsigned long long* n_redo;
+  unsigned* max_resid_bits;
+  // SIMT path: when set, item i is the point redo_in[i] (col * nlev + lev)
+  // instead of the longest-first order.
+  const int32_t* redo_in;
+};
+
+template <typename T>
+__device__ __forceinline__ T gaspari_cohn(T z) {
+  z = fabs(z);
+  if (z >= T(2)) return T(0);
+  if (z <= T(1))
+    return (((T(-0.25) * z + T(0.5)) * z + T(0.625)) * z - T(5.0 / 3.0)) * z * z + T(1);
+  return ((((z / T(12) - T(0.5)) * z + T(0.625)) * z + T(5.0 / 3.0)) * z - T(5)) * z + T(4) -
+         T(2) / (T(3) * z);
+}
+
+// Tensor-core local analyses (mixed precision, Hunt transform, k <= 64):
+// true when this build and the parameters take that path.
+bool letkf_tc_supported(const LetkfParams& prm);
+// Launches them on `stream` with `num_sms` persistent CTA pairs; returns a
+// cudaError_t value (0 on success).
+int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream);
+
+}  // namespace mg

@@ -1,0 +1,827 @@
+// Batched LETKF local analyses on the tensor cores (mixed precision, Hunt
+// transform, k <= 64): the k x k Gram Y'^T R^-1 Y', the products of the
+// symmetric inverse square root and the update X' W all run as tcgen05.mma
+// kind::tf32 products with an error-compensated 3-pass split
+// (hi*hi + hi*lo + lo*hi, hi = x rounded to TF32, lo = x - hi), accumulated in
+// FP32 in tensor memory.  Replaces the grid loop of LETKF::Analyse
+// (LETKF.hpp:101) and the solve and update of updateGridPoint
+// (LETKF.hpp:214-238) in the Hunt et al. (2007) form with Gaspari-Cohn
+// R-localisation.
+//
+// Per local analysis (one CTA of 256 threads, two CTAs per SM, persistent,
+// points pulled longest list first from a work counter):
+//  1. Gram: the candidate list is filtered and weighted, the kept rows
+//     sqrt(w) Y'_o are gathered 32 at a time into a K-major, 128-byte
+//     swizzled operand (members x obs) with sqrt(w) d_o as an extra row, and
+//     [G | b] = B^T [B | sqrt(w) d] accumulates in TMEM (three rotating
+//     buffers, so the gather of one chunk overlaps the MMAs of the previous).
+//  2. A = (k-1)/rho I + G.  The ensemble-mean direction 1 is an exact
+//     eigenvector of A (Y' 1 = 0, eigenvalue delta) that never reaches the
+//     outputs (X' 1 = 0, 1^T b = 0), so the iteration runs on
+//     M = P A P / s + 1 1^T / k (P = I - 1 1^T / k), which puts that mode at 1;
+//     s = min(||A||_inf, ||PAP||_F) >= lambda_max keeps M's spectrum in (0, 1].
+//  3. Coupled Newton-Schulz: T = (3I - Z Y) / 2, [Z; Y] <- [Z; Y] T, with Z
+//     and Y stacked as the 128 rows of one MMA operand; it stops once
+//     max |Z Y - I| < 0.05 (one more step squares that error).  Z -> M^-1/2,
+//     and A^-1/2 = (Z - 1 1^T / k) / sqrt(s) on the complement of 1.
+//  4. First-order finish from the matrix itself: C = Z A Z, F = C - P,
+//     W = sqrt((k-1) c) Z (I - F/2), wa = c Z (P - F) Z b (c = rho for the
+//     reference's inflation placement, else 1).  max |F| is the per-analysis
+//     residual: analyses above kResidMax (or not converged, or not finite)
+//     are listed and re-run by the SIMT Jacobi kernel.
+//  5. Update: D = W^T X'^T (members x variables) on the tensor core, then
+//     x_a = x_mean + X' wa + D (+ RTPS relaxation), written in FP64.
+// Every mbarrier wait is bounded in time; a wait that gives up makes the CTA
+// set the status word, drain its own MMAs (bounded) and free its TMEM.
+#include <cuda_runtime.h>
+
+#include "mg_internal.h"
+#include "mg_letkf.cuh"
+#include "mg_tcgen05.cuh"
+
+namespace {
+
+using namespace mg::t5;
+
+constexpr int kThreads = 256;
+constexpr int KP = 64;          // member slots
+constexpr int kChunk = 32;      // obs per Gram chunk: one 128-byte swizzle atom of TF32
+constexpr int kGramN = 80;      // Gram MMA N: 64 member rows, the innovation row, 15 unused
+constexpr int kNBuf = 3;        // Gram chunk buffers
+constexpr int kSelRing = 512;   // selected-entry ring (a 256-candidate block + carry-over < 32)
+constexpr int kMaxIt = 14;      // Newton-Schulz iterations before an analysis is handed back
+constexpr float kStop = 0.05f;  // max |Z Y - I| that ends the iteration (after one more step)
+constexpr float kResidMax = 5e-3f;  // max |F| accepted from the first-order finish
+constexpr int kVarTile = 16;    // variables per update MMA (N)
+
+// Operand region: 96 KB, 1024-byte aligned.
+//   Newton-Schulz view: STACK (128 rows x 64 columns, two 16 KB slabs, hi
+//   and lo copies) and TB (64 rows x 64 columns, two 8 KB slabs, hi and lo).
+//   Gram view: three chunk buffers of 32 KB (hi slab, lo slab of 128 rows).
+constexpr uint32_t kSlabS = 128 * 128;  // STACK slab / Gram slab
+constexpr uint32_t kSlabT = 64 * 128;   // TB slab
+constexpr uint32_t OFF_STACK_HI = 0;
+constexpr uint32_t OFF_STACK_LO = 2 * kSlabS;
+constexpr uint32_t OFF_TB_HI = 4 * kSlabS;
+constexpr uint32_t OFF_TB_LO = OFF_TB_HI + 2 * kSlabT;
+constexpr uint32_t kRegion = OFF_TB_LO + 2 * kSlabT;  // 96 KB
+constexpr uint32_t kGramBuf = 2 * kSlabS;
+
+// Tensor memory: columns [0, 64) product scratch, [128, 208) the Gram.
+constexpr uint32_t kTmemCols = 256;
+constexpr uint32_t kTmGram = 128;
+
+// Vectors after the operand region.
+struct Vecs {
+  float b[KP], r[KP], u[KP], v[KP], wa[KP];
+  float part[4][KP];
+  float red[16];
+  float xsq[kVarTile], inc[kVarTile], fac[kVarTile], one[kVarTile];
+  float ssa[2][kVarTile];
+  double xm[kVarTile];
+  int sel_o[kSelRing];
+  float sel_sw[kSelRing];
+  float sel_sd[kSelRing];
+  int wcnt[kThreads / 32];
+};
+
+constexpr size_t kSmemBytes = 1024 + kRegion + sizeof(Vecs);
+
+// ---- operand addressing: K-major, 128-byte swizzle, TF32 in 32-bit words ----
+// Byte offset of element (row r, column c) in an operand whose slabs (32
+// columns each) hold `rows` rows.
+__device__ __forceinline__ uint32_t sw_off(int r, int c, uint32_t rows) {
+  return (uint32_t)(c >> 5) * rows * 128u + (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u +
+         ((uint32_t)(((c & 31) >> 2) ^ (r & 7)) << 4) + (uint32_t)(c & 3) * 4u;
+}
+
+__device__ __forceinline__ void split(float x, float& h, float& l) {
+  h = tf32_rna(x);
+  l = x - h;
+}
+
+// Row r, columns c0 .. c0+31 (c0 a multiple of 32: one slab row), 16-byte
+// stores (conflict-free across a warp's 32 consecutive rows).
+__device__ __forceinline__ void put_row32(unsigned char* hi, unsigned char* lo, int r, int c0, uint32_t rows,
+                                          const float (&x)[32]) {
+  const uint32_t base = (uint32_t)(c0 >> 5) * rows * 128u + (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float4 h, l;
+    split(x[4 * j + 0], h.x, l.x);
+    split(x[4 * j + 1], h.y, l.y);
+    split(x[4 * j + 2], h.z, l.z);
+    split(x[4 * j + 3], h.w, l.w);
+    const uint32_t off = base + ((uint32_t)(j ^ (r & 7)) << 4);
+    *reinterpret_cast<float4*>(hi + off) = h;
+    *reinterpret_cast<float4*>(lo + off) = l;
+  }
+}
+
+// Transposed: the thread's row kk of a matrix, columns n0 .. n0+31, goes to
+// operand rows n0 .. n0+31 at column kk (4-byte stores, conflict-free across
+// a warp's 32 consecutive kk).
+__device__ __forceinline__ void put_col32(unsigned char* hi, unsigned char* lo, int kk, int n0, uint32_t rows,
+                                          const float (&x)[32]) {
+  const uint32_t cb = (uint32_t)(kk >> 5) * rows * 128u + (uint32_t)(kk & 3) * 4u;
+  const int ch = (kk & 31) >> 2;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const int n = n0 + j;
+    const uint32_t off = cb + (uint32_t)(n >> 3) * 1024u + (uint32_t)(n & 7) * 128u + ((uint32_t)(ch ^ (n & 7)) << 4);
+    float h, l;
+    split(x[j], h, l);
+    *reinterpret_cast<float*>(hi + off) = h;
+    *reinterpret_cast<float*>(lo + off) = l;
+  }
+}
+
+// Row r, columns c0 .. c0+31 of an operand as values (hi + lo).
+__device__ __forceinline__ void get_row32(const unsigned char* hi, const unsigned char* lo, int r, int c0,
+                                          uint32_t rows, float (&x)[32]) {
+  const uint32_t base = (uint32_t)(c0 >> 5) * rows * 128u + (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const uint32_t off = base + ((uint32_t)(j ^ (r & 7)) << 4);
+    const float4 h = *reinterpret_cast<const float4*>(hi + off);
+    const float4 l = *reinterpret_cast<const float4*>(lo + off);
+    x[4 * j + 0] = h.x + l.x;
+    x[4 * j + 1] = h.y + l.y;
+    x[4 * j + 2] = h.z + l.z;
+    x[4 * j + 3] = h.w + l.w;
+  }
+}
+
+// Column c, rows r0 .. r0+31 of an operand as values (hi + lo); 4-byte
+// loads, conflict-free across a warp's 32 consecutive c.
+__device__ __forceinline__ void get_col32(const unsigned char* hi, const unsigned char* lo, int c, int r0,
+                                          uint32_t rows, float (&x)[32]) {
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const uint32_t off = sw_off(r0 + j, c, rows);
+    x[j] = *reinterpret_cast<const float*>(hi + off) + *reinterpret_cast<const float*>(lo + off);
+  }
+}
+
+// D (TMEM) += A B over nslab slabs of 32 K-columns, 3 passes per K-step of 8.
+// A: 128 rows from a_hi/a_lo (slab stride a_slab); B: N rows from b_hi/b_lo.
+__device__ __forceinline__ void issue3(uint32_t dtm, uint32_t a_hi, uint32_t a_lo, uint32_t a_slab, uint32_t b_hi,
+                                       uint32_t b_lo, uint32_t b_slab, int nslab, uint32_t idesc, bool accumulate) {
+  for (int s = 0; s < nslab; ++s) {
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      const uint32_t ao = s * a_slab + kk * 32, bo = s * b_slab + kk * 32;
+      const uint64_t ah = smem_desc_sw128(a_hi + ao), al = smem_desc_sw128(a_lo + ao);
+      const uint64_t bh = smem_desc_sw128(b_hi + bo), bl = smem_desc_sw128(b_lo + bo);
+      mma_tf32(dtm, ah, bh, idesc, (accumulate || s > 0 || kk > 0) ? 1u : 0u);
+      mma_tf32(dtm, ah, bl, idesc, 1u);
+      mma_tf32(dtm, al, bh, idesc, 1u);
+    }
+  }
+}
+
+// Operands written by the generic proxy become visible to the tensor core,
+// earlier TMEM reads are ordered before what follows the barrier.
+__device__ __forceinline__ void operands_ready() {
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+}
+
+// Every thread waits (bounded) for the phase; one CTA-wide decision.
+__device__ __forceinline__ bool wait_all(uint64_t* bar, uint32_t parity) {
+  const bool ok = mbar_wait(bar, parity);
+  const int bad = __syncthreads_or(ok ? 0 : 1);
+  tc_fence_after();
+  return bad == 0;
+}
+
+// FP64 decision for a candidate whose FP32 vertical distance is within 1e-4
+// of the support (kept out of line: a predicated FP64 instruction would
+// occupy the FP64 pipe for every candidate).
+__device__ __noinline__ bool vertical_keep_fp64(int lev, double obs_lev, double vsupport) {
+  return fabs((double)lev - obs_lev) <= vsupport;
+}
+
+__global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams prm) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* R = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  Vecs& V = *reinterpret_cast<Vecs*>(R + kRegion);
+  unsigned char* const STH = R + OFF_STACK_HI;
+  unsigned char* const STL = R + OFF_STACK_LO;
+  unsigned char* const TBH = R + OFF_TB_HI;
+  unsigned char* const TBL = R + OFF_TB_LO;
+  __shared__ uint64_t mma_bar;
+  __shared__ uint64_t buf_bar[kNBuf];
+  __shared__ uint32_t tmem_s;
+  __shared__ long long s_item;
+  __shared__ unsigned s_flag[4];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int q = warp & 3, hh = warp >> 2;  // TMEM lane quadrant, column half
+  const int k = prm.k;
+  const float ik = 1.0f / (float)k;
+  const float* __restrict__ Y = static_cast<const float*>(prm.Y);
+  const float* __restrict__ Xp = static_cast<const float*>(prm.Xp);
+  const bool r_identity = prm.flags & MG_R_IDENTITY;
+  const bool infl_compat = prm.flags & MG_INFL_COMPAT;
+  const bool rtps = prm.flags & MG_RTPS;
+  const float delta = (infl_compat || rtps) ? (float)(k - 1) : (float)((double)(k - 1) / prm.rho);
+  const float sc = infl_compat ? (float)prm.rho : 1.0f;
+  const float cw = sqrtf((float)(k - 1) * sc);
+  const float hc = (float)(0.5 * prm.hsupport), vc = (float)(0.5 * prm.vsupport), vs = (float)prm.vsupport;
+  const bool vec4 = (k & 3) == 0;
+
+  if (tid == 0) {
+    mbar_init(&mma_bar, 1);
+    for (int b = 0; b < kNBuf; ++b) mbar_init(&buf_bar[b], 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(&tmem_s, kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_s;
+  const uint32_t tm_row = ((uint32_t)(32 * q) << 16);  // this warp's TMEM lanes
+  const uint32_t sR = smem_u32(R);
+  const uint32_t idesc64 = idesc_tf32_f32(128, 64);
+  const uint32_t idescG = idesc_tf32_f32(128, kGramN);
+  const uint32_t idescU = idesc_tf32_f32(128, kVarTile);
+
+  uint32_t mma_ph = 0;      // parity of the next mma_bar phase
+  uint32_t gchunk = 0;      // Gram chunks issued by this CTA (buffer rotation)
+  bool alive = true;
+
+  for (;;) {
+    if (tid == 0) s_item = (long long)atomicAdd(prm.next, 1ull);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= prm.npoints) break;
+    const int lev = (int)(item % prm.nlev);
+    const int64_t col = prm.order[item / prm.nlev];
+    const int64_t base = prm.col_base[col] + (int64_t)lev * prm.lev_stride;
+    const int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
+
+    // ---------------- 1. selection and Gram ----------------
+    int head = 0, nsel = 0, nloc = 0, nch = 0;
+    auto emit_chunk = [&](int cnt) -> bool {
+      const int b = (int)(gchunk % kNBuf);
+      const uint32_t use = gchunk / kNBuf;
+      if (use > 0 && !wait_all(&buf_bar[b], (use - 1) & 1u)) return false;
+      unsigned char* bh = R + b * kGramBuf;
+      unsigned char* bl = bh + kSlabS;
+      // thread: obs slot (lane) x 8 members (warp)
+      const int slot = lane, m0 = warp * 8;
+      float x[8];
+      float sd = 0.0f;
+      if (slot < cnt) {
+        const int e = (head + slot) & (kSelRing - 1);
+        const int o = V.sel_o[e];
+        const float sw = V.sel_sw[e];
+        sd = V.sel_sd[e];
+        const float* yr = Y + (int64_t)o * k;
+        if (vec4 && m0 + 8 <= k) {
+          const float4 a = *reinterpret_cast<const float4*>(yr + m0);
+          const float4 c = *reinterpret_cast<const float4*>(yr + m0 + 4);
+          x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = c.x; x[5] = c.y; x[6] = c.z; x[7] = c.w;
+        } else {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) x[j] = (m0 + j < k) ? yr[m0 + j] : 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] *= sw;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = 0.0f;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const uint32_t off = sw_off(m0 + j, slot, 128);
+        float h, l;
+        split(x[j], h, l);
+        *reinterpret_cast<float*>(bh + off) = h;
+        *reinterpret_cast<float*>(bl + off) = l;
+      }
+      if (warp == 0) {  // the innovation row
+        const uint32_t off = sw_off(KP, slot, 128);
+        float h, l;
+        split(sd, h, l);
+        *reinterpret_cast<float*>(bh + off) = h;
+        *reinterpret_cast<float*>(bl + off) = l;
+      }
+      operands_ready();
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t a = sR + b * kGramBuf;
+        issue3(tmem + kTmGram, a, a + kSlabS, kSlabS, a, a + kSlabS, kSlabS, 1, idescG, nch > 0);
+        mma_commit(&buf_bar[b]);
+      }
+      ++gchunk;
+      ++nch;
+      head = (head + kChunk) & (kSelRing - 1);
+      return true;
+    };
+
+    for (int64_t c0 = e0; c0 < e1 && alive; c0 += kThreads) {
+      bool keep = false;
+      int o = 0;
+      float sw = 0.0f, sd = 0.0f;
+      if (c0 + tid < e1) {
+        const int64_t e = c0 + tid;
+        o = prm.loc_idx[e];
+        float w = 1.0f;
+        keep = true;
+        if (prm.obs_lev) {
+          const float ol = (float)prm.obs_lev[o];
+          const float dl = fabsf((float)lev - ol);
+          if (dl > vs + 1e-4f) keep = false;
+          else if (dl >= vs - 1e-4f) keep = vertical_keep_fp64(lev, prm.obs_lev[o], prm.vsupport);
+          if (keep && !r_identity) w *= mg::gaspari_cohn<float>(dl / vc);
+        }
+        if (keep && !r_identity) {
+          if (prm.loc_dist) w *= mg::gaspari_cohn<float>((float)prm.loc_dist[e] / hc);
+          w *= (float)prm.rinv[o];
+          if (!(w > 0.0f)) keep = false;
+        }
+        if (keep) {
+          sw = sqrtf(w);
+          sd = sw * (float)prm.dinn[o];
+        }
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if (lane == 0) V.wcnt[warp] = __popc(bal);
+      __syncthreads();
+      int wb = 0, cnt = 0;
+#pragma unroll
+      for (int w = 0; w < kThreads / 32; ++w) {
+        if (w < warp) wb += V.wcnt[w];
+        cnt += V.wcnt[w];
+      }
+      if (keep) {
+        const int pos = (head + nsel + wb + __popc(bal & ((1u << lane) - 1u))) & (kSelRing - 1);
+        V.sel_o[pos] = o;
+        V.sel_sw[pos] = sw;
+        V.sel_sd[pos] = sd;
+      }
+      __syncthreads();
+      nsel += cnt;
+      nloc += cnt;
+      while (nsel >= kChunk && alive) {
+        alive = emit_chunk(kChunk);
+        nsel -= kChunk;
+      }
+    }
+    if (alive && nsel > 0) {
+      alive = emit_chunk(nsel);
+      nsel = 0;
+    }
+    if (!alive) break;
+
+    if (nloc == 0) {
+      // LETKF.hpp:167-190: no local obs, x' *= sqrt(rho) (RTPS: unchanged).
+      const double sr = rtps ? 1.0 : sqrt(prm.rho);
+      for (int e = tid; e < prm.n_var * k; e += kThreads) {
+        const int v = e / k, i = e - v * k;
+        const int64_t s = base + (int64_t)v * prm.var_stride;
+        prm.Xa[s * k + i] = prm.xmean[s] + (double)Xp[s * k + i] * sr;
+      }
+      if (tid == 0) atomicAdd(prm.n_empty, 1ull);
+      __syncthreads();
+      continue;
+    }
+    if (tid == 0) mma_commit(&mma_bar);
+    if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
+    mma_ph ^= 1u;
+
+    // ---------------- 2. A, b, deflation and scaling ----------------
+    // Warps of quadrants 0-1 hold rows 0-63; column half hh.
+    const bool rowwarp = q < 2;
+    const int row = 32 * q + lane;
+    const int cb = 32 * hh;
+    float a[32];
+    if (rowwarp) {
+      uint32_t v[32];
+      tmem_ld32(tmem + tm_row + kTmGram + cb, v);
+      uint32_t bv = 0;
+      if (hh == 0) bv = tmem_ld1(tmem + tm_row + kTmGram + KP);
+      tmem_wait_ld();
+      float rs = 0.0f, as = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int c = cb + j;
+        float x = __uint_as_float(v[j]);
+        if (c == row) x += (row < k) ? delta : 1.0f;
+        a[j] = x;
+        if (row < k && c < k) {
+          rs += x;
+          as += fabsf(x);
+        }
+      }
+      V.part[hh][row] = rs;
+      V.part[2 + hh][row] = as;
+      if (hh == 0) V.b[row] = (row < k) ? __uint_as_float(bv) : 0.0f;
+    }
+    __syncthreads();
+    if (warp < 2) {  // row means r, grand mean c, infinity norm
+      const int i = tid;
+      const float r = (i < k) ? (V.part[0][i] + V.part[1][i]) * ik : 0.0f;
+      const float ab = (i < k) ? V.part[2][i] + V.part[3][i] : 0.0f;
+      V.r[i] = r;
+      float sr = r, mx = ab;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, off);
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      }
+      if (lane == 0) {
+        V.red[warp] = sr;
+        V.red[2 + warp] = mx;
+      }
+    }
+    __syncthreads();
+    const float cbar = (V.red[0] + V.red[1]) * ik;
+    const float ninf = fmaxf(V.red[2], V.red[3]);
+    if (rowwarp) {  // P A P in registers, its Frobenius norm
+      const float ri = V.r[row];
+      float fs = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int c = cb + j;
+        const float x = (row < k && c < k) ? (a[j] - ri - V.r[c] + cbar) : 0.0f;
+        a[j] = x;
+        fs += x * x;
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) fs += __shfl_xor_sync(0xffffffffu, fs, off);
+      if (lane == 0) V.red[4 + q + 2 * hh] = fs;
+    }
+    __syncthreads();
+    const float fro = sqrtf(V.red[4] + V.red[5] + V.red[6] + V.red[7]);
+    const float s = fmaxf(fminf(ninf, fro), 1e-30f);
+    const float is = 1.0f / s;
+    // M = PAP / s + 1 1^T / k (identity on unused member slots); STACK <- [I; M]
+    // (row-major), TB <- T0 = (3I - M) / 2 stored transposed; e0 = max |M - I|.
+    float e_it = 0.0f;
+    if (rowwarp) {
+      float mrow[32], id[32], t[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int c = cb + j;
+        float m = (row < k && c < k) ? a[j] * is + ik : ((row == c) ? 1.0f : 0.0f);
+        mrow[j] = m;
+        id[j] = (row == c) ? 1.0f : 0.0f;
+        t[j] = 0.5f * (((row == c) ? 3.0f : 0.0f) - m);
+        e_it = fmaxf(e_it, fabsf(m - id[j]));
+      }
+      put_row32(STH, STL, row, cb, 128, id);
+      put_row32(STH, STL, KP + row, cb, 128, mrow);
+      put_col32(TBH, TBL, row, cb, 64, t);
+    }
+
+    // ---------------- 3. coupled Newton-Schulz ----------------
+    int its = 0;
+    bool stop = false;  // decided from max |Z Y - I| of the current iterate
+    bool conv = false;
+    for (;;) {
+      // [Z; Y] <- [Z; Y] T
+      operands_ready();
+      if (tid == 0) {
+        tc_fence_after();
+        issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2,
+               idesc64, false);
+        mma_commit(&mma_bar);
+      }
+      ++its;
+      const bool last = stop || its >= kMaxIt;
+      conv = stop;
+      if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
+      mma_ph ^= 1u;
+      {
+        uint32_t v[32];
+        tmem_ld32(tmem + tm_row + cb, v);
+        tmem_wait_ld();
+        float x[32];
+        if (!last) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]);
+          put_row32(STH, STL, 32 * q + lane, cb, 128, x);  // rows 0-63 Z, 64-127 Y
+        } else if (rowwarp) {
+          // Final Z -> (Z - 1 1^T / k) / sqrt(s) on the member block, 0 elsewhere,
+          // stored transposed (rows 0-63 hold Z^T); rows 64-127 <- P A P
+          // (re-read from the Gram in TMEM) for the finish.
+          const float isq = rsqrtf(s);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int c = cb + j;
+            x[j] = (row < k && c < k) ? (__uint_as_float(v[j]) - ik) * isq : 0.0f;
+          }
+          put_col32(STH, STL, row, cb, 128, x);
+          uint32_t g[32];
+          tmem_ld32(tmem + tm_row + kTmGram + cb, g);
+          tmem_wait_ld();
+          const float ri = V.r[row];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int c = cb + j;
+            float av = __uint_as_float(g[j]);
+            if (c == row) av += delta;
+            x[j] = (row < k && c < k) ? (av - ri - V.r[c] + cbar) : 0.0f;
+          }
+          put_row32(STH, STL, KP + row, cb, 128, x);
+        }
+      }
+      if (last) break;
+      // P = Z Y (Y as stored, rows 64-127), T = (3I - P) / 2 -> TB transposed.
+      operands_ready();
+      if (tid == 0) {
+        tc_fence_after();
+        issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_STACK_HI + KP * 128,
+               sR + OFF_STACK_LO + KP * 128, kSlabS, 2, idesc64, false);
+        mma_commit(&mma_bar);
+      }
+      if (tid == 0) s_flag[0] = 0u;
+      if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
+      mma_ph ^= 1u;
+      float emax = 0.0f;
+      if (rowwarp) {
+        uint32_t v[32];
+        tmem_ld32(tmem + tm_row + cb, v);
+        tmem_wait_ld();
+        float t[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int c = cb + j;
+          const float p = __uint_as_float(v[j]);
+          const float d = p - ((row == c) ? 1.0f : 0.0f);
+          emax = fmaxf(emax, fabsf(d));
+          t[j] = ((row == c) ? 1.0f : 0.0f) - 0.5f * d;
+        }
+        put_col32(TBH, TBL, row, cb, 64, t);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, off));
+        // a NaN compares false: treat it as not converged
+        if (lane == 0 && !(emax < kStop)) atomicOr(&s_flag[0], 1u);
+      }
+      __syncthreads();
+      stop = s_flag[0] == 0u;
+    }
+    if (!alive) break;
+
+    // ---------------- 4. finish ----------------
+    // The iterate is Z = p(M) up to rounding errors that the coupled
+    // iteration leaves as right factors, so the finish takes C = Z^T A Z:
+    // Q = (P A P) Z (A operand STACK rows 64.. = P A P, B operand Z^T rows),
+    // then C = Z^T Q; A^-1 = Z C^-1 Z^T, A^-1/2 ~ Z C^-1/2.
+    operands_ready();
+    if (tid == 0) {
+      tc_fence_after();
+      issue3(tmem, sR + OFF_STACK_HI + KP * 128, sR + OFF_STACK_LO + KP * 128, kSlabS, sR + OFF_STACK_HI,
+             sR + OFF_STACK_LO, kSlabS, 2, idesc64, false);
+      mma_commit(&mma_bar);
+    }
+    if (tid < KP) {  // u = Z^T b (row tid of Z^T)
+      float z[32], acc = 0.0f;
+      for (int c0 = 0; c0 < KP; c0 += 32) {
+        get_row32(STH, STL, tid, c0, 128, z);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc += z[j] * V.b[c0 + j];
+      }
+      V.u[tid] = acc;
+    }
+    if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
+    mma_ph ^= 1u;
+    if (rowwarp) {  // Q -> TB transposed
+      uint32_t v[32];
+      tmem_ld32(tmem + tm_row + cb, v);
+      tmem_wait_ld();
+      float x[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]);
+      put_col32(TBH, TBL, row, cb, 64, x);
+    }
+    // C = Z^T Q
+    operands_ready();
+    if (tid == 0) {
+      tc_fence_after();
+      issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2, idesc64,
+             false);
+      mma_commit(&mma_bar);
+      s_flag[1] = 0u;
+    }
+    if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
+    mma_ph ^= 1u;
+    // F = C - P (residual, partial F u); Z rows are read back from Z^T
+    // (column reads) and, after every read, stored row-major over Z^T; F goes
+    // to rows 64-127 as the B operand of Z F.
+    float zr[32];
+    if (rowwarp) {
+      float f[32];
+      uint32_t v[32];
+      tmem_ld32(tmem + tm_row + cb, v);
+      tmem_wait_ld();
+      float fu = 0.0f, fm = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int c = cb + j;
+        const float pij = (row < k && c < k) ? (((row == c) ? 1.0f : 0.0f) - ik) : 0.0f;
+        const float x = (row < k && c < k) ? __uint_as_float(v[j]) - pij : 0.0f;
+        f[j] = x;
+        fm = fmaxf(fm, fabsf(x));
+        fu += x * V.u[c];
+      }
+      V.part[hh][row] = fu;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) fm = fmaxf(fm, __shfl_xor_sync(0xffffffffu, fm, off));
+      // NaN or Inf residuals map to the maximum (positive floats order as integers)
+      if (lane == 0) atomicMax(&s_flag[1], (fm == fm && fm < 3.0e38f) ? __float_as_uint(fm) : 0x7f800000u);
+      put_col32(STH, STL, row, KP + cb, 128, f);  // rows 64-127 (P A P) are not read any more
+      get_col32(STH, STL, row, cb, 128, zr);
+    }
+    __syncthreads();
+    if (rowwarp) put_row32(STH, STL, row, cb, 128, zr);
+    // W = cw Z (I - F/2): D = Z F
+    operands_ready();
+    if (tid == 0) {
+      tc_fence_after();
+      issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_STACK_HI + KP * 128,
+             sR + OFF_STACK_LO + KP * 128, kSlabS, 2, idesc64, false);
+      mma_commit(&mma_bar);
+    }
+    const float resid = __uint_as_float(s_flag[1]);
+    if (tid < KP) V.v[tid] = (tid < k) ? V.u[tid] - (V.part[0][tid] + V.part[1][tid]) : 0.0f;
+    __syncthreads();
+    if (tid < KP) {  // wa = c Z v
+      float z[32], acc = 0.0f;
+      for (int c0 = 0; c0 < KP; c0 += 32) {
+        get_row32(STH, STL, tid, c0, 128, z);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) acc += z[j] * V.v[c0 + j];
+      }
+      V.wa[tid] = sc * acc;
+    }
+    if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
+    mma_ph ^= 1u;
+    const bool redo = !conv || !(resid <= kResidMax);
+    if (redo) {
+      // handed to the SIMT Jacobi kernel; nothing written for this point
+      if (tid == 0) {
+        const unsigned long long slot = atomicAdd(prm.n_redo, 1ull);
+        prm.redo_out[slot] = (int32_t)(col * prm.nlev + lev);
+      }
+      __syncthreads();
+      continue;
+    }
+    if (rowwarp) {  // W rows -> U^T = W^T into STACK rows 64.. (A operand of the update)
+      uint32_t v[32];
+      tmem_ld32(tmem + tm_row + cb, v);
+      tmem_wait_ld();
+      float z[32], w[32];
+      get_row32(STH, STL, row, cb, 128, z);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) w[j] = cw * (z[j] - 0.5f * __uint_as_float(v[j]));
+      // operand row m = column index of W, operand column = row of W
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int m = KP + cb + j;
+        const uint32_t off = sw_off(m, row, 128);
+        float h, l;
+        split(w[j], h, l);
+        *reinterpret_cast<float*>(STH + off) = h;
+        *reinterpret_cast<float*>(STL + off) = l;
+      }
+    }
+
+    __syncthreads();  // the W epilogue's reads of Z are done before TB and STACK change
+    // ---------------- 5. update ----------------
+    const float c1 = cw * rsqrtf(delta);  // W's eigenvalue on the mean direction
+    for (int v0 = 0; v0 < prm.n_var; v0 += kVarTile) {
+      const int nv = (prm.n_var - v0 < kVarTile) ? prm.n_var - v0 : kVarTile;
+      // X' rows of the variables -> TB rows 0..15 (B operand, K = members);
+      // one warp per two variables: X' wa, the mean of X', sum of X'^2.
+      for (int vv = warp; vv < kVarTile; vv += kThreads / 32) {
+        const float* xr = (vv < nv) ? Xp + (base + (int64_t)(v0 + vv) * prm.var_stride) * k : nullptr;
+        float x0 = 0.0f, x1 = 0.0f;
+        if (xr) {
+          if (lane < k) x0 = xr[lane];
+          if (lane + 32 < k) x1 = xr[lane + 32];
+        }
+        const uint32_t o0 = sw_off(vv, lane, 64), o1 = sw_off(vv, lane + 32, 64);
+        float h, l;
+        split(x0, h, l);
+        *reinterpret_cast<float*>(TBH + o0) = h;
+        *reinterpret_cast<float*>(TBL + o0) = l;
+        split(x1, h, l);
+        *reinterpret_cast<float*>(TBH + o1) = h;
+        *reinterpret_cast<float*>(TBL + o1) = l;
+        float dw = x0 * V.wa[lane] + x1 * V.wa[lane + 32];
+        float sx = x0 + x1, sq = x0 * x0 + x1 * x1;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          dw += __shfl_xor_sync(0xffffffffu, dw, off);
+          sx += __shfl_xor_sync(0xffffffffu, sx, off);
+          sq += __shfl_xor_sync(0xffffffffu, sq, off);
+        }
+        if (lane == 0) {
+          V.one[vv] = c1 * sx * ik;  // X' W on the mean direction (X' 1 is zero up to rounding)
+          V.inc[vv] = dw;
+          V.xsq[vv] = sq;
+          V.xm[vv] = (vv < nv) ? prm.xmean[base + (int64_t)(v0 + vv) * prm.var_stride] : 0.0;
+        }
+      }
+      operands_ready();
+      if (tid == 0) {
+        tc_fence_after();
+        issue3(tmem, sR + OFF_STACK_HI + KP * 128, sR + OFF_STACK_LO + KP * 128, kSlabS, sR + OFF_TB_HI,
+               sR + OFF_TB_LO, kSlabT, 2, idescU, false);
+        mma_commit(&mma_bar);
+      }
+      if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
+      mma_ph ^= 1u;
+      float dv[kVarTile];
+      if (rowwarp && hh == 0) {
+        uint32_t v[32];
+        tmem_ld32(tmem + tm_row, v);  // 16 columns used
+        tmem_wait_ld();
+#pragma unroll
+        for (int vv = 0; vv < kVarTile; ++vv) dv[vv] = __uint_as_float(v[vv]) + V.one[vv];
+        if (rtps) {  // analysis spread per variable (members = threads 0..63)
+#pragma unroll
+          for (int vv = 0; vv < kVarTile; ++vv) {
+            float s2 = (row < k) ? dv[vv] * dv[vv] : 0.0f;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, off);
+            if (lane == 0) V.ssa[q][vv] = s2;
+          }
+        }
+      }
+      if (rtps) {
+        __syncthreads();
+        if (tid < kVarTile) {
+          const float sb = sqrtf(V.xsq[tid] / (float)(k - 1));
+          const float sa = sqrtf((V.ssa[0][tid] + V.ssa[1][tid]) / (float)(k - 1));
+          V.fac[tid] = (sa > 0.0f) ? (float)prm.rho * (sb - sa) / sa : 0.0f;  // factor - 1
+        }
+        __syncthreads();
+      }
+      if (rowwarp && hh == 0 && row < k) {
+        for (int vv = 0; vv < nv; ++vv) {
+          const float a2 = rtps ? dv[vv] * (1.0f + V.fac[vv]) : dv[vv];
+          prm.Xa[(base + (int64_t)(v0 + vv) * prm.var_stride) * k + row] =
+              (V.xm[vv] + (double)V.inc[vv]) + (double)a2;
+        }
+      }
+      __syncthreads();  // TB and the vectors are rewritten by the next tile
+    }
+    if (!alive) break;
+    if (tid == 0) {
+      atomicAdd(prm.total_local, (unsigned long long)nloc);
+      atomicAdd(prm.total_sweeps, (unsigned long long)its);
+      atomicMax(prm.max_local, nloc);
+      atomicMax(prm.max_sweeps, its);
+      atomicMax(prm.max_resid_bits, s_flag[1]);
+    }
+  }
+
+  if (!alive) {
+    // A bounded wait gave up: record it, drain this CTA's MMAs (bounded).
+    if (tid == 0) {
+      atomicExch(prm.status, 2);
+      mma_commit(&mma_bar);
+      mbar_wait(&mma_bar, mma_ph);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+}  // namespace
+
+namespace mg {
+
+bool letkf_tc_supported(const LetkfParams& prm) {
+  const bool chol = prm.flags & MG_SQRT_CHOLESKY, upd = prm.flags & MG_UPDATE_COMPAT;
+  return prm.k >= 2 && prm.k <= KP && !chol && !upd && !prm.warm_start && prm.redo_out && prm.n_redo;
+}
+
+int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream) {
+  cudaError_t e = cudaFuncSetAttribute(letkf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kSmemBytes);
+  if (e != cudaSuccess) return (int)e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, letkf_tc_kernel, kThreads, kSmemBytes);
+  if (e != cudaSuccess) return (int)e;
+  // Two CTAs per SM share its 512 TMEM columns; never more.
+  if (per_sm > 2) per_sm = 2;
+  if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
+  int64_t grid = (int64_t)per_sm * num_sms;
+  if (grid > prm.npoints) grid = prm.npoints;
+  if (grid < 1) grid = 1;
+  letkf_tc_kernel<<<(unsigned)grid, kThreads, kSmemBytes, static_cast<cudaStream_t>(stream)>>>(prm);
+  MG_COUNT_LAUNCH();
+  return (int)cudaGetLastError();
+}
+
+}  // namespace mg

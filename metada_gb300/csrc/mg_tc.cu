@@ -23,6 +23,7 @@
 #include <mutex>
 
 #include "mg_internal.h"
+#include "mg_tcgen05.cuh"
 
 namespace {
 
@@ -33,101 +34,7 @@ constexpr int kThreads = 64 + 32 * kEpiWarps;  // TMA warp, MMA warp, epilogue w
 // Shared-memory ring of A and B k-blocks (the widest tile keeps three so the
 // ring and the epilogue staging fit in 227 KB).
 __host__ __device__ constexpr int ring_stages(int bn) { return bn >= 256 ? 3 : 4; }
-constexpr uint64_t kWaitNs = 1000000000ull;  // one wait gives up after 1 s (a legitimate one takes microseconds)
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ bool mbar_test(uint32_t addr, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(done)
-      : "r"(addr), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
-// Wait for the given phase parity, bounded by elapsed time (kWaitNs, checked
-// every 64 polls; try_wait itself may suspend for a hardware-defined time, so
-// a poll count would not bound the wall time) and, for mbar_wait_ab, by
-// another role raising *abort.  False if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  const uint32_t addr = smem_u32(bar);
-  const uint64_t t0 = global_ns();
-  for (unsigned it = 1;; ++it) {
-    if (mbar_test(addr, parity)) return true;
-    if ((it & 63u) == 0u && global_ns() - t0 > kWaitNs) return false;
-  }
-}
-
-__device__ __forceinline__ bool mbar_wait_ab(uint64_t* bar, uint32_t parity, volatile int* abort) {
-  const uint32_t addr = smem_u32(bar);
-  const uint64_t t0 = global_ns();
-  for (unsigned it = 1;; ++it) {
-    if (mbar_test(addr, parity)) return true;
-    if ((it & 63u) == 0u && (*abort || global_ns() - t0 > kWaitNs)) return false;
-  }
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
-          smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
-      : "memory");
-}
-
-// SM100 shared-memory matrix descriptor, SWIZZLE_128B, K-major.
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);          // start address
-  d |= (uint64_t)1 << 16;                          // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)((1024 >> 4) & 0x3FFF) << 32;     // stride byte offset: 8 rows x 128 B
-  d |= (uint64_t)1 << 46;                          // descriptor version (SM100)
-  d |= (uint64_t)2 << 61;                          // layout: SWIZZLE_128B
-  return d;
-}
-
-// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
+using namespace mg::t5;
 
 __device__ __forceinline__ float silu_f(float z) { return z / (1.0f + expf(-z)); }
 // SiLU for BF16-only outputs (hidden activations): the hardware exp2-based

@@ -2,10 +2,14 @@
 # Builds oracle/_ref/ref_harness from the reference's own headers where they
 # lie (read-only source tree, nothing copied), against oracle/eigen_subset.
 # Test infrastructure only; the output directory is git-ignored.
-# usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# usage: oracle/build_ref.sh REFERENCE_ROOT   (or METADA_REFERENCE set)
 set -euo pipefail
 here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-ref="${1:-/root/reference}"
+ref="${1:-${METADA_REFERENCE:-}}"
+if [ -z "$ref" ]; then
+  echo "usage: $0 REFERENCE_ROOT (or set METADA_REFERENCE); ref_harness not built" >&2
+  exit 2
+fi
 if [ ! -d "$ref/src" ]; then
   echo "reference tree not found at $ref; ref_harness not built" >&2
   exit 3

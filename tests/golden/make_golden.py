@@ -95,8 +95,8 @@ def main(ref_root: str | None = None) -> None:
     if ref_root:
         os.environ["METADA_REFERENCE"] = ref_root
     if build_reference_harness() is None:
-        raise SystemExit("reference tree not found; cannot regenerate the golden fixtures")
-    ref = Path(os.environ.get("METADA_REFERENCE", "/root/reference"))
+        raise SystemExit("set METADA_REFERENCE (or pass the reference root) to regenerate the golden fixtures")
+    ref = Path(os.environ["METADA_REFERENCE"])
     tut = ref / "src" / "backends" / "simple" / "tutorial"
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)

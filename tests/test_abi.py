@@ -49,7 +49,25 @@ def test_create_without_gpu_reports_cuda_error(built):
     assert rc == _lib.MG_ERR_CUDA and not h.value
 
 
-def test_descriptor_layout_matches_header():
-    # 25 fields; pointer/int64/double are 8 bytes, int32 pairs pack to 8.
-    assert ctypes.sizeof(_lib.LetkfDesc) == 8 * 22
-    assert ctypes.sizeof(_lib.LetkfStats) == 64
+def test_descriptor_layout_matches_header(tmp_path):
+    """The ctypes mirrors have the C structs' sizes and field offsets, as a
+    C compiler lays out include/metada_gb300.h."""
+    import subprocess
+
+    structs = {"mg_letkf_desc": _lib.LetkfDesc, "mg_letkf_stats": _lib.LetkfStats, "mg_etkf_case": _lib.EtkfCase}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "metada_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out if line.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)

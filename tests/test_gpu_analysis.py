@@ -197,22 +197,50 @@ def test_letkf_mixed_odd_member_counts(dev, k):
 
 @pytest.mark.slow
 def test_letkf_latlon_full_size_sampled(dev):
-    """The 360 x 180 x 10 x 4, 64-member, 500k-obs configuration: FP64 and
-    mixed on the GPU, checked against the oracle on a sample of columns, and
-    mixed against FP64 everywhere (rel err <= 1e-5)."""
+    """The 360 x 180 x 10 x 4, 64-member, 500k-obs configuration, on the
+    benchmarked inputs:
+    * local selection (LETKF.hpp:159-165 with Location.hpp:349-357) of 240
+      sampled columns against the oracle's own search over all 500k obs:
+      lists and counts bit-exact, distances to 1e-13;
+    * H(X) rows of every obs in those lists against the oracle's operator:
+      bit-exact;
+    * the FP64 analysis of those columns against the oracle run on its own
+      lists and H(X) (nothing of the GPU's fed in) at 1e-10;
+    * mixed against FP64 everywhere at 1e-5."""
     c = syn.latlon_letkf_case()
     X64, HX, off, idx, dist, st64 = _run_latlon(dev, c, _lib.MG_PREC_FP64)
-    Xmx, _, _, _, _, stmx = _run_latlon(dev, c, _lib.MG_PREC_MIXED)
+    cols = np.sort(np.random.default_rng(7).choice(c.nlat * c.nlon, 240, replace=False))
+    clat, clon = c.col_lat_lon()
+    offc, idxc, distc = ob.select_geo(clat[cols], clon[cols], c.obs_lat, c.obs_lon, c.hsupport_km)
+    for j, col in enumerate(cols):
+        e0, e1 = int(off[col]), int(off[col + 1])
+        assert e1 - e0 == int(offc[j + 1] - offc[j]), f"column {col}: count differs"
+        assert np.array_equal(idx[e0:e1], idxc[offc[j]:offc[j + 1]]), f"column {col}: list differs"
+        # distances come from device sin/cos/asin: equal to the host expression to rounding
+        np.testing.assert_allclose(dist[e0:e1], distc[offc[j]:offc[j + 1]], rtol=1e-13, atol=1e-9)
+    assert offc[-1] > 100 * len(cols)  # the sample holds a realistic share of the lists
+    need = np.unique(idxc)
+    HXc = ob.hx_latlon(c.X, c.nlon, c.nlat, c.nlev, c.obs_lat[need], c.obs_lon[need], c.obs_lev[need],
+                       c.obs_var[need])
+    assert np.array_equal(HX.cpu().numpy()[need], HXc)
+    # oracle analysis of the sampled columns from its own lists and H(X)
+    HXo = np.zeros((c.yo.size, HXc.shape[1]))
+    HXo[need] = HXc
+    offo = np.zeros(c.nlat * c.nlon + 1, dtype=np.int64)
+    offo[cols + 1] = np.diff(offc)
+    offo = np.cumsum(offo)
+    base, want = _oracle_latlon(c, HXo, offo, idxc, distc, cols)
     a64 = X64.cpu().numpy()
+    del X64
+    gv = np.stack([a64[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)
+    assert rel_err(gv, want) <= FP64_TOL
+    Xmx, _, _, _, _, stmx = _run_latlon(dev, c, _lib.MG_PREC_MIXED)
     amx = Xmx.cpu().numpy()
+    del Xmx
     # mean and perturbation errors of the mixed path against FP64
     m64, mmx = a64.mean(0), amx.mean(0)
     assert rel_err(mmx, m64) <= MIXED_TOL
     assert rel_err(amx - mmx, a64 - m64) <= MIXED_TOL
-    cols = np.random.default_rng(7).choice(c.nlat * c.nlon, 40, replace=False)
-    base, want = _oracle_latlon(c, HX.cpu().numpy(), off, idx, dist, cols)
-    gv = np.stack([a64[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)
-    assert rel_err(gv, want) <= FP64_TOL
     # every analysis point of the configuration has local observations
     assert st64.n_points == c.nlat * c.nlon * c.nlev and st64.n_empty == stmx.n_empty == 0
 

@@ -1,7 +1,7 @@
 """GPU test of mg_etkf_noalloc, the entry point for callers that cannot
-allocate device memory while they run the analysis (inside a CUDA-graph
-capture, in a fixed-memory real-time loop, under a framework that owns all
-device allocations).  Its output must match mg_etkf's, call after call: the
+allocate device memory while they run the analysis (a real-time loop whose
+device memory is fixed at start-up, a framework that owns every device
+allocation through its own pool).  Its output must match mg_etkf's, call after call: the
 shared scratch array keeps the previous call's contents and must not leak
 into the next result.  This file is collected last so that a failure here
 stops a `-x` run only after every other test has run."""
