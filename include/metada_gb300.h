@@ -102,6 +102,11 @@ int mg_hx_idw4(mg_context* ctx, const double* X, int32_t k, int64_t ld, int32_t 
 int mg_hx_latlon(mg_context* ctx, const double* X, int32_t k, int64_t ld, int32_t nlon,
                  int32_t nlat, int32_t nlev, const double* obs_lat, const double* obs_lon,
                  const double* obs_lev, const int32_t* obs_var, int64_t p, double* HX);
+/* The same operator on members stored as FP32 (widened to FP64 on load;
+ * the high-resolution configuration keeps its 80 members in FP32). */
+int mg_hx_latlon_f32(mg_context* ctx, const float* X, int32_t k, int64_t ld, int32_t nlon,
+                     int32_t nlat, int32_t nlev, const double* obs_lat, const double* obs_lon,
+                     const double* obs_lev, const int32_t* obs_var, int64_t p, double* HX);
 
 /* LETKF::updateGridPoint local search, src/framework/algorithms/
  * LETKF.hpp:159-165 with Location::distance_to GRID branch
@@ -176,8 +181,13 @@ int mg_etkf_noalloc(void* cuda_stream, double* X, int64_t n, int32_t k, int64_t 
 
 /* Batched LETKF over columns x levels with the obs-space prior of the
  * background (all local analyses independent). */
+/* Storage type of the members in mg_letkf_desc.X. */
+#define MG_DTYPE_F64 0
+#define MG_DTYPE_F32 1 /* mixed precision only: FP64 means from the widened values, the analysis
+                          rounded to FP32 on write-back */
+
 typedef struct mg_letkf_desc {
-  double* X;             /* members, member-major, updated in place */
+  void* X;               /* members, member-major (x_dtype), updated in place */
   int64_t n;             /* state values per member */
   int64_t ld;            /* member stride (>= n) */
   int32_t k;             /* members, 2..128 */
@@ -200,7 +210,7 @@ typedef struct mg_letkf_desc {
   double vsupport;       /* vertical support in levels (obs with |dl| > vsupport dropped) */
   double rho;            /* inflation (MG_RTPS: relaxation alpha) */
   int32_t flags;         /* MG_* semantics bits */
-  int32_t reserved;
+  int32_t x_dtype;       /* MG_DTYPE_F64 or MG_DTYPE_F32 */
   double* mean_out;      /* device n or NULL: analysis ensemble mean */
 } mg_letkf_desc;
 
@@ -408,7 +418,7 @@ typedef struct mg_letkf_stats {
                             that the SIMT Jacobi kernel re-ran */
   double max_residual;   /* tensor-core path: largest max |Z A Z - P| accepted */
   int32_t tensor_path;   /* 1 when the tensor-core kernel ran the analyses */
-  int32_t reserved;
+  int32_t tensor_ctas;   /* CTAs of its persistent grid */
 } mg_letkf_stats;
 int mg_letkf_last_stats(const mg_context* ctx, mg_letkf_stats* stats);
 

@@ -30,6 +30,9 @@ MG_SOLVE_SIMT = 64
 MG_PREC_FP64 = 0
 MG_PREC_MIXED = 1
 
+MG_DTYPE_F64 = 0
+MG_DTYPE_F32 = 1
+
 _ERR_NAMES = {
     MG_ERR_ARG: "invalid argument",
     MG_ERR_CUDA: "CUDA error",
@@ -73,7 +76,7 @@ class LetkfDesc(Structure):
         ("vsupport", c_double),
         ("rho", c_double),
         ("flags", c_int32),
-        ("reserved", c_int32),
+        ("x_dtype", c_int32),
         ("mean_out", c_void_p),
     ]
 
@@ -109,7 +112,7 @@ class LetkfStats(Structure):
         ("n_fallback", c_int64),
         ("max_residual", c_double),
         ("tensor_path", c_int32),
-        ("reserved", c_int32),
+        ("tensor_ctas", c_int32),
     ]
 
 
@@ -138,6 +141,8 @@ _SIGNATURES = {
                    c_void_p],
     "mg_hx_latlon": [c_void_p, c_void_p, c_int32, c_int64, c_int32, c_int32, c_int32, c_void_p, c_void_p,
                      c_void_p, c_void_p, c_int64, c_void_p],
+    "mg_hx_latlon_f32": [c_void_p, c_void_p, c_int32, c_int64, c_int32, c_int32, c_int32, c_void_p, c_void_p,
+                         c_void_p, c_void_p, c_int64, c_void_p],
     "mg_select_grid": [c_void_p, c_int32, c_int32, c_void_p, c_int64, c_double, c_void_p, c_void_p, c_int64,
                        POINTER(c_int64)],
     "mg_select_geo": [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_double, c_void_p,

@@ -11,18 +11,19 @@ namespace {
 
 constexpr int kTile = 32;  // state indices per transpose tile
 
+template <typename TX>
 __global__ void __launch_bounds__(256) mean_pert_members_kernel(
-    const double* __restrict__ X, int64_t n, int k, int64_t ld, double inv_k,
+    const TX* __restrict__ X, int64_t n, int k, int64_t ld, double inv_k,
     double* __restrict__ mean, double* __restrict__ Xp64, float* __restrict__ Xp32, int64_t ldp) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += stride) {
     double m = 0.0;
-    for (int i = 0; i < k; ++i) m = __dadd_rn(m, __ldg(X + (int64_t)i * ld + s));
+    for (int i = 0; i < k; ++i) m = __dadd_rn(m, (double)__ldg(X + (int64_t)i * ld + s));
     m = __dmul_rn(m, inv_k);
     if (mean) mean[s] = m;
     if (Xp64 || Xp32) {
       for (int i = 0; i < k; ++i) {
-        const double v = __dsub_rn(__ldg(X + (int64_t)i * ld + s), m);
+        const double v = __dsub_rn((double)__ldg(X + (int64_t)i * ld + s), m);
         if (Xp64) Xp64[(int64_t)i * ldp + s] = v;
         if (Xp32) Xp32[(int64_t)i * ldp + s] = (float)v;
       }
@@ -33,8 +34,8 @@ __global__ void __launch_bounds__(256) mean_pert_members_kernel(
 // Member-major X -> point-major perturbations P[s*k + i] = X_i[s] - mean[s].
 // One block per 32 consecutive state indices; tile staged in shared memory so
 // both the member rows (input) and the point rows (output) are coalesced.
-template <typename TP>
-__global__ void __launch_bounds__(256) to_point_major_kernel(const double* __restrict__ X, int64_t n,
+template <typename TX, typename TP>
+__global__ void __launch_bounds__(256) to_point_major_kernel(const TX* __restrict__ X, int64_t n,
                                                              int k, int64_t ld, double inv_k,
                                                              double* __restrict__ mean,
                                                              TP* __restrict__ P) {
@@ -44,7 +45,7 @@ __global__ void __launch_bounds__(256) to_point_major_kernel(const double* __res
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int i = warp; i < k; i += nw) {
     const int64_t s = s0 + lane;
-    tile[i * (kTile + 1) + lane] = (s < n) ? __ldg(X + (int64_t)i * ld + s) : 0.0;
+    tile[i * (kTile + 1) + lane] = (s < n) ? (double)__ldg(X + (int64_t)i * ld + s) : 0.0;
   }
   __syncthreads();
   if (threadIdx.x < kTile) {
@@ -64,10 +65,11 @@ __global__ void __launch_bounds__(256) to_point_major_kernel(const double* __res
   }
 }
 
-// Point-major P[s*k + i] -> member-major X_i[s].
-__global__ void __launch_bounds__(256) point_major_to_members_kernel(const double* __restrict__ P,
+// Point-major P[s*k + i] -> member-major X_i[s] (TX: the members' storage type).
+template <typename TP, typename TX>
+__global__ void __launch_bounds__(256) point_major_to_members_kernel(const TP* __restrict__ P,
                                                                      int64_t n, int k,
-                                                                     double* __restrict__ X,
+                                                                     TX* __restrict__ X,
                                                                      int64_t ld) {
   extern __shared__ double tile[];  // [kTile][k + 1]
   const int64_t s0 = (int64_t)blockIdx.x * kTile;
@@ -75,13 +77,13 @@ __global__ void __launch_bounds__(256) point_major_to_members_kernel(const doubl
   for (int e = threadIdx.x; e < total; e += blockDim.x) {
     const int j = e / k, i = e - j * k;
     const int64_t s = s0 + j;
-    tile[j * (k + 1) + i] = (s < n) ? __ldg(P + s * k + i) : 0.0;
+    tile[j * (k + 1) + i] = (s < n) ? (double)__ldg(P + s * k + i) : 0.0;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int i = warp; i < k; i += nw) {
     const int64_t s = s0 + lane;
-    if (s < n) X[(int64_t)i * ld + s] = tile[lane * (k + 1) + i];
+    if (s < n) X[(int64_t)i * ld + s] = (TX)tile[lane * (k + 1) + i];
   }
 }
 
@@ -98,8 +100,8 @@ namespace mg {
 
 cudaError_t launch_mean_pert_members(const double* X, int64_t n, int k, int64_t ld, double* mean,
                                      double* Xp64, float* Xp32, int64_t ldp, cudaStream_t s) {
-  mean_pert_members_kernel<<<grid_for(n, 256), 256, 0, s>>>(X, n, k, ld, 1.0 / (double)k, mean,
-                                                           Xp64, Xp32, ldp);
+  mean_pert_members_kernel<double><<<grid_for(n, 256), 256, 0, s>>>(X, n, k, ld, 1.0 / (double)k, mean,
+                                                                   Xp64, Xp32, ldp);
   MG_COUNT_LAUNCH();
   return cudaGetLastError();
 }
@@ -109,11 +111,11 @@ cudaError_t launch_to_point_major(const double* X, int64_t n, int k, int64_t ld,
   const int64_t blocks = (n + kTile - 1) / kTile;
   const size_t smem = (size_t)k * (kTile + 1) * sizeof(double);
   if (P64)
-    to_point_major_kernel<double><<<(unsigned)blocks, 256, smem, s>>>(X, n, k, ld, 1.0 / (double)k,
-                                                                      mean, P64);
+    to_point_major_kernel<double, double><<<(unsigned)blocks, 256, smem, s>>>(X, n, k, ld, 1.0 / (double)k,
+                                                                              mean, P64);
   else
-    to_point_major_kernel<float><<<(unsigned)blocks, 256, smem, s>>>(X, n, k, ld, 1.0 / (double)k,
-                                                                     mean, P32);
+    to_point_major_kernel<double, float><<<(unsigned)blocks, 256, smem, s>>>(X, n, k, ld, 1.0 / (double)k,
+                                                                             mean, P32);
   MG_COUNT_LAUNCH();
   return cudaGetLastError();
 }
@@ -122,7 +124,34 @@ cudaError_t launch_point_major_to_members(const double* P, int64_t n, int k, dou
                                           cudaStream_t s) {
   const int64_t blocks = (n + kTile - 1) / kTile;
   const size_t smem = (size_t)kTile * (k + 1) * sizeof(double);
-  point_major_to_members_kernel<<<(unsigned)blocks, 256, smem, s>>>(P, n, k, X, ld);
+  point_major_to_members_kernel<double, double><<<(unsigned)blocks, 256, smem, s>>>(P, n, k, X, ld);
+  MG_COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+// Members stored as FP32: the mean in FP64 of the widened values (member
+// order), FP32 perturbations point-major, and the FP32 write-back.
+cudaError_t launch_mean_members_f32(const float* X, int64_t n, int k, int64_t ld, double* mean, cudaStream_t s) {
+  mean_pert_members_kernel<float><<<grid_for(n, 256), 256, 0, s>>>(X, n, k, ld, 1.0 / (double)k, mean, nullptr,
+                                                                  nullptr, 0);
+  MG_COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_point_major_f32(const float* X, int64_t n, int k, int64_t ld, double* mean, float* P32,
+                                      cudaStream_t s) {
+  const int64_t blocks = (n + kTile - 1) / kTile;
+  const size_t smem = (size_t)k * (kTile + 1) * sizeof(double);
+  to_point_major_kernel<float, float><<<(unsigned)blocks, 256, smem, s>>>(X, n, k, ld, 1.0 / (double)k, mean, P32);
+  MG_COUNT_LAUNCH();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_point_major_to_members_f32(const float* P, int64_t n, int k, float* X, int64_t ld,
+                                              cudaStream_t s) {
+  const int64_t blocks = (n + kTile - 1) / kTile;
+  const size_t smem = (size_t)kTile * (k + 1) * sizeof(double);
+  point_major_to_members_kernel<float, float><<<(unsigned)blocks, 256, smem, s>>>(P, n, k, X, ld);
   MG_COUNT_LAUNCH();
   return cudaGetLastError();
 }

@@ -67,6 +67,12 @@ cudaError_t launch_to_point_major(const double* X, int64_t n, int k, int64_t ld,
                                   double* P64, float* P32, cudaStream_t s);
 cudaError_t launch_point_major_to_members(const double* P, int64_t n, int k, double* X,
                                           int64_t ld, cudaStream_t s);
+// The same stages for members stored as FP32 (FP64 mean of the widened values).
+cudaError_t launch_mean_members_f32(const float* X, int64_t n, int k, int64_t ld, double* mean, cudaStream_t s);
+cudaError_t launch_to_point_major_f32(const float* X, int64_t n, int k, int64_t ld, double* mean, float* P32,
+                                      cudaStream_t s);
+cudaError_t launch_point_major_to_members_f32(const float* P, int64_t n, int k, float* X, int64_t ld,
+                                              cudaStream_t s);
 // Obs-space prior: ym = rowmean(HX), Y' = HX - ym (FP64 and/or FP32 copies),
 // d = yo - ym, rinv = 1/rvar.
 cudaError_t launch_obs_prior(const double* HX, const double* yo, const double* rvar, int64_t p,

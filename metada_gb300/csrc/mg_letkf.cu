@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
       for (int e = tid; e < prm.n_var * k; e += kThreads) {
         const int v = e / k, i = e - v * k;
         const int64_t s = base + (int64_t)v * prm.var_stride;
-        prm.Xa[s * k + i] = prm.xmean[s] + (double)Xp[s * k + i] * sr;
+        mg::letkf_store(prm, s * k + i, prm.xmean[s] + (double)Xp[s * k + i] * sr);
       }
       if (tid == 0) atomicAdd(prm.n_empty, 1ull);
       __syncthreads();
@@ -527,7 +527,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
           out = (xm[v] + (double)inc) + (double)s2;
           if (rtps) Ys[v * KMAX + i] = s2;  // analysis perturbation for the spread
         }
-        prm.Xa[(base + (int64_t)(v0 + v) * prm.var_stride) * k + i] = out;
+        mg::letkf_store(prm, (base + (int64_t)(v0 + v) * prm.var_stride) * k + i, out);
       }
     } else
     for (int e = tid; e < nv * k; e += kThreads) {
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
         out = (xm[v] + (double)inc) + (double)s2;
         if (rtps) Ys[v * KMAX + i] = s2;  // analysis perturbation for the spread
       }
-      prm.Xa[(base + (int64_t)(v0 + v) * prm.var_stride) * k + i] = out;
+      mg::letkf_store(prm, (base + (int64_t)(v0 + v) * prm.var_stride) * k + i, out);
     }
     if (rtps && !upd_compat) {
       __syncthreads();
@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
       __syncthreads();
       for (int e = tid; e < nv * k; e += kThreads) {
         const int v = e / k, i = e - v * k;
-        prm.Xa[(base + (int64_t)(v0 + v) * prm.var_stride) * k + i] += red[v] * (double)Ys[v * KMAX + i];
+        mg::letkf_add(prm, (base + (int64_t)(v0 + v) * prm.var_stride) * k + i, red[v] * (double)Ys[v * KMAX + i]);
       }
     }
     __syncthreads();
@@ -579,6 +579,15 @@ __global__ void __launch_bounds__(kThreads, (sizeof(TE) == 4 && KMAX <= 64) ? 4 
     }
     __syncthreads();
   }
+}
+
+// Per-observation FP32 pack for the tensor-core kernel: (level, 1/sigma^2,
+// innovation, 0), one 16-byte gather per candidate instead of three.
+__global__ void obs_pack_kernel(const double* __restrict__ obs_lev, const double* __restrict__ rinv,
+                                const double* __restrict__ dinn, int64_t p, float4* __restrict__ out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p; o += stride)
+    out[o] = make_float4(obs_lev ? (float)obs_lev[o] : 0.0f, (float)rinv[o], (float)dinn[o], 0.0f);
 }
 
 // Column list lengths (keys) for the longest-first order.
@@ -771,6 +780,11 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   const bool fp64 = d->precision == MG_PREC_FP64;
   const int k = d->k;
   MG_CHECK_ARG(!fp64 || k <= 96, "mg_letkf_batched: FP64 path supports k <= 96");
+  MG_CHECK_ARG(d->x_dtype == MG_DTYPE_F64 || d->x_dtype == MG_DTYPE_F32, "mg_letkf_batched: bad x_dtype");
+  // Members stored as FP32: the mixed path only, analysis written over the
+  // FP32 perturbations (no FP64 point-major copy) and back as FP32.
+  const bool x32 = d->x_dtype == MG_DTYPE_F32;
+  MG_CHECK_ARG(!x32 || !fp64, "mg_letkf_batched: FP32 members need the mixed precision path");
   const int64_t n = d->n, p = d->p;
   const int64_t npoints = d->ncol * d->nlev;
   const size_t te = fp64 ? sizeof(double) : sizeof(float);
@@ -783,7 +797,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   mg::Carver cv;
   cv.reserve<char>((size_t)n * k * te);            // Xp
   cv.reserve<double>((size_t)n);                   // mean
-  cv.reserve<double>((size_t)n * k);               // Xa
+  cv.reserve<double>(x32 ? 1 : (size_t)n * k);     // Xa (FP64 members only)
   cv.reserve<char>((size_t)(p + 1) * k * te);      // Y
   cv.reserve<double>((size_t)p + 1);               // d
   cv.reserve<double>((size_t)p + 1);               // rinv
@@ -791,13 +805,14 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   cv.reserve<int32_t>((size_t)d->ncol * 2);        // vals
   cv.reserve<unsigned long long>(8);               // counters
   cv.reserve<int32_t>((size_t)npoints);            // points handed back by the tensor-core path
+  cv.reserve<float4>((size_t)p + 1);               // per-obs FP32 pack (tensor-core path)
   cv.reserve<char>(sort_bytes);
   void* ws = mg::workspace(ctx, cv.off);
   if (!ws) return MG_ERR_NOMEM;
   cv = mg::Carver{static_cast<char*>(ws), 0};
   void* Xp = cv.take<char>((size_t)n * k * te);
   double* mean = cv.take<double>((size_t)n);
-  double* Xa = cv.take<double>((size_t)n * k);
+  double* Xa = cv.take<double>(x32 ? 1 : (size_t)n * k);
   void* Y = cv.take<char>((size_t)(p + 1) * k * te);
   double* dinn = cv.take<double>((size_t)p + 1);
   double* rinv = cv.take<double>((size_t)p + 1);
@@ -805,13 +820,17 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   int32_t* vals = cv.take<int32_t>((size_t)d->ncol * 2);
   auto* cnt = cv.take<unsigned long long>(8);
   int32_t* redo = cv.take<int32_t>((size_t)npoints);
+  float4* opack = cv.take<float4>((size_t)p + 1);
   void* sort_tmp = cv.take<char>(sort_bytes);
   cudaStream_t s = ctx->stream;
 
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[0], s));
   // Point-major perturbations and means (Ensemble.hpp:105-151).
-  MG_TRY_CUDA(mg::launch_to_point_major(d->X, n, k, d->ld, mean, fp64 ? (double*)Xp : nullptr,
-                                        fp64 ? nullptr : (float*)Xp, s));
+  if (x32)
+    MG_TRY_CUDA(mg::launch_to_point_major_f32(static_cast<const float*>(d->X), n, k, d->ld, mean, (float*)Xp, s));
+  else
+    MG_TRY_CUDA(mg::launch_to_point_major(static_cast<const double*>(d->X), n, k, d->ld, mean,
+                                          fp64 ? (double*)Xp : nullptr, fp64 ? nullptr : (float*)Xp, s));
   // Obs-space prior from the background (snapshot).
   if (p > 0)
     MG_TRY_CUDA(mg::launch_obs_prior(d->HX, d->yo, d->rvar, p, k, fp64 ? (double*)Y : nullptr,
@@ -838,7 +857,8 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   prm.var_stride = d->var_stride;
   prm.Xp = Xp;
   prm.xmean = mean;
-  prm.Xa = Xa;
+  prm.Xa = x32 ? nullptr : Xa;
+  prm.Xa32 = x32 ? static_cast<float*>(Xp) : nullptr;
   prm.Y = Y;
   prm.dinn = dinn;
   prm.rinv = rinv;
@@ -869,10 +889,18 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   int rc;
   const bool tensor = !fp64 && !(d->flags & MG_SOLVE_SIMT) && mg::letkf_tc_supported(prm);
   int64_t n_fallback = 0;
+  int tc_ctas = 0;
   if (tensor) {
     // Tensor-core local analyses; the few whose residual test fails are
     // re-run by the SIMT kernel over the list the first kernel wrote.
-    const int e = mg::letkf_tc_launch(prm, ctx->num_sms, s);
+    if (p > 0) {
+      const unsigned pb = (unsigned)std::min<int64_t>((p + 255) / 256, (int64_t)ctx->num_sms * 16);
+      obs_pack_kernel<<<pb, 256, 0, s>>>(d->obs_lev, rinv, dinn, p, opack);
+      MG_COUNT_LAUNCH();
+      MG_TRY_CUDA(cudaGetLastError());
+    }
+    prm.opack = opack;
+    const int e = mg::letkf_tc_launch(prm, ctx->num_sms, s, &tc_ctas);
     if (e != 0)
       return mg::fail(ctx, MG_ERR_CUDA, std::string("letkf_tc_kernel: ") + cudaGetErrorString((cudaError_t)e));
     unsigned long long hr = 0;
@@ -902,9 +930,17 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   if (rc != MG_OK) return rc;
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[2], s));
   // Write back member-major; the analysis mean as LETKF.hpp:116 recomputes it.
-  MG_TRY_CUDA(mg::launch_point_major_to_members(Xa, n, k, d->X, d->ld, s));
-  if (d->mean_out)
-    MG_TRY_CUDA(mg::launch_mean_pert_members(d->X, n, k, d->ld, d->mean_out, nullptr, nullptr, 0, s));
+  if (x32) {
+    MG_TRY_CUDA(mg::launch_point_major_to_members_f32(static_cast<const float*>(Xp), n, k,
+                                                      static_cast<float*>(d->X), d->ld, s));
+    if (d->mean_out)
+      MG_TRY_CUDA(mg::launch_mean_members_f32(static_cast<const float*>(d->X), n, k, d->ld, d->mean_out, s));
+  } else {
+    MG_TRY_CUDA(mg::launch_point_major_to_members(Xa, n, k, static_cast<double*>(d->X), d->ld, s));
+    if (d->mean_out)
+      MG_TRY_CUDA(mg::launch_mean_pert_members(static_cast<const double*>(d->X), n, k, d->ld, d->mean_out, nullptr,
+                                               nullptr, 0, s));
+  }
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[3], s));
   unsigned long long host_cnt[8];
   MG_TRY_CUDA(cudaMemcpyAsync(host_cnt, cnt, sizeof(host_cnt), cudaMemcpyDeviceToHost, s));
@@ -928,6 +964,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
     ctx->stats.max_residual = tensor ? (double)r : 0.0;
   }
   ctx->stats.tensor_path = tensor ? 1 : 0;
+  ctx->stats.tensor_ctas = tc_ctas;
   if ((int)(host_cnt[4] & 0xffffffffull) == 2)
     return mg::fail(ctx, MG_ERR_TIMEOUT, "mg_letkf_batched: a bounded tensor-core wait gave up");
   if ((int)(host_cnt[4] & 0xffffffffull) != 0)

@@ -2,6 +2,7 @@
 // (mg_letkf.cu) and the tensor-core kernel (mg_letkf_tc.cu).
 #pragma once
 
+#include <cuda_runtime.h>
 #include <stdint.h>
 
 namespace mg {
@@ -14,10 +15,13 @@ struct LetkfParams {
   const void* Xp;        // point-major perturbations, TE, [s*k + i]
   const double* xmean;   // n
   double* Xa;            // point-major analysis, [s*k + i]
+  float* Xa32;           // or, for members stored as FP32, the FP32 analysis (may be Xp itself:
+                         // each point's rows are read before they are written)
   const void* Y;         // obs anomalies, TE, [o*k + i]
   const double* dinn;    // innovation
   const double* rinv;    // 1 / error variance
   const double* obs_lev; // or null
+  const float4* opack;    // tensor-core path: per obs (level, 1/sigma^2, innovation, 0) in FP32
   const int64_t* loc_off;
   const int32_t* loc_idx;
   const double* loc_dist;  // or null
@@ -44,6 +48,16 @@ struct LetkfParams {
   const int32_t* redo_in;
 };
 
+// Analysis value of point-major element idx, in the output's precision.
+__device__ __forceinline__ void letkf_store(const LetkfParams& prm, int64_t idx, double v) {
+  if (prm.Xa32) prm.Xa32[idx] = (float)v;
+  else prm.Xa[idx] = v;
+}
+__device__ __forceinline__ void letkf_add(const LetkfParams& prm, int64_t idx, double dv) {
+  if (prm.Xa32) prm.Xa32[idx] = (float)((double)prm.Xa32[idx] + dv);
+  else prm.Xa[idx] += dv;
+}
+
 template <typename T>
 __device__ __forceinline__ T gaspari_cohn(T z) {
   z = fabs(z);
@@ -57,8 +71,8 @@ __device__ __forceinline__ T gaspari_cohn(T z) {
 // Tensor-core local analyses (mixed precision, Hunt transform, k <= 64):
 // true when this build and the parameters take that path.
 bool letkf_tc_supported(const LetkfParams& prm);
-// Launches them on `stream` with `num_sms` persistent CTA pairs; returns a
-// cudaError_t value (0 on success).
-int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream);
+// Launches them on `stream` as a persistent grid (two CTAs per SM when they
+// fit); returns a cudaError_t value (0 on success) and the CTA count.
+int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream, int* ctas);
 
 }  // namespace mg

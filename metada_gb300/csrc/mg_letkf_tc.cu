@@ -167,15 +167,17 @@ __device__ __forceinline__ void get_col32(const unsigned char* hi, const unsigne
 // A: 128 rows from a_hi/a_lo (slab stride a_slab); B: N rows from b_hi/b_lo.
 __device__ __forceinline__ void issue3(uint32_t dtm, uint32_t a_hi, uint32_t a_lo, uint32_t a_slab, uint32_t b_hi,
                                        uint32_t b_lo, uint32_t b_slab, int nslab, uint32_t idesc, bool accumulate) {
+  // Descriptors of the first K-step; later steps add (byte offset >> 4) to
+  // the 14-bit start-address field (shared addresses stay below 256 KB).
+  const uint64_t ah = smem_desc_sw128(a_hi), al = smem_desc_sw128(a_lo);
+  const uint64_t bh = smem_desc_sw128(b_hi), bl = smem_desc_sw128(b_lo);
   for (int s = 0; s < nslab; ++s) {
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
-      const uint32_t ao = s * a_slab + kk * 32, bo = s * b_slab + kk * 32;
-      const uint64_t ah = smem_desc_sw128(a_hi + ao), al = smem_desc_sw128(a_lo + ao);
-      const uint64_t bh = smem_desc_sw128(b_hi + bo), bl = smem_desc_sw128(b_lo + bo);
-      mma_tf32(dtm, ah, bh, idesc, (accumulate || s > 0 || kk > 0) ? 1u : 0u);
-      mma_tf32(dtm, ah, bl, idesc, 1u);
-      mma_tf32(dtm, al, bh, idesc, 1u);
+      const uint64_t ao = (uint64_t)((s * a_slab + kk * 32) >> 4), bo = (uint64_t)((s * b_slab + kk * 32) >> 4);
+      mma_tf32(dtm, ah + ao, bh + bo, idesc, (accumulate || s > 0 || kk > 0) ? 1u : 0u);
+      mma_tf32(dtm, ah + ao, bl + bo, idesc, 1u);
+      mma_tf32(dtm, al + ao, bh + bo, idesc, 1u);
     }
   }
 }
@@ -264,117 +266,124 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     const int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
 
     // ---------------- 1. selection and Gram ----------------
-    int head = 0, nsel = 0, nloc = 0, nch = 0;
-    auto emit_chunk = [&](int cnt) -> bool {
-      const int b = (int)(gchunk % kNBuf);
-      const uint32_t use = gchunk / kNBuf;
-      if (use > 0 && !wait_all(&buf_bar[b], (use - 1) & 1u)) return false;
-      unsigned char* bh = R + b * kGramBuf;
-      unsigned char* bl = bh + kSlabS;
-      // thread: obs slot (lane) x 8 members (warp)
-      const int slot = lane, m0 = warp * 8;
-      float x[8];
-      float sd = 0.0f;
+    // Rounds: compact candidates into the ring (up to kSelRing - kThreads
+    // entries), then emit its chunks; each chunk's rows are loaded into
+    // registers while the previous chunk is stored and its MMAs issued.
+    int64_t cpos = e0;
+    int nloc = 0, nch = 0, head = 0, nsel = 0;
+    const int slot = lane, m0 = warp * 8;  // gather: obs slot (lane) x 8 members (warp)
+    auto load_rows = [&](int pos, int cnt, float (&x)[8], float& sd) {
       if (slot < cnt) {
-        const int e = (head + slot) & (kSelRing - 1);
+        const int e = (pos + slot) & (kSelRing - 1);
         const int o = V.sel_o[e];
         const float sw = V.sel_sw[e];
         sd = V.sel_sd[e];
         const float* yr = Y + (int64_t)o * k;
         if (vec4 && m0 + 8 <= k) {
-          const float4 a = *reinterpret_cast<const float4*>(yr + m0);
-          const float4 c = *reinterpret_cast<const float4*>(yr + m0 + 4);
-          x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = c.x; x[5] = c.y; x[6] = c.z; x[7] = c.w;
+          const float4 a4 = *reinterpret_cast<const float4*>(yr + m0);
+          const float4 c4 = *reinterpret_cast<const float4*>(yr + m0 + 4);
+          x[0] = a4.x * sw; x[1] = a4.y * sw; x[2] = a4.z * sw; x[3] = a4.w * sw;
+          x[4] = c4.x * sw; x[5] = c4.y * sw; x[6] = c4.z * sw; x[7] = c4.w * sw;
         } else {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) x[j] = (m0 + j < k) ? yr[m0 + j] : 0.0f;
+          for (int j = 0; j < 8; ++j) x[j] = (m0 + j < k) ? yr[m0 + j] * sw : 0.0f;
         }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) x[j] *= sw;
       } else {
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[j] = 0.0f;
+        sd = 0.0f;
       }
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const uint32_t off = sw_off(m0 + j, slot, 128);
-        float h, l;
-        split(x[j], h, l);
-        *reinterpret_cast<float*>(bh + off) = h;
-        *reinterpret_cast<float*>(bl + off) = l;
-      }
-      if (warp == 0) {  // the innovation row
-        const uint32_t off = sw_off(KP, slot, 128);
-        float h, l;
-        split(sd, h, l);
-        *reinterpret_cast<float*>(bh + off) = h;
-        *reinterpret_cast<float*>(bl + off) = l;
-      }
-      operands_ready();
-      if (tid == 0) {
-        tc_fence_after();
-        const uint32_t a = sR + b * kGramBuf;
-        issue3(tmem + kTmGram, a, a + kSlabS, kSlabS, a, a + kSlabS, kSlabS, 1, idescG, nch > 0);
-        mma_commit(&buf_bar[b]);
-      }
-      ++gchunk;
-      ++nch;
-      head = (head + kChunk) & (kSelRing - 1);
-      return true;
     };
-
-    for (int64_t c0 = e0; c0 < e1 && alive; c0 += kThreads) {
-      bool keep = false;
-      int o = 0;
-      float sw = 0.0f, sd = 0.0f;
-      if (c0 + tid < e1) {
-        const int64_t e = c0 + tid;
-        o = prm.loc_idx[e];
-        float w = 1.0f;
-        keep = true;
-        if (prm.obs_lev) {
-          const float ol = (float)prm.obs_lev[o];
-          const float dl = fabsf((float)lev - ol);
-          if (dl > vs + 1e-4f) keep = false;
-          else if (dl >= vs - 1e-4f) keep = vertical_keep_fp64(lev, prm.obs_lev[o], prm.vsupport);
-          if (keep && !r_identity) w *= mg::gaspari_cohn<float>(dl / vc);
+    while (alive) {
+      while (cpos < e1 && nsel <= kSelRing - kThreads) {
+        bool keep = false;
+        int o = 0;
+        float sw = 0.0f, sd = 0.0f;
+        if (cpos + tid < e1) {
+          const int64_t e = cpos + tid;
+          o = prm.loc_idx[e];
+          const float4 pk = prm.opack[o];  // (level, 1/sigma^2, innovation, 0) as FP32
+          float w = 1.0f;
+          keep = true;
+          if (prm.obs_lev) {
+            const float dl = fabsf((float)lev - pk.x);
+            if (dl > vs + 1e-4f) keep = false;
+            else if (dl >= vs - 1e-4f) keep = vertical_keep_fp64(lev, prm.obs_lev[o], prm.vsupport);
+            if (keep && !r_identity) w *= mg::gaspari_cohn<float>(dl / vc);
+          }
+          if (keep && !r_identity) {
+            if (prm.loc_dist) w *= mg::gaspari_cohn<float>((float)prm.loc_dist[e] / hc);
+            w *= pk.y;
+            if (!(w > 0.0f)) keep = false;
+          }
+          if (keep) {
+            sw = sqrtf(w);
+            sd = sw * pk.z;
+          }
         }
-        if (keep && !r_identity) {
-          if (prm.loc_dist) w *= mg::gaspari_cohn<float>((float)prm.loc_dist[e] / hc);
-          w *= (float)prm.rinv[o];
-          if (!(w > 0.0f)) keep = false;
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) V.wcnt[warp] = __popc(bal);
+        __syncthreads();
+        int wb = 0, cnt = 0;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) {
+          if (w < warp) wb += V.wcnt[w];
+          cnt += V.wcnt[w];
         }
         if (keep) {
-          sw = sqrtf(w);
-          sd = sw * (float)prm.dinn[o];
+          const int pos = (head + nsel + wb + __popc(bal & ((1u << lane) - 1u))) & (kSelRing - 1);
+          V.sel_o[pos] = o;
+          V.sel_sw[pos] = sw;
+          V.sel_sd[pos] = sd;
         }
+        __syncthreads();
+        nsel += cnt;
+        nloc += cnt;
+        cpos += kThreads;
       }
-      const unsigned bal = __ballot_sync(0xffffffffu, keep);
-      if (lane == 0) V.wcnt[warp] = __popc(bal);
-      __syncthreads();
-      int wb = 0, cnt = 0;
+      const bool done = cpos >= e1;
+      const int nchunks = done ? (nsel + kChunk - 1) / kChunk : nsel / kChunk;
+      float x[8], sdv;
+      if (nchunks > 0) load_rows(head, nsel < kChunk ? nsel : kChunk, x, sdv);
+      for (int c = 0; c < nchunks; ++c) {
+        const int b = (int)(gchunk % kNBuf);
+        const uint32_t use = gchunk / kNBuf;
+        if (use > 0 && !wait_all(&buf_bar[b], (use - 1) & 1u)) { alive = false; break; }
+        unsigned char* bh = R + b * kGramBuf;
+        unsigned char* bl = bh + kSlabS;
 #pragma unroll
-      for (int w = 0; w < kThreads / 32; ++w) {
-        if (w < warp) wb += V.wcnt[w];
-        cnt += V.wcnt[w];
+        for (int j = 0; j < 8; ++j) {
+          const uint32_t off = sw_off(m0 + j, slot, 128);
+          float h, l;
+          split(x[j], h, l);
+          *reinterpret_cast<float*>(bh + off) = h;
+          *reinterpret_cast<float*>(bl + off) = l;
+        }
+        if (warp == 0) {  // the innovation row
+          const uint32_t off = sw_off(KP, slot, 128);
+          float h, l;
+          split(sdv, h, l);
+          *reinterpret_cast<float*>(bh + off) = h;
+          *reinterpret_cast<float*>(bl + off) = l;
+        }
+        if (c + 1 < nchunks) {  // next chunk's rows in flight during the barrier and the MMAs
+          const int rem = nsel - (c + 1) * kChunk;
+          load_rows(head + (c + 1) * kChunk, rem < kChunk ? rem : kChunk, x, sdv);
+        }
+        operands_ready();
+        if (tid == 0) {
+          tc_fence_after();
+          const uint32_t a = sR + b * kGramBuf;
+          issue3(tmem + kTmGram, a, a + kSlabS, kSlabS, a, a + kSlabS, kSlabS, 1, idescG, nch > 0);
+          mma_commit(&buf_bar[b]);
+        }
+        ++gchunk;
+        ++nch;
       }
-      if (keep) {
-        const int pos = (head + nsel + wb + __popc(bal & ((1u << lane) - 1u))) & (kSelRing - 1);
-        V.sel_o[pos] = o;
-        V.sel_sw[pos] = sw;
-        V.sel_sd[pos] = sd;
-      }
-      __syncthreads();
-      nsel += cnt;
-      nloc += cnt;
-      while (nsel >= kChunk && alive) {
-        alive = emit_chunk(kChunk);
-        nsel -= kChunk;
-      }
-    }
-    if (alive && nsel > 0) {
-      alive = emit_chunk(nsel);
-      nsel = 0;
+      if (!alive) break;
+      head = (head + nchunks * kChunk) & (kSelRing - 1);
+      nsel = (nsel > nchunks * kChunk) ? nsel - nchunks * kChunk : 0;
+      if (done) break;
     }
     if (!alive) break;
 
@@ -384,7 +393,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       for (int e = tid; e < prm.n_var * k; e += kThreads) {
         const int v = e / k, i = e - v * k;
         const int64_t s = base + (int64_t)v * prm.var_stride;
-        prm.Xa[s * k + i] = prm.xmean[s] + (double)Xp[s * k + i] * sr;
+        mg::letkf_store(prm, s * k + i, prm.xmean[s] + (double)Xp[s * k + i] * sr);
       }
       if (tid == 0) atomicAdd(prm.n_empty, 1ull);
       __syncthreads();
@@ -461,22 +470,21 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     const float s = fmaxf(fminf(ninf, fro), 1e-30f);
     const float is = 1.0f / s;
     // M = PAP / s + 1 1^T / k (identity on unused member slots); STACK <- [I; M]
-    // (row-major), TB <- T0 = (3I - M) / 2 stored transposed; e0 = max |M - I|.
-    float e_it = 0.0f;
+    // (row-major), TB <- T0 = (3I - M) / 2 stored transposed.
     if (rowwarp) {
-      float mrow[32], id[32], t[32];
+      float x[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) x[j] = (row == cb + j) ? 1.0f : 0.0f;
+      put_row32(STH, STL, row, cb, 128, x);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int c = cb + j;
-        float m = (row < k && c < k) ? a[j] * is + ik : ((row == c) ? 1.0f : 0.0f);
-        mrow[j] = m;
-        id[j] = (row == c) ? 1.0f : 0.0f;
-        t[j] = 0.5f * (((row == c) ? 3.0f : 0.0f) - m);
-        e_it = fmaxf(e_it, fabsf(m - id[j]));
+        a[j] = (row < k && c < k) ? a[j] * is + ik : ((row == c) ? 1.0f : 0.0f);
       }
-      put_row32(STH, STL, row, cb, 128, id);
-      put_row32(STH, STL, KP + row, cb, 128, mrow);
-      put_col32(TBH, TBL, row, cb, 64, t);
+      put_row32(STH, STL, KP + row, cb, 128, a);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) a[j] = 0.5f * (((row == cb + j) ? 3.0f : 0.0f) - a[j]);
+      put_col32(TBH, TBL, row, cb, 64, a);
     }
 
     // ---------------- 3. coupled Newton-Schulz ----------------
@@ -517,14 +525,13 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
             x[j] = (row < k && c < k) ? (__uint_as_float(v[j]) - ik) * isq : 0.0f;
           }
           put_col32(STH, STL, row, cb, 128, x);
-          uint32_t g[32];
-          tmem_ld32(tmem + tm_row + kTmGram + cb, g);
+          tmem_ld32(tmem + tm_row + kTmGram + cb, v);  // the Gram row again (v is free)
           tmem_wait_ld();
           const float ri = V.r[row];
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int c = cb + j;
-            float av = __uint_as_float(g[j]);
+            float av = __uint_as_float(v[j]);
             if (c == row) av += delta;
             x[j] = (row < k && c < k) ? (av - ri - V.r[c] + cbar) : 0.0f;
           }
@@ -767,8 +774,8 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       if (rowwarp && hh == 0 && row < k) {
         for (int vv = 0; vv < nv; ++vv) {
           const float a2 = rtps ? dv[vv] * (1.0f + V.fac[vv]) : dv[vv];
-          prm.Xa[(base + (int64_t)(v0 + vv) * prm.var_stride) * k + row] =
-              (V.xm[vv] + (double)V.inc[vv]) + (double)a2;
+          mg::letkf_store(prm, (base + (int64_t)(v0 + vv) * prm.var_stride) * k + row,
+                          (V.xm[vv] + (double)V.inc[vv]) + (double)a2);
         }
       }
       __syncthreads();  // TB and the vectors are rewritten by the next tile
@@ -806,19 +813,37 @@ bool letkf_tc_supported(const LetkfParams& prm) {
   return prm.k >= 2 && prm.k <= KP && !chol && !upd && !prm.warm_start && prm.redo_out && prm.n_redo;
 }
 
-int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream) {
+int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream, int* ctas) {
   cudaError_t e = cudaFuncSetAttribute(letkf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kSmemBytes);
   if (e != cudaSuccess) return (int)e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, letkf_tc_kernel, kThreads, kSmemBytes);
+  // The whole unified L1/shared array as shared memory, so two CTAs fit.
+  e = cudaFuncSetAttribute(letkf_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return (int)e;
-  // Two CTAs per SM share its 512 TMEM columns; never more.
+  // CTAs per SM from the SM's shared memory and register file (the design
+  // point is two, which also share the SM's 512 TMEM columns evenly).
+  cudaFuncAttributes fa{};
+  e = cudaFuncGetAttributes(&fa, letkf_tc_kernel);
+  if (e != cudaSuccess) return (int)e;
+  int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
+    return (int)e;
+  if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess)
+    return (int)e;
+  if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess)
+    return (int)e;
+  const size_t per_cta = kSmemBytes + fa.sharedSizeBytes + (size_t)reserved;
+  int per_sm = (int)((size_t)smem_sm / per_cta);
+  const int by_regs = fa.numRegs > 0 ? regs_sm / (fa.numRegs * kThreads) : 2;
+  if (by_regs < per_sm) per_sm = by_regs;
   if (per_sm > 2) per_sm = 2;
   if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
   int64_t grid = (int64_t)per_sm * num_sms;
   if (grid > prm.npoints) grid = prm.npoints;
   if (grid < 1) grid = 1;
+  if (ctas) *ctas = (int)grid;
   letkf_tc_kernel<<<(unsigned)grid, kThreads, kSmemBytes, static_cast<cudaStream_t>(stream)>>>(prm);
   MG_COUNT_LAUNCH();
   return (int)cudaGetLastError();

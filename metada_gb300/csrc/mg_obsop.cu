@@ -43,7 +43,9 @@ __global__ void hx_idw4_kernel(const double* __restrict__ X, int k, int64_t ld, 
 
 // Bilinear in (lon, lat), linear in level; the operation order matches the
 // oracle's restatement exactly.
-__global__ void hx_latlon_kernel(const double* __restrict__ X, int k, int64_t ld, int nlon,
+// TX: the members' storage type (FP64, or FP32 widened to FP64 on load).
+template <typename TX>
+__global__ void hx_latlon_kernel(const TX* __restrict__ X, int k, int64_t ld, int nlon,
                                  int nlat, int nlev, const double* __restrict__ olat,
                                  const double* __restrict__ olon, const double* __restrict__ olev,
                                  const int32_t* __restrict__ ovar, int64_t p,
@@ -80,20 +82,18 @@ __global__ void hx_latlon_kernel(const double* __restrict__ X, int k, int64_t ld
     if (l0 < 0) l0 = 0;
     const double fz = (nlev > 1) ? __dsub_rn(gz, (double)l0) : 0.0;
     const long long l1 = (nlev > 1) ? l0 + 1 : l0;
-    const double* x = X + (int64_t)m * ld + (int64_t)ovar[o] * nlev * plane;
-    const double* lo = x + l0 * plane;
-    const double* hi = x + l1 * plane;
+    const TX* x = X + (int64_t)m * ld + (int64_t)ovar[o] * nlev * plane;
+    const TX* lo = x + l0 * plane;
+    const TX* hi = x + l1 * plane;
     const double ax = __dsub_rn(1.0, fx), ay = __dsub_rn(1.0, fy), az = __dsub_rn(1.0, fz);
-    const double b0 = __dadd_rn(
-        __dmul_rn(__dadd_rn(__dmul_rn(lo[j0 * nlon + i0], ax), __dmul_rn(lo[j0 * nlon + i1], fx)), ay),
-        __dmul_rn(__dadd_rn(__dmul_rn(lo[(j0 + 1) * nlon + i0], ax),
-                            __dmul_rn(lo[(j0 + 1) * nlon + i1], fx)),
-                  fy));
-    const double b1 = __dadd_rn(
-        __dmul_rn(__dadd_rn(__dmul_rn(hi[j0 * nlon + i0], ax), __dmul_rn(hi[j0 * nlon + i1], fx)), ay),
-        __dmul_rn(__dadd_rn(__dmul_rn(hi[(j0 + 1) * nlon + i0], ax),
-                            __dmul_rn(hi[(j0 + 1) * nlon + i1], fx)),
-                  fy));
+    const double l00 = (double)lo[j0 * nlon + i0], l01 = (double)lo[j0 * nlon + i1];
+    const double l10 = (double)lo[(j0 + 1) * nlon + i0], l11 = (double)lo[(j0 + 1) * nlon + i1];
+    const double h00 = (double)hi[j0 * nlon + i0], h01 = (double)hi[j0 * nlon + i1];
+    const double h10 = (double)hi[(j0 + 1) * nlon + i0], h11 = (double)hi[(j0 + 1) * nlon + i1];
+    const double b0 = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(l00, ax), __dmul_rn(l01, fx)), ay),
+                                __dmul_rn(__dadd_rn(__dmul_rn(l10, ax), __dmul_rn(l11, fx)), fy));
+    const double b1 = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(h00, ax), __dmul_rn(h01, fx)), ay),
+                                __dmul_rn(__dadd_rn(__dmul_rn(h10, ax), __dmul_rn(h11, fx)), fy));
     HX[e] = __dadd_rn(__dmul_rn(b0, az), __dmul_rn(b1, fz));
   }
 }
@@ -170,9 +170,25 @@ int mg_hx_latlon(mg_context* ctx, const double* X, int32_t k, int64_t ld, int32_
                    nlat > 1 && nlev > 0 && p >= 0,
                "mg_hx_latlon: bad arguments");
   if (p == 0) return MG_OK;
-  hx_latlon_kernel<<<grid_for(p * k, 256), 256, 0, ctx->stream>>>(X, k, ld, nlon, nlat, nlev,
-                                                                  obs_lat, obs_lon, obs_lev,
-                                                                  obs_var, p, HX);
+  hx_latlon_kernel<double><<<grid_for(p * k, 256), 256, 0, ctx->stream>>>(X, k, ld, nlon, nlat, nlev,
+                                                                          obs_lat, obs_lon, obs_lev,
+                                                                          obs_var, p, HX);
+  MG_COUNT_LAUNCH();
+  MG_TRY_CUDA(cudaGetLastError());
+  return MG_OK;
+}
+
+int mg_hx_latlon_f32(mg_context* ctx, const float* X, int32_t k, int64_t ld, int32_t nlon,
+                     int32_t nlat, int32_t nlev, const double* obs_lat, const double* obs_lon,
+                     const double* obs_lev, const int32_t* obs_var, int64_t p, double* HX) {
+  if (!ctx) return MG_ERR_ARG;
+  MG_CHECK_ARG(X && obs_lat && obs_lon && obs_lev && obs_var && HX && k > 0 && nlon > 0 &&
+                   nlat > 1 && nlev > 0 && p >= 0,
+               "mg_hx_latlon_f32: bad arguments");
+  if (p == 0) return MG_OK;
+  hx_latlon_kernel<float><<<grid_for(p * k, 256), 256, 0, ctx->stream>>>(X, k, ld, nlon, nlat, nlev,
+                                                                         obs_lat, obs_lon, obs_lev,
+                                                                         obs_var, p, HX);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   return MG_OK;

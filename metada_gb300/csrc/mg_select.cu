@@ -29,7 +29,7 @@ namespace {
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kEarthKm = 6371.0;
 constexpr int kNBand = 180, kNLonCell = 360, kNCell = kNBand * kNLonCell;
-constexpr int kMaxList = 16384;   // longest per-column list sorted in shared memory
+constexpr int kMaxList = 32768;   // longest per-column list sorted in shared memory (128 KB)
 constexpr int kBorderCap = 65536; // near-threshold pairs re-decided on the host
 constexpr double kBorderRel = 1e-9;
 
@@ -268,7 +268,10 @@ __global__ void __launch_bounds__(256) geo_count_kernel(
   });
   atomicAdd(&scount, mine);
   __syncthreads();
-  if (threadIdx.x == 0) counts[col] = (int64_t)scount;
+  if (threadIdx.x == 0) {
+    counts[col] = (int64_t)scount;
+    atomicMax(nborder + 1, scount);  // the longest list sizes the fill pass's shared memory
+  }
 }
 
 __global__ void apply_rejections_kernel(const unsigned long long* __restrict__ rej, int nrej,
@@ -284,8 +287,8 @@ __global__ void __launch_bounds__(256) geo_fill_kernel(
     const int64_t* __restrict__ offsets, const unsigned long long* __restrict__ rej, int nrej,
     const double* __restrict__ obs_lat, const double* __restrict__ obs_lon, const double* __restrict__ oux,
     const double* __restrict__ ouy, const double* __restrict__ ouz, int32_t* __restrict__ idx,
-    double* __restrict__ dist, int* __restrict__ overflow) {
-  extern __shared__ int32_t slist[];  // capacity: next power of two >= kMaxList
+    double* __restrict__ dist, int* __restrict__ overflow, int list_cap) {
+  extern __shared__ int32_t slist[];  // list_cap entries, a power of two
   __shared__ int scount;
   __shared__ ColPlan pl;
   __shared__ int64_t run_lo[kMaxRuns], run_hi[kMaxRuns];
@@ -293,7 +296,7 @@ __global__ void __launch_bounds__(256) geo_fill_kernel(
   const int64_t base = offsets[col];
   const int64_t n = offsets[col + 1] - base;
   if (n == 0) return;
-  if (n > kMaxList) {
+  if (n > list_cap) {
     if (threadIdx.x == 0) atomicExch(overflow, 1);
     return;
   }
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(256) geo_fill_kernel(
     const int32_t o = co.obs[t];
     if (cls == 0 && nrej > 0 && key_rejected(rej, nrej, ((unsigned long long)col << 32) | (unsigned)o)) return;
     const int pos = atomicAdd(&scount, 1);
-    if (pos < kMaxList) slist[pos] = o;
+    if (pos < list_cap) slist[pos] = o;
   });
   __syncthreads();
   const int cnt = scount;
@@ -472,9 +475,12 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
                                                   nborder);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
-  unsigned long long nb = 0;
-  MG_TRY_CUDA(cudaMemcpyAsync(&nb, nborder, sizeof(nb), cudaMemcpyDeviceToHost, s));
+  unsigned long long nbm[2] = {0, 0};
+  MG_TRY_CUDA(cudaMemcpyAsync(nbm, nborder, sizeof(nbm), cudaMemcpyDeviceToHost, s));
   MG_TRY_CUDA(cudaStreamSynchronize(s));
+  const unsigned long long nb = nbm[0], longest = nbm[1];
+  if (longest > (unsigned long long)kMaxList)
+    return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_geo: a local list exceeds 32768 obs");
   if (nb > (unsigned long long)kBorderCap)
     return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_geo: too many near-threshold pairs");
   int nrej = 0;
@@ -502,19 +508,20 @@ int mg_select_geo(mg_context* ctx, const double* col_lat, const double* col_lon,
     return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_geo: index buffer too small");
   if (*total == 0) return MG_OK;
   // Pass 2: fill, sort each list by obs index, distances.
-  int smem_entries = 1;
-  while (smem_entries < kMaxList) smem_entries <<= 1;
+  int smem_entries = 32;
+  while ((unsigned long long)smem_entries < longest) smem_entries <<= 1;
   const size_t smem = sizeof(int32_t) * smem_entries;
   MG_TRY_CUDA(cudaFuncSetAttribute(geo_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
   geo_fill_kernel<<<(unsigned)ncol, 256, smem, s>>>(col_lat, col_lon, ncol, radius_km, cstart, co, offsets, rej,
-                                                    nrej, obs_lat, obs_lon, oux, ouy, ouz, idx, dist_km, overflow);
+                                                    nrej, obs_lat, obs_lon, oux, ouy, ouz, idx, dist_km, overflow,
+                                                    smem_entries);
   MG_COUNT_LAUNCH();
   MG_TRY_CUDA(cudaGetLastError());
   int ovf = 0;
   MG_TRY_CUDA(cudaMemcpyAsync(&ovf, overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
   MG_TRY_CUDA(cudaStreamSynchronize(s));
-  if (ovf == 1) return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_geo: a local list exceeds 16384 obs");
+  if (ovf == 1) return mg::fail(ctx, MG_ERR_CAPACITY, "mg_select_geo: a local list exceeds its sort buffer");
   if (ovf == 2) return mg::fail(ctx, MG_ERR_NUMERIC, "mg_select_geo: count and fill passes disagree");
   return MG_OK;
 }

@@ -198,12 +198,16 @@ def hx_idw4(X: torch.Tensor, nx: int, ny: int, obs_xy: torch.Tensor,
 
 def hx_latlon(X: torch.Tensor, nlon: int, nlat: int, nlev: int, obs_lat: torch.Tensor,
               obs_lon: torch.Tensor, obs_lev: torch.Tensor, obs_var: torch.Tensor) -> torch.Tensor:
-    _need(X, torch.float64, "X")
+    if X.dtype != torch.float32:
+        _need(X, torch.float64, "X")
+    else:
+        _need(X, torch.float32, "X")
     _need(obs_var, torch.int32, "obs_var")
     k, n = X.shape
     p = obs_lat.shape[0]
     HX = torch.empty((p, k), dtype=torch.float64, device=X.device)
-    context(X.device.index).call("mg_hx_latlon", _ptr(X), k, n, nlon, nlat, nlev, _ptr(obs_lat),
+    fn = "mg_hx_latlon_f32" if X.dtype == torch.float32 else "mg_hx_latlon"
+    context(X.device.index).call(fn, _ptr(X), k, n, nlon, nlat, nlev, _ptr(obs_lat),
                                  _ptr(obs_lon), _ptr(obs_lev), _ptr(obs_var), p, _ptr(HX))
     return HX
 
@@ -290,12 +294,18 @@ def letkf_batched(X: torch.Tensor, *, col_base: torch.Tensor, nlev: int, n_var: 
                   obs_lev: torch.Tensor | None = None, hsupport: float = 0.0, vsupport: float = 0.0,
                   rho: float = 1.0, flags: int = 0, precision: int = _lib.MG_PREC_FP64,
                   want_mean: bool = True) -> tuple[torch.Tensor | None, LetkfStats]:
-    """Batched LETKF in place on X (k x n)."""
-    _need(X, torch.float64, "X")
+    """Batched LETKF in place on X (k x n, float64, or float32 with the mixed
+    precision path)."""
+    if X.dtype == torch.float32:
+        if precision != _lib.MG_PREC_MIXED:
+            raise TypeError("X: float32 members need precision=MG_PREC_MIXED")
+    else:
+        _need(X, torch.float64, "X")
     k, n = X.shape
     mean = torch.empty(n, dtype=torch.float64, device=X.device) if want_mean else None
     d = LetkfDesc()
     d.X = X.data_ptr()
+    d.x_dtype = _lib.MG_DTYPE_F32 if X.dtype == torch.float32 else _lib.MG_DTYPE_F64
     d.n = n
     d.ld = n
     d.k = k

@@ -407,3 +407,122 @@ def column_letkf_case(nlon: int = 720, nlat: int = 360, nlev: int = 30, k: int =
     yo = y + so * g2.standard_normal(p)
     return ColumnLetkfCase(nlon, nlat, nlev, op, truth, np.ascontiguousarray(X), obs_col, obs_ch, yo, so,
                            hsupport_km, float_config(rho))
+
+
+# ------------------------------------------------ high-resolution case ----
+@dataclass
+class HighResCase:
+    """The high-resolution LETKF configuration, generated on the GPU: members
+    stored as FP32 (k x n), obs positions, levels, variables and values as
+    device tensors."""
+    nlon: int
+    nlat: int
+    nlev: int
+    nvar: int
+    X: "object"         # torch float32 (k, n), member-major
+    truth: "object"     # torch float64 (n,)
+    obs_lat: "object"
+    obs_lon: "object"
+    obs_lev: "object"
+    obs_var: "object"   # int32
+    yo: "object"
+    sigma_o: float
+    hsupport_km: float
+    vsupport: float
+    rho: float
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return self.nvar * self.nlev * self.nlat * self.nlon
+
+    def col_lat_lon(self) -> tuple[np.ndarray, np.ndarray]:
+        return LatLonCase.col_lat_lon(self)  # same cell-centred grid
+
+    def col_base(self) -> np.ndarray:
+        return np.arange(self.nlat * self.nlon, dtype=np.int64)
+
+    @property
+    def lev_stride(self) -> int:
+        return self.nlat * self.nlon
+
+    @property
+    def var_stride(self) -> int:
+        return self.nlev * self.nlat * self.nlon
+
+
+def grf_fields_gpu(count: int, nlat: int, nlon: int, length_cells: float, gen, device):
+    """`count` unit-variance Gaussian random fields on the nlat x nlon grid
+    with squared-exponential covariance of the given length (in cells):
+    white noise filtered in the 2-D Fourier domain by the square root of the
+    covariance's spectrum (periodic in both directions), as float32."""
+    import torch
+
+    fy = torch.fft.fftfreq(nlat, device=device, dtype=torch.float64)
+    fx = torch.fft.rfftfreq(nlon, device=device, dtype=torch.float64)
+    amp = torch.exp(-(np.pi ** 2) * length_cells ** 2 * (fy[:, None] ** 2 + fx[None, :] ** 2))
+    # unit variance: with orthonormal transforms the output variance is the
+    # mean of |H|^2 over the full (two-sided) spectrum
+    w = torch.ones_like(amp)
+    w[:, 1:(nlon + 1) // 2] = 2.0  # rfft columns that stand for two frequencies
+    var = float((w * amp * amp).sum() / (nlat * nlon))
+    amp = (amp / np.sqrt(var)).to(torch.complex64)
+    noise = torch.randn((count, nlat, nlon), generator=gen, device=device, dtype=torch.float32)
+    spec = torch.fft.rfft2(noise, norm="ortho") * amp
+    return torch.fft.irfft2(spec, s=(nlat, nlon), norm="ortho")
+
+
+def highres_letkf_case(device, nlon: int = 1440, nlat: int = 720, nlev: int = 30, nvar: int = 4, k: int = 80,
+                       p: int = 5_000_000, clustered: float = 0.6, n_patches: int = 20, patch_km: float = 800.0,
+                       length_cells: float = 8.0, alpha_v: float = 0.7, sigma_o: float = 1.0,
+                       hsupport_km: float = 300.0, vsupport: float = 2.0, rho: float = 0.9,
+                       seed: int = 20261203 + 300) -> HighResCase:
+    """High-resolution LETKF configuration: truth and members (truth plus an
+    independent draw of the same field) from squared-exponential Gaussian
+    random fields with AR(1) vertical correlation, members kept in FP32;
+    p point obs, a fraction `clustered` in n_patches Gaussian patches
+    (standard deviation patch_km), the rest uniform on the sphere, at
+    uniform random levels and variables, y = H(truth) + N(0, sigma_o^2)."""
+    import torch
+
+    from . import kernels as K
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    n = nvar * nlev * nlat * nlon
+    s = float(np.sqrt(1.0 - alpha_v * alpha_v))
+
+    def draw():  # (nvar, nlev, nlat, nlon) float32, AR(1) in the vertical
+        F = grf_fields_gpu(nvar * nlev, nlat, nlon, length_cells, g, device).view(nvar, nlev, nlat, nlon)
+        for l in range(1, nlev):
+            F[:, l] = alpha_v * F[:, l - 1] + s * F[:, l]
+        return F.reshape(-1)
+
+    truth32 = draw()
+    X = torch.empty((k, n), dtype=torch.float32, device=device)
+    for i in range(k):
+        X[i] = truth32 + draw()
+    truth = truth32.double()
+    # observations
+    rng_ = np.random.default_rng(seed + 1)
+    lat = np.rad2deg(np.arcsin(rng_.uniform(-1.0, 1.0, p)))
+    lon = rng_.uniform(0.0, 360.0, p)
+    nc = int(round(clustered * p))
+    if nc > 0:
+        clat = np.rad2deg(np.arcsin(rng_.uniform(-0.9, 0.9, n_patches)))
+        clon = rng_.uniform(0.0, 360.0, n_patches)
+        which = rng_.integers(0, n_patches, nc)
+        s_deg = np.rad2deg(patch_km / 6371.0)
+        lat[:nc] = np.clip(clat[which] + s_deg * rng_.standard_normal(nc), -89.9, 89.9)
+        lon[:nc] = np.mod(clon[which] + s_deg * rng_.standard_normal(nc) / np.cos(np.deg2rad(clat[which])), 360.0)
+    lev = rng_.uniform(0.0, nlev - 1.0, p)
+    var = rng_.integers(0, nvar, p).astype(np.int32)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)  # noqa: E731
+    olat, olon, olev, ovar = T(lat), T(lon), T(lev), T(var)
+    so = float_config(sigma_o)
+    hx_truth = K.hx_latlon(truth[None, :].contiguous(), nlon, nlat, nlev, olat, olon, olev, ovar)[:, 0]
+    yo = hx_truth + so * T(rng_.standard_normal(p))
+    return HighResCase(nlon, nlat, nlev, nvar, X, truth, olat, olon, olev, ovar, yo, so, hsupport_km, vsupport,
+                       float_config(rho), meta={"length_cells": length_cells, "alpha_v": alpha_v,
+                                                "clustered": clustered, "n_patches": n_patches,
+                                                "patch_km": patch_km, "seed": seed})

@@ -55,7 +55,7 @@ def _gather(X, c, base):
 def test_tensor_path_matches_oracle_and_simt(dev, k):
     c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=5, nvar=2, k=k, p=20_000, T=20, case=41)
     got, HX, off, idx, dist, st = _run(dev, c)
-    assert st.tensor_path == 1
+    assert st.tensor_path == 1 and st.tensor_ctas >= torch.cuda.get_device_properties(dev).multi_processor_count
     assert st.n_fallback == 0 and 0.0 < st.max_residual < 5e-3
     assert st.total_sweeps > 0 and st.max_sweeps <= 14
     cols = np.arange(c.nlat * c.nlon)
@@ -99,4 +99,49 @@ def test_tensor_path_uneven_clustered_lists(dev):
     assert st.tensor_path == 1 and st.n_fallback <= st.n_points // 1000
     cols = np.concatenate([np.argsort(counts)[-60:], np.random.default_rng(1).choice(c.nlat * c.nlon, 60)])
     base, want = _oracle(c, HX, off, idx, dist, cols, 0)
+    assert rel_err(_gather(got, c, base), want) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("k", [64, 80])
+def test_fp32_member_storage_highres_shape(dev, k):
+    """The high-resolution configuration's analysis at reduced size with the
+    members stored as FP32: 60 % of the obs in Gaussian patches, 300 km
+    support, RTPS 0.9; k = 64 runs the tensor-core kernel, k = 80 the SIMT
+    kernel.  H(X) of the FP32 members is bit-identical to the oracle's on the
+    widened values; the analysis of sampled columns (the longest lists among
+    them) matches the oracle run on its own lists and H(X)."""
+    c = syn.latlon_letkf_case(nlon=144, nlat=72, nlev=6, nvar=3, k=k, p=60_000, T=40, hsupport_km=300.0,
+                              rho=0.9, case=45, clustered=0.6)
+    X32 = T(c.X, dev).float().contiguous()
+    Xw = X32.double().cpu().numpy()  # the background the FP32 path sees
+    olat, olon, olev = T(c.obs_lat, dev), T(c.obs_lon, dev), T(c.obs_lev, dev)
+    HX = K.hx_latlon(X32, c.nlon, c.nlat, c.nlev, olat, olon, olev, T(c.obs_var, dev))
+    clat, clon = c.col_lat_lon()
+    off, idx, dist = K.select_geo(T(clat, dev), T(clon, dev), olat, olon, c.hsupport_km)
+    yo = T(c.yo, dev)
+    _, st = K.letkf_batched(X32, col_base=T(c.col_base(), dev), nlev=c.nlev, n_var=c.nvar,
+                            lev_stride=c.lev_stride, var_stride=c.var_stride, HX=HX, yo=yo,
+                            rvar=torch.full_like(yo, c.sigma_o ** 2), loc_off=off, loc_idx=idx, loc_dist=dist,
+                            obs_lev=olev, hsupport=c.hsupport_km, vsupport=c.vsupport, rho=c.rho,
+                            flags=_lib.MG_RTPS, precision=_lib.MG_PREC_MIXED, want_mean=False)
+    assert X32.dtype == torch.float32
+    assert st.tensor_path == (1 if k <= 64 else 0)
+    counts = np.diff(off.cpu().numpy())
+    assert counts.max() > 8 * max(1.0, np.median(counts))
+    cols = np.unique(np.concatenate([np.argsort(counts)[-20:],
+                                     np.random.default_rng(2).choice(c.nlat * c.nlon, 100, replace=False)]))
+    offc, idxc, distc = ob.select_geo(clat[cols], clon[cols], c.obs_lat, c.obs_lon, c.hsupport_km)
+    need = np.unique(idxc)
+    HXc = ob.hx_latlon(Xw, c.nlon, c.nlat, c.nlev, c.obs_lat[need], c.obs_lon[need], c.obs_lev[need],
+                       c.obs_var[need])
+    assert np.array_equal(HX.cpu().numpy()[need], HXc)
+    HXo = np.zeros((c.yo.size, k))
+    HXo[need] = HXc
+    offo = np.zeros(c.nlat * c.nlon + 1, dtype=np.int64)
+    offo[cols + 1] = np.diff(offc)
+    offo = np.cumsum(offo)
+    pts, poff, pidx, pw = point_lists(cols, c.nlev, offo, idxc, distc, c.obs_lev, c.hsupport_km, c.vsupport)
+    base = c.col_base()[pts[:, 0]] + pts[:, 1] * c.lev_stride
+    want = ob.letkf_points(Xw, base, c.nvar, c.var_stride, HXo, c.yo, c.rvar, poff, pidx, pw, c.rho, ob.ORC_RTPS)
+    got = X32.double().cpu().numpy()
     assert rel_err(_gather(got, c, base), want) <= MIXED_TOL

@@ -57,10 +57,17 @@ def test_reference_arm_prints_once_under_torchrun():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"), "--impl", "reference", "--gpus", "2",
            "--steps", "1", "--warmup", "0", "--cpu-points", "200"]
+    import time
+
+    t0 = time.perf_counter()
     p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    wall = time.perf_counter() - t0
     assert p.returncode == 0, p.stderr[-2000:]
     lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    # the printed step time is the sample step that ran, so the steps fit in the run
+    assert 0 < line["ms_per_step"] * line["steps"] / 1e3 <= wall
+    assert "local analyses" in line["config"]["step"]
