@@ -422,6 +422,17 @@ typedef struct mg_letkf_stats {
 } mg_letkf_stats;
 int mg_letkf_last_stats(const mg_context* ctx, mg_letkf_stats* stats);
 
+/* State vector arithmetic on the device, for the device-resident state
+ * backend (SimpleState::add / subtract / multiply / dot, SimpleState.hpp:96-140):
+ * y[i] += x[i] (subtract = 0) or y[i] -= x[i] (subtract != 0), and
+ * y[i] *= a, one IEEE operation per element, so the results equal the
+ * reference's host loops bit for bit.  mg_vec_dot sums in a fixed
+ * (deterministic) order that differs from the reference's sequential one;
+ * *result is host memory and the call synchronises the stream. */
+int mg_vec_update(mg_context* ctx, double* y, const double* x, int64_t n, int32_t subtract);
+int mg_vec_scale(mg_context* ctx, double* y, int64_t n, double a);
+int mg_vec_dot(mg_context* ctx, const double* x, const double* y, int64_t n, double* result);
+
 /* Number of kernels this context has launched since creation (host). */
 int64_t mg_kernel_launches(const mg_context* ctx);
 

@@ -42,6 +42,8 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "runtime.hpp"
@@ -182,6 +184,53 @@ void scatter_members(Ens& ens, const std::vector<double>& host, int k, size_t n)
   }
 }
 
+// Members whose backend keeps its data on the device (DeviceState, the
+// Gb300BackendTag state): the analysis reads and writes them device to device.
+template <typename M>
+concept DeviceMember = requires(M& m) {
+  { m.backend().device_data() } -> std::convertible_to<double*>;
+};
+
+template <typename Ens>
+constexpr bool device_members() {
+  return DeviceMember<std::remove_reference_t<decltype(std::declval<Ens&>().GetMember(0))>>;
+}
+
+// Members into (from) the k x n member-major device matrix X: device copies
+// when the members live on the device, else a host gather and one upload.
+template <typename Ens>
+void load_members(Ens& ens, DeviceBuffer<double>& X, std::vector<double>& host, int k, size_t n, cudaStream_t s) {
+  if constexpr (device_members<Ens>()) {
+    X.resize((size_t)k * n);
+    for (int i = 0; i < k; ++i) {
+      auto& m = ens.GetMember(i);
+      if (m.size() != n) throw std::runtime_error("ensemble members differ in size");
+      cuda_check(cudaMemcpyAsync(X.data() + (size_t)i * n, m.backend().device_data(), n * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, s),
+                 "member gather");
+    }
+  } else {
+    gather_members(ens, host, k, n);
+    X.upload(host, s);
+  }
+}
+
+template <typename Ens>
+void store_members(Ens& ens, const DeviceBuffer<double>& X, std::vector<double>& host, int k, size_t n,
+                   cudaStream_t s) {
+  if constexpr (device_members<Ens>()) {
+    for (int i = 0; i < k; ++i)
+      cuda_check(cudaMemcpyAsync(ens.GetMember(i).backend().device_data(), X.data() + (size_t)i * n,
+                                 n * sizeof(double), cudaMemcpyDeviceToDevice, s),
+                 "member scatter");
+    cuda_check(cudaStreamSynchronize(s), "member scatter sync");
+  } else {
+    host.resize((size_t)k * n);
+    X.download(host.data(), host.size(), s);
+    scatter_members(ens, host, k, n);
+  }
+}
+
 // HX (p x k) for the raw members: on the device (IDW4 for grid obs) or via
 // the bound operator on the host (ETKF.hpp:128-132).
 template <typename Ens, typename Obs, typename H>
@@ -234,21 +283,19 @@ class ETKF {
     // (ETKF.hpp:111-112, 190-191).
     ens.RecomputeMean();
     std::vector<double> host;
-    detail::gather_members(ens, host, k, n);
+    DeviceBuffer<double> X, HX, yo, rvar;
+    detail::load_members(ens, X, host, k, n, ctx_->stream());
     const detail::HostObs ho = detail::collect_obs(obs);
     detail::HostGrid grid;
     const bool have_grid = ho.grid && ens.GetMember(0).geometry() != nullptr;
     if (have_grid) grid = detail::collect_grid(*ens.GetMember(0).geometry());
-    DeviceBuffer<double> X, HX, yo, rvar;
-    X.upload(host, ctx_->stream());
     detail::obs_space(*ctx_, ens, obs, op, ho, have_grid ? &grid : nullptr, X, k, n, settings_.host_h, HX);
     yo.upload(ho.yo, ctx_->stream());
     rvar.upload(ho.rvar, ctx_->stream());
     ctx_->check(mg_etkf(ctx_->get(), X.data(), (int64_t)n, k, (int64_t)n, HX.data(), yo.data(), rvar.data(),
                         (int64_t)ho.size(), settings_.inflation, settings_.flags, settings_.precision, nullptr),
                 "mg_etkf");
-    X.download(host.data(), host.size(), ctx_->stream());
-    detail::scatter_members(ens, host, k, n);
+    detail::store_members(ens, X, host, k, n, ctx_->stream());
   }
 
   template <typename Ens>
@@ -292,9 +339,8 @@ class LETKF {
     const size_t npt = grid.grid ? (size_t)grid.nx * grid.ny : grid.lat.size();
     if (npt != n) throw std::runtime_error("LETKF: one state value per geometry point is required");
     std::vector<double> host;
-    detail::gather_members(ens, host, k, n);
     DeviceBuffer<double> X, yo, rvar;
-    X.upload(host, ctx_->stream());
+    detail::load_members(ens, X, host, k, n, ctx_->stream());
     yo.upload(ho.yo, ctx_->stream());
     rvar.upload(ho.rvar, ctx_->stream());
     const int64_t p = (int64_t)ho.size();
@@ -372,8 +418,7 @@ class LETKF {
       ctx_->check(mg_letkf_batched(ctx_->get(), &d), "mg_letkf_batched");
       ctx_->check(mg_letkf_last_stats(ctx_->get(), &stats_), "mg_letkf_last_stats");
     }
-    X.download(host.data(), host.size(), ctx_->stream());
-    detail::scatter_members(ens, host, k, n);
+    detail::store_members(ens, X, host, k, n, ctx_->stream());
     ens.RecomputeMean();  // LETKF.hpp:116
   }
 
@@ -450,7 +495,12 @@ class EnKF {
     const int k = static_cast<int>(ens.Size());
     const size_t n = ens.GetMember(0).size();
     std::vector<double> host;
-    detail::gather_members(ens, host, k, n);
+    DeviceBuffer<double> X, HX, yo, rvar, E, Xb;
+    detail::load_members(ens, X, host, k, n, ctx_->stream());
+    Xb.resize(X.size());
+    cuda_check(cudaMemcpyAsync(Xb.data(), X.data(), X.size() * sizeof(double), cudaMemcpyDeviceToDevice,
+                               ctx_->stream()),
+               "background copy");
     const detail::HostObs ho = detail::collect_obs(obs);
     detail::HostGrid grid;
     const bool have_grid = ho.grid && ens.GetMember(0).geometry() != nullptr;
@@ -470,8 +520,6 @@ class EnKF {
         for (int j = 0; j < k; ++j) eps[o * k + j] = sd * dist(gen);
       }
     }
-    DeviceBuffer<double> X, HX, yo, rvar, E;
-    X.upload(host, ctx_->stream());
     detail::obs_space(*ctx_, ens, obs, op, ho, have_grid ? &grid : nullptr, X, k, n, settings_.host_h, HX);
     yo.upload(ho.yo, ctx_->stream());
     rvar.upload(ho.rvar, ctx_->stream());
@@ -480,13 +528,13 @@ class EnKF {
     ctx_->check(mg_enkf(ctx_->get(), X.data(), (int64_t)n, k, (int64_t)n, HX.data(), yo.data(), rvar.data(),
                         E.data(), (int64_t)p, settings_.inflation, settings_.precision, nullptr, &d),
                 "mg_enkf");
-    std::vector<double> before = host;
-    X.download(host.data(), host.size(), ctx_->stream());
-    detail::scatter_members(ens, host, k, n);
+    // analysis increment norm on the device: || X_a - X_b ||
+    ctx_->check(mg_vec_update(ctx_->get(), Xb.data(), X.data(), (int64_t)X.size(), 1), "mg_vec_update");
+    double inc = 0.0;
+    ctx_->check(mg_vec_dot(ctx_->get(), Xb.data(), Xb.data(), (int64_t)Xb.size(), &inc), "mg_vec_dot");
+    detail::store_members(ens, X, host, k, n, ctx_->stream());
     ens.RecomputeMean();  // EnKF.hpp:237-238
     ens.RecomputePerturbations();
-    double inc = 0.0;
-    for (size_t i = 0; i < host.size(); ++i) inc += (host[i] - before[i]) * (host[i] - before[i]);
     const double nan = std::numeric_limits<double>::quiet_NaN();
     results_ = AnalysisResults{d.innovation_norm, std::sqrt(inc), d.background_spread, d.analysis_spread, nan, nan,
                                nan, k, (int)p, method_, settings_.inflation};

@@ -154,6 +154,9 @@ _SIGNATURES = {
     "mg_letkf_batched": [c_void_p, POINTER(LetkfDesc)],
     "mg_letkf_last_stats": [c_void_p, POINTER(LetkfStats)],
     "mg_kernel_launches": [c_void_p],
+    "mg_vec_update": [c_void_p, c_void_p, c_void_p, c_int64, c_int32],
+    "mg_vec_scale": [c_void_p, c_void_p, c_int64, c_double],
+    "mg_vec_dot": [c_void_p, c_void_p, c_void_p, c_int64, POINTER(c_double)],
     "mg_etkf_batch_create": [c_void_p, c_void_p, c_int32, c_int32, c_int32, POINTER(c_void_p)],
     "mg_etkf_batch_autotune": [c_void_p, c_void_p, POINTER(c_int32), POINTER(c_int32)],
     "mg_etkf_batch_run": [c_void_p, c_void_p],
