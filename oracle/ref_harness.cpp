@@ -10,6 +10,7 @@
 //
 // usage: ref_harness etkf|letkf|enkf NX NY K ENS_PREFIX OBS_FILE ERROR
 //                    INFLATION RADIUS OUT_DIR [SEED]
+//        ref_harness nearest IN_FILE OUT_FILE   (see nearest::run)
 //   reads ENS_PREFIX<i>.txt (i = 1..K, SimpleState text) and OBS_FILE
 //   (GridObservation text format, grid coordinates); writes the analysed
 //   members as raw little-endian doubles to OUT_DIR/member_<i>.bin
@@ -57,9 +58,94 @@ struct harness_seeded_device {
 #include "Logger.hpp"
 #include "ObsOperator.hpp"
 #include "Observation.hpp"
+#include "IdentityObsOperator.hpp"
+#include "PointObservation.hpp"
 
 namespace fw = metada::framework;
 using Tag = harness::HarnessBackendTag;
+
+// ---- nearest-node mode: the reference's IdentityObsOperator::apply on a
+// WRF-style geometry, reaching its geographic branch
+// (convertGeographicToGrid, IdentityObsOperator.hpp:484-505 and the vertical
+// search below it).  The state holds the node's linear index
+// i + nx (j + ny k); at an exact node the 1e12 weight makes apply() return
+// that index (the other neighbours add less than 1e-6), so the rounded
+// result names the node the reference chose.
+namespace nearest {
+
+struct GridInfo {  // the members convertGeographicToGrid reads
+  size_t nx = 0, ny = 0;
+  std::vector<double> latitude_2d, longitude_2d, vertical_coords;
+  bool has_2d_coords() const { return !latitude_2d.empty(); }
+  bool has_vertical_coords() const { return !vertical_coords.empty(); }
+};
+
+struct Geometry {
+  GridInfo info;
+  const GridInfo& unstaggered_info() const { return info; }
+  size_t x_dim() const { return info.nx; }
+  size_t y_dim() const { return info.ny; }
+  size_t z_dim() const { return info.vertical_coords.empty() ? 1 : info.vertical_coords.size(); }
+  // The operator's generic fallback (not reached: the grid has 2-D coordinates).
+  fw::Location getLocation(int i, int j, int) const {
+    const size_t t = (size_t)j * info.nx + (size_t)i;
+    return fw::Location(info.latitude_2d[t], info.longitude_2d[t], 0.0, fw::CoordinateSystem::GEOGRAPHIC);
+  }
+};
+
+struct State {
+  const Geometry* g;
+  std::vector<double> data;
+  const Geometry& geometry() const { return *g; }
+  std::vector<double> getVariable(const std::string&) const { return data; }
+};
+
+using Obs = std::vector<fw::ObservationPoint>;
+using Op = metada::backends::common::obsoperator::IdentityObsOperator<State, Obs, int>;
+
+// IN: int64 nx, ny, nz, p; doubles lat2d[nx*ny], lon2d[nx*ny], vcoord[nz],
+// obs_lat[p], obs_lon[p], obs_level[p].  OUT: int64 (i, j, k) per obs.
+int run(const std::string& in, const std::string& out) {
+  std::ifstream f(in, std::ios::binary);
+  if (!f) throw std::runtime_error("cannot read " + in);
+  int64_t hdr[4];
+  f.read(reinterpret_cast<char*>(hdr), sizeof(hdr));
+  const size_t nx = (size_t)hdr[0], ny = (size_t)hdr[1], nz = (size_t)hdr[2], p = (size_t)hdr[3];
+  auto rd = [&](size_t n) {
+    std::vector<double> v(n);
+    f.read(reinterpret_cast<char*>(v.data()), (std::streamsize)(n * sizeof(double)));
+    return v;
+  };
+  Geometry geo;
+  geo.info.nx = nx;
+  geo.info.ny = ny;
+  geo.info.latitude_2d = rd(nx * ny);
+  geo.info.longitude_2d = rd(nx * ny);
+  geo.info.vertical_coords = rd(nz);
+  const auto olat = rd(p), olon = rd(p), olev = rd(p);
+  if (!f) throw std::runtime_error("short input " + in);
+  const size_t nzz = geo.z_dim();
+  State st{&geo, std::vector<double>(nx * ny * nzz)};
+  for (size_t t = 0; t < st.data.size(); ++t) st.data[t] = (double)t;
+  Obs obs;
+  for (size_t o = 0; o < p; ++o)
+    obs.emplace_back(fw::Location(olat[o], olon[o], olev[o], fw::CoordinateSystem::GEOGRAPHIC), 0.0, 1.0);
+  harness::MapConfig cfg(fw::ConfigMap{});
+  Op op(cfg);
+  const std::vector<double> h = op.apply(st, obs);
+  std::vector<int64_t> ijk(3 * p);
+  for (size_t o = 0; o < p; ++o) {
+    const int64_t id = (int64_t)std::llround(h[o]);
+    ijk[3 * o] = id % (int64_t)nx;
+    ijk[3 * o + 1] = (id / (int64_t)nx) % (int64_t)ny;
+    ijk[3 * o + 2] = id / (int64_t)(nx * ny);
+  }
+  std::ofstream fo(out, std::ios::binary);
+  fo.write(reinterpret_cast<const char*>(ijk.data()), (std::streamsize)(ijk.size() * sizeof(int64_t)));
+  return fo ? 0 : 1;
+}
+
+}  // namespace nearest
 
 static void dump(const std::string& path, const double* p, size_t n) {
   std::ofstream f(path, std::ios::binary);
@@ -69,6 +155,7 @@ static void dump(const std::string& path, const double* p, size_t n) {
 
 int main(int argc, char** argv) {
   try {
+    if (argc == 4 && std::string(argv[1]) == "nearest") return nearest::run(argv[2], argv[3]);
     if (argc != 11 && argc != 12) {
       std::cerr << "usage: ref_harness etkf|letkf|enkf NX NY K ENS_PREFIX OBS_FILE ERROR INFLATION "
                    "RADIUS OUT_DIR [SEED]\n";

@@ -81,6 +81,54 @@ def run_harness(algo: str, nx: int, ny: int, k: int, ens_prefix: str, obs_file: 
     return members, mean
 
 
+def run_nearest(lat, lon, nx, ny, vc, olat, olon, olev, tmp: Path) -> np.ndarray:
+    """The reference's IdentityObsOperator geographic branch (nearest node and
+    level, IdentityObsOperator.hpp:484-520) through the harness: (i, j, k)
+    per observation."""
+    fin, fout = tmp / "near_in.bin", tmp / "near_out.bin"
+    with open(fin, "wb") as f:
+        np.array([nx, ny, len(vc), len(olat)], dtype="<i8").tofile(f)
+        for a in (lat, lon, vc, olat, olon, olev):
+            np.ascontiguousarray(a, dtype="<f8").tofile(f)
+    subprocess.run([str(HARNESS), "nearest", str(fin), str(fout)], check=True)
+    return np.fromfile(fout, dtype="<i8").reshape(-1, 3)
+
+
+def make_nearest(tmp: Path) -> None:
+    """Golden nearest nodes: a curvilinear grid (obs inside and outside it,
+    on nodes, at midpoints of two nodes) and a regular 0.5 degree grid whose
+    midpoints are exact ties; levels with exact midpoint ties."""
+    out = {}
+    g = np.random.default_rng(20261203 + 600)
+    nx, ny = 40, 30
+    lon, lat = np.meshgrid(np.linspace(70.0, 140.0, nx), np.linspace(5.0, 55.0, ny))
+    lon = lon + 0.8 * np.sin(np.deg2rad(lat) * 3.0) + 0.05 * g.standard_normal(lon.shape)
+    lat = lat + 0.4 * np.cos(np.deg2rad(lon) * 2.0)
+    lat, lon = lat.ravel(), lon.ravel()
+    p = 800
+    oa, ol = g.uniform(0.0, 60.0, p), g.uniform(60.0, 150.0, p)
+    oa[:60], ol[:60] = 0.5 * (lat[:60] + lat[1:61]), 0.5 * (lon[:60] + lon[1:61])
+    oa[60:120], ol[60:120] = lat[300:360], lon[300:360]
+    vc = np.array([1000.0, 925.0, 850.0, 700.0, 500.0, 300.0, 100.0])
+    lev = g.uniform(50.0, 1050.0, p)
+    lev[:30] = 0.5 * (1000.0 + 925.0)
+    lev[30:40] = 700.0
+    out.update(curv_lat=lat, curv_lon=lon, curv_nx=nx, curv_ny=ny, curv_vc=vc, curv_olat=oa, curv_olon=ol,
+               curv_olev=lev, curv_ijk=run_nearest(lat, lon, nx, ny, vc, oa, ol, lev, tmp))
+    nx, ny = 20, 15
+    lon, lat = np.meshgrid(-100.0 + 0.5 * np.arange(nx), 20.0 + 0.5 * np.arange(ny))
+    lat, lon = lat.ravel(), lon.ravel()
+    i, j = g.integers(0, nx - 1, 300), g.integers(0, ny - 1, 300)
+    ol = -100.0 + 0.5 * i + 0.25  # exact midpoints in longitude (ties between i and i + 1)
+    oa = 20.0 + 0.5 * j + np.where(np.arange(300) % 2 == 0, 0.25, 0.0)  # and in both directions
+    vc = np.array([0.95, 0.85, 0.75, 0.65])
+    lev = np.where(np.arange(300) % 3 == 0, 0.9, g.uniform(0.6, 1.0, 300))
+    out.update(reg_lat=lat, reg_lon=lon, reg_nx=nx, reg_ny=ny, reg_vc=vc, reg_olat=oa, reg_olon=ol, reg_olev=lev,
+               reg_ijk=run_nearest(lat, lon, nx, ny, vc, oa, ol, lev, tmp))
+    np.savez_compressed(HERE / "nearest.npz", **out)
+    print("nearest.npz", {k2: np.shape(v) for k2, v in out.items() if k2.endswith("ijk")})
+
+
 def grid_case_to_files(case: syn.GridCase, tmp: Path) -> tuple[str, str]:
     k = case.X.shape[0]
     for i in range(k):
@@ -89,7 +137,7 @@ def grid_case_to_files(case: syn.GridCase, tmp: Path) -> tuple[str, str]:
     return str(tmp / "ens_"), str(tmp / "obs.txt")
 
 
-def main(ref_root: str | None = None) -> None:
+def main(ref_root: str | None = None, only: str | None = None) -> None:
     import os
 
     if ref_root:
@@ -100,6 +148,9 @@ def main(ref_root: str | None = None) -> None:
     tut = ref / "src" / "backends" / "simple" / "tutorial"
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)
+        if only == "nearest":
+            make_nearest(tmp)
+            return
         # --- tutorial ---
         nx, ny, k = 36, 18, 9
         X = np.stack([read_simple_state(tut / f"ens_{i}.txt") for i in range(1, k + 1)])
@@ -168,7 +219,9 @@ def main(ref_root: str | None = None) -> None:
         np.savez_compressed(HERE / "enkf.npz", tut_X=X, tut_obs_xy=obs_xy, tut_yo=yo, tut_sigma=sigma, nx=nx, ny=ny,
                             c1_nx=c.nx, c1_ny=c.ny, **outs)
         print("enkf.npz", {k2: np.shape(v) for k2, v in outs.items()})
+        make_nearest(tmp)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else None)
+    # usage: make_golden.py [REFERENCE_ROOT] [nearest]
+    main(sys.argv[1] if len(sys.argv) > 1 else None, sys.argv[2] if len(sys.argv) > 2 else None)

@@ -98,3 +98,20 @@ def test_nearest_node_ties_of_rounded_square_roots(dev):
     T = lambda a: torch.tensor(a, device=dev)  # noqa: E731
     xy, _ = K.nearest_node(T(lat), T(lon), 2, n, T(oa), T(ol))
     assert np.array_equal(xy.cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("case", ["curv", "reg"])
+def test_nearest_node_matches_reference_golden(dev, case):
+    """Against the reference's own IdentityObsOperator geographic branch
+    (IdentityObsOperator.hpp:484-520, run by the header harness): nodes and
+    levels identical, ties and obs outside the grid included."""
+    from conftest import GOLDEN
+
+    g = np.load(GOLDEN / "nearest.npz")
+    c = lambda k: g[f"{case}_{k}"]  # noqa: E731
+    T = lambda a: torch.tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)  # noqa: E731
+    xy, kk = K.nearest_node(T(c("lat")), T(c("lon")), int(c("nx")), int(c("ny")), T(c("olat")), T(c("olon")),
+                            T(c("vc")), T(c("olev")))
+    ijk = c("ijk")
+    assert np.array_equal(xy.cpu().numpy()[:, 0], ijk[:, 0]) and np.array_equal(xy.cpu().numpy()[:, 1], ijk[:, 1])
+    assert np.array_equal(kk.cpu().numpy(), ijk[:, 2])

@@ -246,3 +246,18 @@ def test_parse_values_is_the_istringstream_loop(built):
     got = ob.parse_values(text)
     assert np.array_equal(got, [1.5, 2.25, -300.0, 4.0, 7.0, 0.5, 8.0, 2.5, -0.0])
     assert np.signbit(got[-1])
+
+
+@pytest.mark.parametrize("case", ["curv", "reg"])
+def test_nearest_node_matches_reference(case):
+    """The oracle's nearest-node scan against the reference's own
+    IdentityObsOperator geographic branch (IdentityObsOperator.hpp:484-520),
+    run by the header harness (tests/golden/nearest.npz): nodes and levels
+    identical, including exact ties (the first minimum wins) and obs outside
+    the grid."""
+    g = np.load(GOLDEN / "nearest.npz")
+    c = lambda k: g[f"{case}_{k}"]  # noqa: E731
+    xy, kk = ob.nearest_node(c("lat"), c("lon"), int(c("nx")), int(c("ny")), c("olat"), c("olon"), c("vc"), c("olev"))
+    ijk = c("ijk")
+    assert np.array_equal(xy[:, 0], ijk[:, 0]) and np.array_equal(xy[:, 1], ijk[:, 1])
+    assert np.array_equal(kk, ijk[:, 2])
