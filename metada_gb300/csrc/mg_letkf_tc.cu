@@ -11,21 +11,23 @@
 // Per local analysis (one CTA of 256 threads, two CTAs per SM, persistent,
 // points pulled longest list first from a work counter):
 //  1. Gram: the candidate list is filtered and weighted, the kept rows
-//     sqrt(w) Y'_o are gathered 32 at a time into a K-major, 128-byte
+//     sqrt(w) Y'_o are gathered 64 at a time into a K-major, 128-byte
 //     swizzled operand (members x obs) with sqrt(w) d_o as an extra row, and
-//     [G | b] = B^T [B | sqrt(w) d] accumulates in TMEM (three rotating
-//     buffers, so the gather of one chunk overlaps the MMAs of the previous).
+//     [G | b] = B^T [B | sqrt(w) d] accumulates in TMEM (two rotating
+//     buffers; each chunk's rows are loaded while the previous one's MMAs run).
 //  2. A = (k-1)/rho I + G.  The ensemble-mean direction 1 is an exact
 //     eigenvector of A (Y' 1 = 0, eigenvalue delta) that never reaches the
 //     outputs (X' 1 = 0, 1^T b = 0), so the iteration runs on
 //     M = P A P / s + 1 1^T / k (P = I - 1 1^T / k), which puts that mode at 1;
 //     s = min(||A||_inf, ||PAP||_F) >= lambda_max keeps M's spectrum in (0, 1].
-//  3. Coupled Newton-Schulz: T = (3I - Z Y) / 2, [Z; Y] <- [Z; Y] T, with Z
-//     and Y stacked as the 128 rows of one MMA operand; it stops once
+//  3. Coupled Newton-Schulz with scaled steps: T = a I - b Z Y (a, b from
+//     ns_coeffs: the classic (3I - Z Y)/2 after scaling Z and Y by sqrt(mu),
+//     mu from the known spectrum bounds [delta/s, 1]), [Z; Y] <- [Z; Y] T, with
+//     Z and Y stacked as the 128 rows of one MMA operand; it stops once
 //     max |Z Y - I| < 0.05 (one more step squares that error).  Z -> M^-1/2,
 //     and A^-1/2 = (Z - 1 1^T / k) / sqrt(s) on the complement of 1.
-//  4. First-order finish from the matrix itself: C = Z A Z, F = C - P,
-//     W = sqrt((k-1) c) Z (I - F/2), wa = c Z (P - F) Z b (c = rho for the
+//  4. First-order finish from the matrix itself: C = Z^T A Z, F = C - P,
+//     W = sqrt((k-1) c) Z (I - F/2), wa = c Z (P - F) Z^T b (c = rho for the
 //     reference's inflation placement, else 1).  max |F| is the per-analysis
 //     residual: analyses above kResidMax (or not converged, or not finite)
 //     are listed and re-run by the SIMT Jacobi kernel.
@@ -45,9 +47,9 @@ using namespace mg::t5;
 
 constexpr int kThreads = 256;
 constexpr int KP = 64;          // member slots
-constexpr int kChunk = 32;      // obs per Gram chunk: one 128-byte swizzle atom of TF32
+constexpr int kChunk = 64;      // obs per Gram chunk: two 128-byte swizzle atoms of TF32
 constexpr int kGramN = 80;      // Gram MMA N: 64 member rows, the innovation row, 15 unused
-constexpr int kNBuf = 3;        // Gram chunk buffers
+constexpr int kNBuf = 2;        // Gram chunk buffers
 constexpr int kSelRing = 512;   // selected-entry ring (a 256-candidate block + carry-over < 32)
 constexpr int kMaxIt = 14;      // Newton-Schulz iterations before an analysis is handed back
 constexpr float kStop = 0.05f;  // max |Z Y - I| that ends the iteration (after one more step)
@@ -57,7 +59,7 @@ constexpr int kVarTile = 16;    // variables per update MMA (N)
 // Operand region: 96 KB, 1024-byte aligned.
 //   Newton-Schulz view: STACK (128 rows x 64 columns, two 16 KB slabs, hi
 //   and lo copies) and TB (64 rows x 64 columns, two 8 KB slabs, hi and lo).
-//   Gram view: three chunk buffers of 32 KB (hi slab, lo slab of 128 rows).
+//   Gram view: two chunk buffers of 40 KB (64 obs: two 10 KB slabs, hi and lo).
 constexpr uint32_t kSlabS = 128 * 128;  // STACK slab / Gram slab
 constexpr uint32_t kSlabT = 64 * 128;   // TB slab
 constexpr uint32_t OFF_STACK_HI = 0;
@@ -65,7 +67,14 @@ constexpr uint32_t OFF_STACK_LO = 2 * kSlabS;
 constexpr uint32_t OFF_TB_HI = 4 * kSlabS;
 constexpr uint32_t OFF_TB_LO = OFF_TB_HI + 2 * kSlabT;
 constexpr uint32_t kRegion = OFF_TB_LO + 2 * kSlabT;  // 96 KB
-constexpr uint32_t kGramBuf = 2 * kSlabS;
+// Gram chunk: 80 operand rows per slab (64 members, the innovation row, 15
+// unused) so a slab is 10 KB; as the 128-row A operand a slab's last 48 rows
+// read the next slab (their products land in unused accumulator rows).
+constexpr int kGramRows = 80;
+constexpr uint32_t kGramSlab = kGramRows * 128;
+constexpr uint32_t kGramBuf = 4 * kGramSlab;  // hi (2 slabs), lo (2 slabs)
+static_assert(kGramSlab % 1024 == 0, "swizzle atoms are 1024-byte aligned");
+static_assert(kNBuf * kGramBuf + (128 - kGramRows) * 128 <= kRegion, "Gram buffers and the A-operand overhang");
 
 // Tensor memory: columns [0, 64) product scratch, [128, 208) the Gram.
 constexpr uint32_t kTmemCols = 256;
@@ -198,6 +207,27 @@ __device__ __forceinline__ bool wait_all(uint64_t* bar, uint32_t parity) {
   return bad == 0;
 }
 
+// Scaled Newton-Schulz step.  The spectrum of Z Y lies in [l, 1] (l = delta / s
+// at the start: P A P >= delta on the complement of 1, s >= lambda_max).  The
+// step scales Z and Y by sqrt(mu) before T = (3I - mu Z Y)/2, i.e.
+// T = a I - b Z Y with a = 1.5 sqrt(mu), b = 0.5 mu^1.5, where mu equalises
+// the map h(e) = e (3 - e)^2 / 4 at both ends of [mu l, mu]:
+// mu = 3 (1 - sqrt l) / (1 - l^1.5).  The new interval is [h(mu l), 1].  The
+// iteration keeps its fixed point (Z -> M^-1/2) and needs about 4 steps
+// instead of 6 at the configurations' conditioning.
+__device__ __forceinline__ void ns_coeffs(float& l, float& a, float& b) {
+  float mu = 1.0f;
+  if (l < 1.0f) {
+    const float sl = sqrtf(l);
+    mu = fmaxf(3.0f * (1.0f - sl) / (1.0f - l * sl), 1.0f);
+  }
+  const float smu = sqrtf(mu);
+  a = 1.5f * smu;
+  b = 0.5f * mu * smu;
+  const float ml = fminf(mu * l, 1.0f);
+  l = ml * (3.0f - ml) * (3.0f - ml) * 0.25f;
+}
+
 // FP64 decision for a candidate whose FP32 vertical distance is within 1e-4
 // of the support (kept out of line: a predicated FP64 instruction would
 // occupy the FP64 pipe for every candidate).
@@ -271,26 +301,27 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     // registers while the previous chunk is stored and its MMAs issued.
     int64_t cpos = e0;
     int nloc = 0, nch = 0, head = 0, nsel = 0;
-    const int slot = lane, m0 = warp * 8;  // gather: obs slot (lane) x 8 members (warp)
-    auto load_rows = [&](int pos, int cnt, float (&x)[8], float& sd) {
+    const int slot = tid & (kChunk - 1), m0 = (tid / kChunk) * 16;  // gather: obs slot x 16 members
+    auto load_rows = [&](int pos, int cnt, float (&x)[16], float& sd) {
       if (slot < cnt) {
         const int e = (pos + slot) & (kSelRing - 1);
         const int o = V.sel_o[e];
         const float sw = V.sel_sw[e];
         sd = V.sel_sd[e];
         const float* yr = Y + (int64_t)o * k;
-        if (vec4 && m0 + 8 <= k) {
-          const float4 a4 = *reinterpret_cast<const float4*>(yr + m0);
-          const float4 c4 = *reinterpret_cast<const float4*>(yr + m0 + 4);
-          x[0] = a4.x * sw; x[1] = a4.y * sw; x[2] = a4.z * sw; x[3] = a4.w * sw;
-          x[4] = c4.x * sw; x[5] = c4.y * sw; x[6] = c4.z * sw; x[7] = c4.w * sw;
+        if (vec4 && m0 + 16 <= k) {
+#pragma unroll
+          for (int q4 = 0; q4 < 4; ++q4) {
+            const float4 a4 = *reinterpret_cast<const float4*>(yr + m0 + 4 * q4);
+            x[4 * q4 + 0] = a4.x * sw; x[4 * q4 + 1] = a4.y * sw; x[4 * q4 + 2] = a4.z * sw; x[4 * q4 + 3] = a4.w * sw;
+          }
         } else {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) x[j] = (m0 + j < k) ? yr[m0 + j] * sw : 0.0f;
+          for (int j = 0; j < 16; ++j) x[j] = (m0 + j < k) ? yr[m0 + j] * sw : 0.0f;
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) x[j] = 0.0f;
+        for (int j = 0; j < 16; ++j) x[j] = 0.0f;
         sd = 0.0f;
       }
     };
@@ -343,24 +374,24 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       }
       const bool done = cpos >= e1;
       const int nchunks = done ? (nsel + kChunk - 1) / kChunk : nsel / kChunk;
-      float x[8], sdv;
+      float x[16], sdv;
       if (nchunks > 0) load_rows(head, nsel < kChunk ? nsel : kChunk, x, sdv);
       for (int c = 0; c < nchunks; ++c) {
         const int b = (int)(gchunk % kNBuf);
         const uint32_t use = gchunk / kNBuf;
         if (use > 0 && !wait_all(&buf_bar[b], (use - 1) & 1u)) { alive = false; break; }
         unsigned char* bh = R + b * kGramBuf;
-        unsigned char* bl = bh + kSlabS;
+        unsigned char* bl = bh + 2 * kGramSlab;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const uint32_t off = sw_off(m0 + j, slot, 128);
+        for (int j = 0; j < 16; ++j) {
+          const uint32_t off = sw_off(m0 + j, slot, kGramRows);
           float h, l;
           split(x[j], h, l);
           *reinterpret_cast<float*>(bh + off) = h;
           *reinterpret_cast<float*>(bl + off) = l;
         }
-        if (warp == 0) {  // the innovation row
-          const uint32_t off = sw_off(KP, slot, 128);
+        if (m0 == 0) {  // the innovation row
+          const uint32_t off = sw_off(KP, slot, kGramRows);
           float h, l;
           split(sdv, h, l);
           *reinterpret_cast<float*>(bh + off) = h;
@@ -374,7 +405,8 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
         if (tid == 0) {
           tc_fence_after();
           const uint32_t a = sR + b * kGramBuf;
-          issue3(tmem + kTmGram, a, a + kSlabS, kSlabS, a, a + kSlabS, kSlabS, 1, idescG, nch > 0);
+          issue3(tmem + kTmGram, a, a + 2 * kGramSlab, kGramSlab, a, a + 2 * kGramSlab, kGramSlab, 2, idescG,
+                 nch > 0);
           mma_commit(&buf_bar[b]);
         }
         ++gchunk;
@@ -469,6 +501,9 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     const float fro = sqrtf(V.red[4] + V.red[5] + V.red[6] + V.red[7]);
     const float s = fmaxf(fminf(ninf, fro), 1e-30f);
     const float is = 1.0f / s;
+    float lsp = fminf(delta * is, 1.0f);  // lower end of the spectrum of Z Y (upper end 1)
+    float nsa, nsb;
+    ns_coeffs(lsp, nsa, nsb);
     // M = PAP / s + 1 1^T / k (identity on unused member slots); STACK <- [I; M]
     // (row-major), TB <- T0 = (3I - M) / 2 stored transposed.
     if (rowwarp) {
@@ -483,7 +518,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       }
       put_row32(STH, STL, KP + row, cb, 128, a);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) a[j] = 0.5f * (((row == cb + j) ? 3.0f : 0.0f) - a[j]);
+      for (int j = 0; j < 32; ++j) a[j] = ((row == cb + j) ? nsa : 0.0f) - nsb * a[j];
       put_col32(TBH, TBL, row, cb, 64, a);
     }
 
@@ -539,7 +574,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
         }
       }
       if (last) break;
-      // P = Z Y (Y as stored, rows 64-127), T = (3I - P) / 2 -> TB transposed.
+      // P = Z Y (Y as stored, rows 64-127), T = a I - b P (scaled step) -> TB transposed.
       operands_ready();
       if (tid == 0) {
         tc_fence_after();
@@ -548,6 +583,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
         mma_commit(&mma_bar);
       }
       if (tid == 0) s_flag[0] = 0u;
+      ns_coeffs(lsp, nsa, nsb);
       if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
       mma_ph ^= 1u;
       float emax = 0.0f;
@@ -562,7 +598,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
           const float p = __uint_as_float(v[j]);
           const float d = p - ((row == c) ? 1.0f : 0.0f);
           emax = fmaxf(emax, fabsf(d));
-          t[j] = ((row == c) ? 1.0f : 0.0f) - 0.5f * d;
+          t[j] = ((row == c) ? nsa - nsb : 0.0f) - nsb * d;  // a I - b P, P = I + d
         }
         put_col32(TBH, TBL, row, cb, 64, t);
 #pragma unroll

@@ -107,3 +107,49 @@ def test_batch_mixed_large_offset_values(dev):
         ma, mw = a.mean(0), w.mean(0)
         assert rel_err(ma, mw) <= 1e-5
         assert rel_err(a - ma, w - mw) <= 1e-5
+
+
+def test_batch_at_the_configuration_extremes(dev):
+    """Cases at the uneven-batch configuration's limits: n up to 200k, p up
+    to 50k (more obs than states in one case), k from 20 to 100.  FP64
+    batch against the single-case path at 1e-10, mixed against FP64 at
+    1e-5, and the oracle on the smallest case."""
+    g = np.random.default_rng(20261203 + 500 + 7)
+    shapes = [(200_000, 100, 50_000), (180_000, 64, 40_000), (1_000, 20, 100), (40_000, 48, 50_000),
+              (200_000, 32, 100), (5_000, 100, 30_000)]
+    cases = []
+    for n, k, p in shapes:
+        truth = g.standard_normal(n).astype(np.float32)
+        X = (truth[None, :] + g.standard_normal((k, n)).astype(np.float32)).astype(np.float64)
+        nodes = g.choice(n, size=p, replace=p > n).astype(np.int64)
+        yo = truth[nodes].astype(np.float64) + g.standard_normal(p)
+        cases.append(syn.UnevenCase(X, nodes, yo, 1.0, syn.float_config(1.05)))
+    d64 = _device_cases(cases, dev)
+    ref = []
+    for c in d64:
+        X = c["X"].clone()
+        K.etkf(X, X[:, c["obs_node"]].T.contiguous(), c["yo"], c["rvar"], c["rho"], flags=0,
+               precision=_lib.MG_PREC_FP64)
+        ref.append(X.cpu().numpy())
+    b64 = K.EtkfBatch(d64, flags=0, precision=_lib.MG_PREC_FP64)
+    b64.run(graph=True)
+    b64.finish()
+    for c, r in zip(d64, ref):
+        assert rel_err(c["X"].cpu().numpy(), r) <= 1e-10
+    dmx = _device_cases(cases, dev)
+    bmx = K.EtkfBatch(dmx, flags=0, precision=_lib.MG_PREC_MIXED)
+    bmx.autotune()
+    bmx.run(graph=True)
+    bmx.finish()
+    for c, r in zip(dmx, d64):
+        a, w = c["X"].cpu().numpy(), r["X"].cpu().numpy()
+        ma, mw = a.mean(0), w.mean(0)
+        assert rel_err(ma, mw) <= 1e-5
+        assert rel_err(a - ma, w - mw) <= 1e-5
+    c = cases[2]
+    pts = np.arange(c.X.shape[1])
+    HX = c.X[:, c.obs_node].T.copy()
+    p = len(c.yo)
+    want = ob.letkf_points(c.X, pts, 1, 0, HX, c.yo, np.full(p, 1.0), np.arange(len(pts) + 1, dtype=np.int64) * p,
+                           np.tile(np.arange(p, dtype=np.int32), len(pts)), None, c.rho, 0)[:, 0, :].T
+    assert rel_err(d64[2]["X"].cpu().numpy(), want) <= 1e-10
