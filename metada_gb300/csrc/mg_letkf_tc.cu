@@ -54,7 +54,7 @@ constexpr int kSelRing = 512;   // selected-entry ring (a 256-candidate block + 
 constexpr int kMaxIt = 14;      // Newton-Schulz iterations before an analysis is handed back
 constexpr float kStop = 0.05f;  // max |Z Y - I| that ends the iteration (after one more step)
 constexpr float kResidMax = 5e-3f;  // max |F| accepted from the first-order finish
-constexpr int kVarTile = 16;    // variables per update MMA (N)
+constexpr int kVarTile = 16;    // variables per update MMA (N): two 8-column TMEM loads
 
 // Operand region: 96 KB, 1024-byte aligned.
 //   Newton-Schulz view: STACK (128 rows x 64 columns, two 16 KB slabs, hi
@@ -109,72 +109,79 @@ __device__ __forceinline__ void split(float x, float& h, float& l) {
   l = x - h;
 }
 
-// Row r, columns c0 .. c0+31 (c0 a multiple of 32: one slab row), 16-byte
-// stores (conflict-free across a warp's 32 consecutive rows).
-__device__ __forceinline__ void put_row32(unsigned char* hi, unsigned char* lo, int r, int c0, uint32_t rows,
-                                          const float (&x)[32]) {
+// The epilogues work on 8 columns at a time inside loops that are not
+// unrolled: fully unrolled 32-column bodies at every call site made the
+// kernel's code larger than the instruction caches.
+//
+// Row r, columns c0 .. c0+7 (c0 a multiple of 8): two 16-byte chunks
+// (conflict-free across a warp's 32 consecutive rows).
+__device__ __forceinline__ void put_row8(unsigned char* hi, unsigned char* lo, int r, int c0, uint32_t rows,
+                                         const float (&x)[8]) {
   const uint32_t base = (uint32_t)(c0 >> 5) * rows * 128u + (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u;
+  const int j0 = (c0 & 31) >> 2;
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    float4 h, l;
-    split(x[4 * j + 0], h.x, l.x);
-    split(x[4 * j + 1], h.y, l.y);
-    split(x[4 * j + 2], h.z, l.z);
-    split(x[4 * j + 3], h.w, l.w);
-    const uint32_t off = base + ((uint32_t)(j ^ (r & 7)) << 4);
-    *reinterpret_cast<float4*>(hi + off) = h;
-    *reinterpret_cast<float4*>(lo + off) = l;
+  for (int h = 0; h < 2; ++h) {
+    float4 vh, vl;
+    split(x[4 * h + 0], vh.x, vl.x);
+    split(x[4 * h + 1], vh.y, vl.y);
+    split(x[4 * h + 2], vh.z, vl.z);
+    split(x[4 * h + 3], vh.w, vl.w);
+    const uint32_t off = base + ((uint32_t)((j0 + h) ^ (r & 7)) << 4);
+    *reinterpret_cast<float4*>(hi + off) = vh;
+    *reinterpret_cast<float4*>(lo + off) = vl;
   }
 }
 
-// Transposed: the thread's row kk of a matrix, columns n0 .. n0+31, goes to
-// operand rows n0 .. n0+31 at column kk (4-byte stores, conflict-free across
+// Row r, columns c0 .. c0+7 of an operand as values (hi + lo).
+__device__ __forceinline__ void get_row8(const unsigned char* hi, const unsigned char* lo, int r, int c0,
+                                         uint32_t rows, float (&x)[8]) {
+  const uint32_t base = (uint32_t)(c0 >> 5) * rows * 128u + (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u;
+  const int j0 = (c0 & 31) >> 2;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const uint32_t off = base + ((uint32_t)((j0 + h) ^ (r & 7)) << 4);
+    const float4 vh = *reinterpret_cast<const float4*>(hi + off);
+    const float4 vl = *reinterpret_cast<const float4*>(lo + off);
+    x[4 * h + 0] = vh.x + vl.x;
+    x[4 * h + 1] = vh.y + vl.y;
+    x[4 * h + 2] = vh.z + vl.z;
+    x[4 * h + 3] = vh.w + vl.w;
+  }
+}
+
+// Transposed: the thread's row kk of a matrix, columns n0 .. n0+7, goes to
+// operand rows n0 .. n0+7 at column kk (4-byte stores, conflict-free across
 // a warp's 32 consecutive kk).
-__device__ __forceinline__ void put_col32(unsigned char* hi, unsigned char* lo, int kk, int n0, uint32_t rows,
-                                          const float (&x)[32]) {
-  const uint32_t cb = (uint32_t)(kk >> 5) * rows * 128u + (uint32_t)(kk & 3) * 4u;
+__device__ __forceinline__ void put_col8(unsigned char* hi, unsigned char* lo, int kk, int n0, uint32_t rows,
+                                         const float (&x)[8]) {
+  const uint32_t cb = (uint32_t)(kk >> 5) * rows * 128u + (uint32_t)(kk & 3) * 4u + (uint32_t)(n0 >> 3) * 1024u;
   const int ch = (kk & 31) >> 2;
 #pragma unroll
-  for (int j = 0; j < 32; ++j) {
-    const int n = n0 + j;
-    const uint32_t off = cb + (uint32_t)(n >> 3) * 1024u + (uint32_t)(n & 7) * 128u + ((uint32_t)(ch ^ (n & 7)) << 4);
-    float h, l;
-    split(x[j], h, l);
-    *reinterpret_cast<float*>(hi + off) = h;
-    *reinterpret_cast<float*>(lo + off) = l;
+  for (int j = 0; j < 8; ++j) {
+    const uint32_t off = cb + (uint32_t)j * 128u + ((uint32_t)(ch ^ j) << 4);
+    float vh, vl;
+    split(x[j], vh, vl);
+    *reinterpret_cast<float*>(hi + off) = vh;
+    *reinterpret_cast<float*>(lo + off) = vl;
   }
 }
 
-// Row r, columns c0 .. c0+31 of an operand as values (hi + lo).
-__device__ __forceinline__ void get_row32(const unsigned char* hi, const unsigned char* lo, int r, int c0,
-                                          uint32_t rows, float (&x)[32]) {
-  const uint32_t base = (uint32_t)(c0 >> 5) * rows * 128u + (uint32_t)(r >> 3) * 1024u + (uint32_t)(r & 7) * 128u;
+// Column c, rows r0 .. r0+7 (r0 a multiple of 8) of an operand as values.
+__device__ __forceinline__ void get_col8(const unsigned char* hi, const unsigned char* lo, int c, int r0,
+                                         uint32_t rows, float (&x)[8]) {
+  const uint32_t cb = (uint32_t)(c >> 5) * rows * 128u + (uint32_t)(c & 3) * 4u + (uint32_t)(r0 >> 3) * 1024u;
+  const int ch = (c & 31) >> 2;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const uint32_t off = base + ((uint32_t)(j ^ (r & 7)) << 4);
-    const float4 h = *reinterpret_cast<const float4*>(hi + off);
-    const float4 l = *reinterpret_cast<const float4*>(lo + off);
-    x[4 * j + 0] = h.x + l.x;
-    x[4 * j + 1] = h.y + l.y;
-    x[4 * j + 2] = h.z + l.z;
-    x[4 * j + 3] = h.w + l.w;
-  }
-}
-
-// Column c, rows r0 .. r0+31 of an operand as values (hi + lo); 4-byte
-// loads, conflict-free across a warp's 32 consecutive c.
-__device__ __forceinline__ void get_col32(const unsigned char* hi, const unsigned char* lo, int c, int r0,
-                                          uint32_t rows, float (&x)[32]) {
-#pragma unroll
-  for (int j = 0; j < 32; ++j) {
-    const uint32_t off = sw_off(r0 + j, c, rows);
+    const uint32_t off = cb + (uint32_t)j * 128u + ((uint32_t)(ch ^ j) << 4);
     x[j] = *reinterpret_cast<const float*>(hi + off) + *reinterpret_cast<const float*>(lo + off);
   }
 }
 
 // D (TMEM) += A B over nslab slabs of 32 K-columns, 3 passes per K-step of 8.
 // A: 128 rows from a_hi/a_lo (slab stride a_slab); B: N rows from b_hi/b_lo.
-__device__ __forceinline__ void issue3(uint32_t dtm, uint32_t a_hi, uint32_t a_lo, uint32_t a_slab, uint32_t b_hi,
+// Out of line: one copy of the issue loop for every product of the kernel.
+__device__ __noinline__ void issue3(uint32_t dtm, uint32_t a_hi, uint32_t a_lo, uint32_t a_slab, uint32_t b_hi,
                                        uint32_t b_lo, uint32_t b_slab, int nslab, uint32_t idesc, bool accumulate) {
   // Descriptors of the first K-step; later steps add (byte offset >> 4) to
   // the 14-bit start-address field (shared addresses stay below 256 KB).
@@ -436,32 +443,35 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     mma_ph ^= 1u;
 
     // ---------------- 2. A, b, deflation and scaling ----------------
-    // Warps of quadrants 0-1 hold rows 0-63; column half hh.
+    // Warps of quadrants 0-1 hold rows 0-63 (their TMEM lanes), column half
+    // hh; each walks its 32 columns 8 at a time.
     const bool rowwarp = q < 2;
     const int row = 32 * q + lane;
     const int cb = 32 * hh;
-    float a[32];
     if (rowwarp) {
-      uint32_t v[32];
-      tmem_ld32(tmem + tm_row + kTmGram + cb, v);
-      uint32_t bv = 0;
-      if (hh == 0) bv = tmem_ld1(tmem + tm_row + kTmGram + KP);
-      tmem_wait_ld();
       float rs = 0.0f, as = 0.0f;
+#pragma unroll 1
+      for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+        uint32_t v[8];
+        tmem_ld8(tmem + tm_row + kTmGram + c0, v);
+        tmem_wait_ld();
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int c = cb + j;
-        float x = __uint_as_float(v[j]);
-        if (c == row) x += (row < k) ? delta : 1.0f;
-        a[j] = x;
-        if (row < k && c < k) {
-          rs += x;
-          as += fabsf(x);
+        for (int j = 0; j < 8; ++j) {
+          const int c = c0 + j;
+          const float x = __uint_as_float(v[j]) + ((c == row) ? delta : 0.0f);
+          if (row < k && c < k) {
+            rs += x;
+            as += fabsf(x);
+          }
         }
       }
       V.part[hh][row] = rs;
       V.part[2 + hh][row] = as;
-      if (hh == 0) V.b[row] = (row < k) ? __uint_as_float(bv) : 0.0f;
+      if (hh == 0) {
+        const uint32_t bv = tmem_ld1(tmem + tm_row + kTmGram + KP);
+        tmem_wait_ld();
+        V.b[row] = (row < k) ? __uint_as_float(bv) : 0.0f;
+      }
     }
     __syncthreads();
     if (warp < 2) {  // row means r, grand mean c, infinity norm
@@ -483,15 +493,28 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     __syncthreads();
     const float cbar = (V.red[0] + V.red[1]) * ik;
     const float ninf = fmaxf(V.red[2], V.red[3]);
-    if (rowwarp) {  // P A P in registers, its Frobenius norm
+    // Row `row` of P A P, columns c0 .. c0+7, from the Gram in TMEM (zero
+    // outside the member block).
+    auto pap8 = [&](int c0, float (&x)[8]) {
+      uint32_t v[8];
+      tmem_ld8(tmem + tm_row + kTmGram + c0, v);
+      tmem_wait_ld();
       const float ri = V.r[row];
-      float fs = 0.0f;
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int c = cb + j;
-        const float x = (row < k && c < k) ? (a[j] - ri - V.r[c] + cbar) : 0.0f;
-        a[j] = x;
-        fs += x * x;
+      for (int j = 0; j < 8; ++j) {
+        const int c = c0 + j;
+        const float av = __uint_as_float(v[j]) + ((c == row) ? delta : 0.0f);
+        x[j] = (row < k && c < k) ? (av - ri - V.r[c] + cbar) : 0.0f;
+      }
+    };
+    if (rowwarp) {  // Frobenius norm of P A P
+      float fs = 0.0f;
+#pragma unroll 1
+      for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+        float x[8];
+        pap8(c0, x);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) fs += x[j] * x[j];
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) fs += __shfl_xor_sync(0xffffffffu, fs, off);
@@ -505,21 +528,25 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     float nsa, nsb;
     ns_coeffs(lsp, nsa, nsb);
     // M = PAP / s + 1 1^T / k (identity on unused member slots); STACK <- [I; M]
-    // (row-major), TB <- T0 = (3I - M) / 2 stored transposed.
+    // (row-major), TB <- T0 = a I - b M stored transposed.
     if (rowwarp) {
-      float x[32];
+#pragma unroll 1
+      for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+        float x[8];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) x[j] = (row == cb + j) ? 1.0f : 0.0f;
-      put_row32(STH, STL, row, cb, 128, x);
+        for (int j = 0; j < 8; ++j) x[j] = (row == c0 + j) ? 1.0f : 0.0f;
+        put_row8(STH, STL, row, c0, 128, x);
+        pap8(c0, x);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int c = cb + j;
-        a[j] = (row < k && c < k) ? a[j] * is + ik : ((row == c) ? 1.0f : 0.0f);
+        for (int j = 0; j < 8; ++j) {
+          const int c = c0 + j;
+          x[j] = (row < k && c < k) ? x[j] * is + ik : ((row == c) ? 1.0f : 0.0f);
+        }
+        put_row8(STH, STL, KP + row, c0, 128, x);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = ((row == c0 + j) ? nsa : 0.0f) - nsb * x[j];
+        put_col8(TBH, TBL, row, c0, 64, x);
       }
-      put_row32(STH, STL, KP + row, cb, 128, a);
-#pragma unroll
-      for (int j = 0; j < 32; ++j) a[j] = ((row == cb + j) ? nsa : 0.0f) - nsb * a[j];
-      put_col32(TBH, TBL, row, cb, 64, a);
     }
 
     // ---------------- 3. coupled Newton-Schulz ----------------
@@ -540,37 +567,36 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       conv = stop;
       if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
       mma_ph ^= 1u;
-      {
-        uint32_t v[32];
-        tmem_ld32(tmem + tm_row + cb, v);
-        tmem_wait_ld();
-        float x[32];
-        if (!last) {
+      if (!last) {  // all eight warps: rows 0-63 Z, 64-127 Y
+#pragma unroll 1
+        for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+          uint32_t v[8];
+          tmem_ld8(tmem + tm_row + c0, v);
+          tmem_wait_ld();
+          float x[8];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]);
-          put_row32(STH, STL, 32 * q + lane, cb, 128, x);  // rows 0-63 Z, 64-127 Y
-        } else if (rowwarp) {
-          // Final Z -> (Z - 1 1^T / k) / sqrt(s) on the member block, 0 elsewhere,
-          // stored transposed (rows 0-63 hold Z^T); rows 64-127 <- P A P
-          // (re-read from the Gram in TMEM) for the finish.
-          const float isq = rsqrtf(s);
+          for (int j = 0; j < 8; ++j) x[j] = __uint_as_float(v[j]);
+          put_row8(STH, STL, 32 * q + lane, c0, 128, x);
+        }
+      } else if (rowwarp) {
+        // Final Z -> (Z - 1 1^T / k) / sqrt(s) on the member block, 0 elsewhere,
+        // stored transposed (rows 0-63 hold Z^T); rows 64-127 <- P A P
+        // (from the Gram in TMEM) for the finish.
+        const float isq = rsqrtf(s);
+#pragma unroll 1
+        for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+          uint32_t v[8];
+          tmem_ld8(tmem + tm_row + c0, v);
+          tmem_wait_ld();
+          float x[8];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int c = cb + j;
+          for (int j = 0; j < 8; ++j) {
+            const int c = c0 + j;
             x[j] = (row < k && c < k) ? (__uint_as_float(v[j]) - ik) * isq : 0.0f;
           }
-          put_col32(STH, STL, row, cb, 128, x);
-          tmem_ld32(tmem + tm_row + kTmGram + cb, v);  // the Gram row again (v is free)
-          tmem_wait_ld();
-          const float ri = V.r[row];
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int c = cb + j;
-            float av = __uint_as_float(v[j]);
-            if (c == row) av += delta;
-            x[j] = (row < k && c < k) ? (av - ri - V.r[c] + cbar) : 0.0f;
-          }
-          put_row32(STH, STL, KP + row, cb, 128, x);
+          put_col8(STH, STL, row, c0, 128, x);
+          pap8(c0, x);
+          put_row8(STH, STL, KP + row, c0, 128, x);
         }
       }
       if (last) break;
@@ -586,21 +612,23 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       ns_coeffs(lsp, nsa, nsb);
       if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
       mma_ph ^= 1u;
-      float emax = 0.0f;
       if (rowwarp) {
-        uint32_t v[32];
-        tmem_ld32(tmem + tm_row + cb, v);
-        tmem_wait_ld();
-        float t[32];
+        float emax = 0.0f;
+#pragma unroll 1
+        for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+          uint32_t v[8];
+          tmem_ld8(tmem + tm_row + c0, v);
+          tmem_wait_ld();
+          float t[8];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int c = cb + j;
-          const float p = __uint_as_float(v[j]);
-          const float d = p - ((row == c) ? 1.0f : 0.0f);
-          emax = fmaxf(emax, fabsf(d));
-          t[j] = ((row == c) ? nsa - nsb : 0.0f) - nsb * d;  // a I - b P, P = I + d
+          for (int j = 0; j < 8; ++j) {
+            const int c = c0 + j;
+            const float d = __uint_as_float(v[j]) - ((row == c) ? 1.0f : 0.0f);
+            emax = fmaxf(emax, fabsf(d));
+            t[j] = ((row == c) ? nsa - nsb : 0.0f) - nsb * d;  // a I - b P, P = I + d
+          }
+          put_col8(TBH, TBL, row, c0, 64, t);
         }
-        put_col32(TBH, TBL, row, cb, 64, t);
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, off));
         // a NaN compares false: treat it as not converged
@@ -624,24 +652,29 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       mma_commit(&mma_bar);
     }
     if (tid < KP) {  // u = Z^T b (row tid of Z^T)
-      float z[32], acc = 0.0f;
-      for (int c0 = 0; c0 < KP; c0 += 32) {
-        get_row32(STH, STL, tid, c0, 128, z);
+      float acc = 0.0f;
+#pragma unroll 1
+      for (int c0 = 0; c0 < KP; c0 += 8) {
+        float z[8];
+        get_row8(STH, STL, tid, c0, 128, z);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) acc += z[j] * V.b[c0 + j];
+        for (int j = 0; j < 8; ++j) acc += z[j] * V.b[c0 + j];
       }
       V.u[tid] = acc;
     }
     if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
     mma_ph ^= 1u;
     if (rowwarp) {  // Q -> TB transposed
-      uint32_t v[32];
-      tmem_ld32(tmem + tm_row + cb, v);
-      tmem_wait_ld();
-      float x[32];
+#pragma unroll 1
+      for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+        uint32_t v[8];
+        tmem_ld8(tmem + tm_row + c0, v);
+        tmem_wait_ld();
+        float x[8];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) x[j] = __uint_as_float(v[j]);
-      put_col32(TBH, TBL, row, cb, 64, x);
+        for (int j = 0; j < 8; ++j) x[j] = __uint_as_float(v[j]);
+        put_col8(TBH, TBL, row, c0, 64, x);
+      }
     }
     // C = Z^T Q
     operands_ready();
@@ -654,52 +687,55 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     }
     if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
     mma_ph ^= 1u;
-    // F = C - P (residual, partial F u); Z rows are read back from Z^T
-    // (column reads) and, after every read, stored row-major over Z^T; F goes
-    // to rows 64-127 as the B operand of Z F.
-    float zr[32];
+    // F = C - P (residual, partial F u) -> TB transposed (B operand of Z F);
+    // Z rows, read from the columns of Z^T, -> STACK rows 64-127 row-major
+    // (A operand of Z F; P A P there is not read any more).
     if (rowwarp) {
-      float f[32];
-      uint32_t v[32];
-      tmem_ld32(tmem + tm_row + cb, v);
-      tmem_wait_ld();
       float fu = 0.0f, fm = 0.0f;
+#pragma unroll 1
+      for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+        uint32_t v[8];
+        tmem_ld8(tmem + tm_row + c0, v);
+        tmem_wait_ld();
+        float f[8];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int c = cb + j;
-        const float pij = (row < k && c < k) ? (((row == c) ? 1.0f : 0.0f) - ik) : 0.0f;
-        const float x = (row < k && c < k) ? __uint_as_float(v[j]) - pij : 0.0f;
-        f[j] = x;
-        fm = fmaxf(fm, fabsf(x));
-        fu += x * V.u[c];
+        for (int j = 0; j < 8; ++j) {
+          const int c = c0 + j;
+          const float pij = (row < k && c < k) ? (((row == c) ? 1.0f : 0.0f) - ik) : 0.0f;
+          const float x = (row < k && c < k) ? __uint_as_float(v[j]) - pij : 0.0f;
+          f[j] = x;
+          fm = fmaxf(fm, fabsf(x));
+          fu += x * V.u[c];
+        }
+        put_col8(TBH, TBL, row, c0, 64, f);
+        get_col8(STH, STL, row, c0, 128, f);
+        put_row8(STH, STL, KP + row, c0, 128, f);
       }
       V.part[hh][row] = fu;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) fm = fmaxf(fm, __shfl_xor_sync(0xffffffffu, fm, off));
       // NaN or Inf residuals map to the maximum (positive floats order as integers)
       if (lane == 0) atomicMax(&s_flag[1], (fm == fm && fm < 3.0e38f) ? __float_as_uint(fm) : 0x7f800000u);
-      put_col32(STH, STL, row, KP + cb, 128, f);  // rows 64-127 (P A P) are not read any more
-      get_col32(STH, STL, row, cb, 128, zr);
     }
-    __syncthreads();
-    if (rowwarp) put_row32(STH, STL, row, cb, 128, zr);
     // W = cw Z (I - F/2): D = Z F
     operands_ready();
     if (tid == 0) {
       tc_fence_after();
-      issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_STACK_HI + KP * 128,
-             sR + OFF_STACK_LO + KP * 128, kSlabS, 2, idesc64, false);
+      issue3(tmem, sR + OFF_STACK_HI + KP * 128, sR + OFF_STACK_LO + KP * 128, kSlabS, sR + OFF_TB_HI,
+             sR + OFF_TB_LO, kSlabT, 2, idesc64, false);
       mma_commit(&mma_bar);
     }
     const float resid = __uint_as_float(s_flag[1]);
     if (tid < KP) V.v[tid] = (tid < k) ? V.u[tid] - (V.part[0][tid] + V.part[1][tid]) : 0.0f;
     __syncthreads();
-    if (tid < KP) {  // wa = c Z v
-      float z[32], acc = 0.0f;
-      for (int c0 = 0; c0 < KP; c0 += 32) {
-        get_row32(STH, STL, tid, c0, 128, z);
+    if (tid < KP) {  // wa = c Z v (row tid of Z, STACK row 64 + tid)
+      float acc = 0.0f;
+#pragma unroll 1
+      for (int c0 = 0; c0 < KP; c0 += 8) {
+        float z[8];
+        get_row8(STH, STL, KP + tid, c0, 128, z);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) acc += z[j] * V.v[c0 + j];
+        for (int j = 0; j < 8; ++j) acc += z[j] * V.v[c0 + j];
       }
       V.wa[tid] = sc * acc;
     }
@@ -715,27 +751,20 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       __syncthreads();
       continue;
     }
-    if (rowwarp) {  // W rows -> U^T = W^T into STACK rows 64.. (A operand of the update)
-      uint32_t v[32];
-      tmem_ld32(tmem + tm_row + cb, v);
-      tmem_wait_ld();
-      float z[32], w[32];
-      get_row32(STH, STL, row, cb, 128, z);
+    if (rowwarp) {  // W rows -> U^T = W^T into STACK rows 0-63 (A operand of the update)
+#pragma unroll 1
+      for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+        uint32_t v[8];
+        tmem_ld8(tmem + tm_row + c0, v);
+        tmem_wait_ld();
+        float w[8];
+        get_row8(STH, STL, KP + row, c0, 128, w);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) w[j] = cw * (z[j] - 0.5f * __uint_as_float(v[j]));
-      // operand row m = column index of W, operand column = row of W
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int m = KP + cb + j;
-        const uint32_t off = sw_off(m, row, 128);
-        float h, l;
-        split(w[j], h, l);
-        *reinterpret_cast<float*>(STH + off) = h;
-        *reinterpret_cast<float*>(STL + off) = l;
+        for (int j = 0; j < 8; ++j) w[j] = cw * (w[j] - 0.5f * __uint_as_float(v[j]));
+        put_col8(STH, STL, row, c0, 128, w);
       }
     }
 
-    __syncthreads();  // the W epilogue's reads of Z are done before TB and STACK change
     // ---------------- 5. update ----------------
     const float c1 = cw * rsqrtf(delta);  // W's eigenvalue on the mean direction
     for (int v0 = 0; v0 < prm.n_var; v0 += kVarTile) {
@@ -775,19 +804,23 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       operands_ready();
       if (tid == 0) {
         tc_fence_after();
-        issue3(tmem, sR + OFF_STACK_HI + KP * 128, sR + OFF_STACK_LO + KP * 128, kSlabS, sR + OFF_TB_HI,
-               sR + OFF_TB_LO, kSlabT, 2, idescU, false);
+        issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2,
+               idescU, false);
         mma_commit(&mma_bar);
       }
       if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
       mma_ph ^= 1u;
       float dv[kVarTile];
       if (rowwarp && hh == 0) {
-        uint32_t v[32];
-        tmem_ld32(tmem + tm_row, v);  // 16 columns used
+        uint32_t v[8], v2[8];
+        tmem_ld8(tmem + tm_row, v);
+        tmem_ld8(tmem + tm_row + 8, v2);
         tmem_wait_ld();
 #pragma unroll
-        for (int vv = 0; vv < kVarTile; ++vv) dv[vv] = __uint_as_float(v[vv]) + V.one[vv];
+        for (int vv = 0; vv < 8; ++vv) {
+          dv[vv] = __uint_as_float(v[vv]) + V.one[vv];
+          dv[8 + vv] = __uint_as_float(v2[vv]) + V.one[8 + vv];
+        }
         if (rtps) {  // analysis spread per variable (members = threads 0..63)
 #pragma unroll
           for (int vv = 0; vv < kVarTile; ++vv) {
