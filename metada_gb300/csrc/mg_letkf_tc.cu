@@ -180,7 +180,8 @@ __device__ __forceinline__ void get_col8(const unsigned char* hi, const unsigned
 
 // D (TMEM) += A B over nslab slabs of 32 K-columns, 3 passes per K-step of 8.
 // A: 128 rows from a_hi/a_lo (slab stride a_slab); B: N rows from b_hi/b_lo.
-// Out of line: one copy of the issue loop for every product of the kernel.
+// Called by all of warp 0 with the same arguments (lane 0 issues); out of
+// line: one copy of the issue loop for every product of the kernel.
 __device__ __noinline__ void issue3(uint32_t dtm, uint32_t a_hi, uint32_t a_lo, uint32_t a_slab, uint32_t b_hi,
                                        uint32_t b_lo, uint32_t b_slab, int nslab, uint32_t idesc, bool accumulate) {
   // Descriptors of the first K-step; later steps add (byte offset >> 4) to
@@ -191,9 +192,9 @@ __device__ __noinline__ void issue3(uint32_t dtm, uint32_t a_hi, uint32_t a_lo, 
 #pragma unroll
     for (int kk = 0; kk < 4; ++kk) {
       const uint64_t ao = (uint64_t)((s * a_slab + kk * 32) >> 4), bo = (uint64_t)((s * b_slab + kk * 32) >> 4);
-      mma_tf32(dtm, ah + ao, bh + bo, idesc, (accumulate || s > 0 || kk > 0) ? 1u : 0u);
-      mma_tf32(dtm, ah + ao, bl + bo, idesc, 1u);
-      mma_tf32(dtm, al + ao, bh + bo, idesc, 1u);
+      mma_tf32_elect(dtm, ah + ao, bh + bo, idesc, (accumulate || s > 0 || kk > 0) ? 1u : 0u);
+      mma_tf32_elect(dtm, ah + ao, bl + bo, idesc, 1u);
+      mma_tf32_elect(dtm, al + ao, bh + bo, idesc, 1u);
     }
   }
 }
@@ -409,12 +410,12 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
           load_rows(head + (c + 1) * kChunk, rem < kChunk ? rem : kChunk, x, sdv);
         }
         operands_ready();
-        if (tid == 0) {
+        if (warp == 0) {
           tc_fence_after();
           const uint32_t a = sR + b * kGramBuf;
           issue3(tmem + kTmGram, a, a + 2 * kGramSlab, kGramSlab, a, a + 2 * kGramSlab, kGramSlab, 2, idescG,
                  nch > 0);
-          mma_commit(&buf_bar[b]);
+          mma_commit_elect(&buf_bar[b]);
         }
         ++gchunk;
         ++nch;
@@ -438,7 +439,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       __syncthreads();
       continue;
     }
-    if (tid == 0) mma_commit(&mma_bar);
+    if (warp == 0) mma_commit_elect(&mma_bar);
     if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
     mma_ph ^= 1u;
 
@@ -556,11 +557,11 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     for (;;) {
       // [Z; Y] <- [Z; Y] T
       operands_ready();
-      if (tid == 0) {
+      if (warp == 0) {
         tc_fence_after();
         issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2,
                idesc64, false);
-        mma_commit(&mma_bar);
+        mma_commit_elect(&mma_bar);
       }
       ++its;
       const bool last = stop || its >= kMaxIt;
@@ -602,11 +603,11 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       if (last) break;
       // P = Z Y (Y as stored, rows 64-127), T = a I - b P (scaled step) -> TB transposed.
       operands_ready();
-      if (tid == 0) {
+      if (warp == 0) {
         tc_fence_after();
         issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_STACK_HI + KP * 128,
                sR + OFF_STACK_LO + KP * 128, kSlabS, 2, idesc64, false);
-        mma_commit(&mma_bar);
+        mma_commit_elect(&mma_bar);
       }
       if (tid == 0) s_flag[0] = 0u;
       ns_coeffs(lsp, nsa, nsb);
@@ -645,11 +646,11 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     // Q = (P A P) Z (A operand STACK rows 64.. = P A P, B operand Z^T rows),
     // then C = Z^T Q; A^-1 = Z C^-1 Z^T, A^-1/2 ~ Z C^-1/2.
     operands_ready();
-    if (tid == 0) {
+    if (warp == 0) {
       tc_fence_after();
       issue3(tmem, sR + OFF_STACK_HI + KP * 128, sR + OFF_STACK_LO + KP * 128, kSlabS, sR + OFF_STACK_HI,
              sR + OFF_STACK_LO, kSlabS, 2, idesc64, false);
-      mma_commit(&mma_bar);
+      mma_commit_elect(&mma_bar);
     }
     if (tid < KP) {  // u = Z^T b (row tid of Z^T)
       float acc = 0.0f;
@@ -678,12 +679,12 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     }
     // C = Z^T Q
     operands_ready();
-    if (tid == 0) {
+    if (warp == 0) {
       tc_fence_after();
       issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2, idesc64,
              false);
-      mma_commit(&mma_bar);
-      s_flag[1] = 0u;
+      mma_commit_elect(&mma_bar);
+      if (lane == 0) s_flag[1] = 0u;
     }
     if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
     mma_ph ^= 1u;
@@ -719,11 +720,11 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     }
     // W = cw Z (I - F/2): D = Z F
     operands_ready();
-    if (tid == 0) {
+    if (warp == 0) {
       tc_fence_after();
       issue3(tmem, sR + OFF_STACK_HI + KP * 128, sR + OFF_STACK_LO + KP * 128, kSlabS, sR + OFF_TB_HI,
              sR + OFF_TB_LO, kSlabT, 2, idesc64, false);
-      mma_commit(&mma_bar);
+      mma_commit_elect(&mma_bar);
     }
     const float resid = __uint_as_float(s_flag[1]);
     if (tid < KP) V.v[tid] = (tid < k) ? V.u[tid] - (V.part[0][tid] + V.part[1][tid]) : 0.0f;
@@ -802,11 +803,11 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
         }
       }
       operands_ready();
-      if (tid == 0) {
+      if (warp == 0) {
         tc_fence_after();
         issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2,
                idescU, false);
-        mma_commit(&mma_bar);
+        mma_commit_elect(&mma_bar);
       }
       if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
       mma_ph ^= 1u;
