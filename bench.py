@@ -421,6 +421,72 @@ def run_uneven(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def global_etkf_results(warmup: int, steps: int) -> dict:
+    """The global ETKF of the 64 x 64 grid, k = 32, p = 1024 configuration
+    (ETKF.hpp:100-179): one analysis = IDW4 H(X) of the members plus the ETKF
+    update, per call on device-resident inputs, with the reference's
+    semantics in FP64 and the Hunt form in mixed precision; the oracle's
+    restatement of the reference's ETKF timed on the host beside it."""
+    import torch
+
+    from metada_gb300 import _lib
+    from metada_gb300 import kernels as K
+    from metada_gb300 import synthetic as syn
+    from oracle import bind as ob
+
+    dev = torch.device("cuda", 0)
+    c = syn.global_etkf_grid(case=1)
+    k, n = c.X.shape
+    X0 = torch.tensor(c.X, device=dev)
+    X = X0.clone()
+    oxy = torch.tensor(c.obs_xy, device=dev)
+    yo = torch.tensor(c.yo, device=dev)
+    rvar = torch.full((len(c.yo),), c.sigma_o * c.sigma_o, dtype=torch.float64, device=dev)
+    res = {}
+    for name, flags, prec in (("reference_semantics_fp64", _lib.MG_COMPAT, _lib.MG_PREC_FP64),
+                              ("hunt_mixed", 0, _lib.MG_PREC_MIXED)):
+        def call():
+            HX = K.hx_idw4(X, c.nx, c.ny, oxy)
+            K.etkf(X, HX, yo, rvar, c.rho, flags=flags, precision=prec)
+        for _ in range(warmup):
+            X.copy_(X0)
+            call()
+        ts = []
+        for _ in range(steps):
+            X.copy_(X0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            call()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        t = statistics.median(ts)
+        res[name] = {"ms_per_analysis": 1e3 * t, "analyses_per_s": 1.0 / t}
+    # parity of the FP64 reference-semantics call against the oracle
+    X.copy_(X0)
+    HX = K.hx_idw4(X, c.nx, c.ny, oxy)
+    K.etkf(X, HX, yo, rvar, c.rho, flags=_lib.MG_COMPAT, precision=_lib.MG_PREC_FP64)
+    HXo = ob.hx_idw4(c.X, c.nx, c.ny, c.obs_xy)
+    rv = np.full(len(c.yo), c.sigma_o * c.sigma_o)
+    want, _ = ob.etkf_compat(c.X, HXo, c.yo, rv, c.rho)
+    got = X.cpu().numpy()
+    err = float(np.abs(got - want).max() / np.abs(want).max())
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        ob.etkf_compat(c.X, ob.hx_idw4(c.X, c.nx, c.ny, c.obs_xy), c.yo, rv, c.rho)
+        reps += 1
+        if time.perf_counter() - t0 >= 3.0:
+            break
+    tc = (time.perf_counter() - t0) / reps
+    return {"workload": f"global ETKF, {c.nx}x{c.ny} grid (n={n}), k={k}, p={len(c.yo)}, IDW4 H, sigma 0.5, "
+                        f"rho 1.05 (as float)",
+            "step": "H(X) and one ETKF analysis per call, inputs on the device", "steps": steps, "warmup": warmup,
+            **res, "rel_err_fp64_vs_oracle": err,
+            "cpu_baseline": {"value": 1.0 / tc, "unit": "analyses/s", "cores": int(ob.load().orc_num_threads()),
+                             "kind": "port", "sample": "the whole case: the oracle's restatement of ETKF.hpp "
+                                                       "(dense p x p R, LU inverses)"}}
+
+
 def uneven_results(warmup: int, steps: int) -> dict:
     """The uneven batch (mixed and FP64): analyses/s, per-case p50/p99
     latency, the autotuned plan, and the mixed path's error against FP64."""
@@ -1020,6 +1086,7 @@ def main():
             "mixed": u["mixed"], "fp64": {kk: u["fp64"][kk] for kk in ("analyses_per_s", "ms_per_batch")},
             "max_rel_err_mixed_vs_fp64": u["max_rel_err_mixed_vs_fp64"], "steps": 3, "warmup": 1}
         torch.cuda.empty_cache()
+        extras["global_etkf_small"] = global_etkf_results(warmup=3, steps=20)
         col = column_results(args.extra_train_steps, 4096)
         extras["column_operator"] = {
             "workload": col["config"]["workload"],

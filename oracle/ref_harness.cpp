@@ -35,9 +35,11 @@ struct harness_seeded_device {
 }  // namespace std
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
+#include <iomanip>
 #include <iostream>
 #include <memory>
 #include <sstream>
@@ -216,16 +218,24 @@ int main(int argc, char** argv) {
     auto control = std::make_shared<fw::IdentityControlVariableBackend<Tag>>();
     fw::ObsOperator<Tag> obs_operator(config.GetSubsection("obs_operator"), *control);
 
+    // Wall time of the policy's construction and Analyse() (inputs already
+    // read), written to OUT_DIR/analyse_seconds.txt.
+    const auto t0 = std::chrono::steady_clock::now();
+    auto elapsed = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
+    double seconds = 0.0;
     if (algo == "etkf") {
       fw::ETKF<Tag> etkf(ensemble, observations, obs_operator, config.GetSubsection("analysis"));
       etkf.Analyse();
+      seconds = elapsed();
     } else if (algo == "letkf") {
       fw::LETKF<Tag> letkf(ensemble, observations, obs_operator, config.GetSubsection("analysis"));
       letkf.Analyse();
+      seconds = elapsed();
     } else if (algo == "enkf") {
       // EnKF reads the "analysis" subsection itself (EnKF.hpp:109).
       fw::EnKF<Tag> enkf(ensemble, observations, obs_operator, config);
       enkf.Analyse();
+      seconds = elapsed();
       const auto r = enkf.getAnalysisResults();
       const double dg[5] = {r.innovation_norm, r.background_spread, r.analysis_spread, r.max_kalman_gain,
                             r.min_kalman_gain};
@@ -243,6 +253,7 @@ int main(int argc, char** argv) {
     } else {
       throw std::runtime_error("unknown algorithm " + algo);
     }
+    std::ofstream(out + "/analyse_seconds.txt") << std::setprecision(9) << seconds << "\n";
     const size_t n = ensemble.GetMember(0).size();
     for (int i = 0; i < k; ++i)
       dump(out + "/member_" + std::to_string(i) + ".bin",
