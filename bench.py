@@ -425,7 +425,8 @@ def global_etkf_results(warmup: int, steps: int) -> dict:
     """The global ETKF of the 64 x 64 grid, k = 32, p = 1024 configuration
     (ETKF.hpp:100-179): one analysis = IDW4 H(X) of the members plus the ETKF
     update, per call on device-resident inputs, with the reference's
-    semantics in FP64 and the Hunt form in mixed precision; the oracle's
+    semantics (Cholesky W) in FP64 and the Hunt form (symmetric W from a
+    Jacobi eigen-solve) in FP64 and mixed precision; the oracle's
     restatement of the reference's ETKF timed on the host beside it."""
     import torch
 
@@ -444,7 +445,7 @@ def global_etkf_results(warmup: int, steps: int) -> dict:
     rvar = torch.full((len(c.yo),), c.sigma_o * c.sigma_o, dtype=torch.float64, device=dev)
     res = {}
     for name, flags, prec in (("reference_semantics_fp64", _lib.MG_COMPAT, _lib.MG_PREC_FP64),
-                              ("hunt_mixed", 0, _lib.MG_PREC_MIXED)):
+                              ("hunt_fp64", 0, _lib.MG_PREC_FP64), ("hunt_mixed", 0, _lib.MG_PREC_MIXED)):
         def call():
             HX = K.hx_idw4(X, c.nx, c.ny, oxy)
             K.etkf(X, HX, yo, rvar, c.rho, flags=flags, precision=prec)

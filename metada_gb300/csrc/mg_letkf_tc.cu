@@ -29,8 +29,10 @@
 //  4. First-order finish from the matrix itself: C = Z^T A Z, F = C - P,
 //     W = sqrt((k-1) c) Z (I - F/2), wa = c Z (P - F) Z^T b (c = rho for the
 //     reference's inflation placement, else 1).  max |F| is the per-analysis
-//     residual: analyses above kResidMax (or not converged, or not finite)
-//     are listed and re-run by the SIMT Jacobi kernel.
+//     residual.  Analyses whose conditioning bound s / delta is above
+//     kMaxCond, whose iteration does not converge or leaves its basin, whose
+//     residual is above the gates (kResidMax, kCondResid delta / s) or whose
+//     values are not finite are listed and re-run by the SIMT Jacobi kernel.
 //  5. Update: D = W^T X'^T (members x variables) on the tensor core, then
 //     x_a = x_mean + X' wa + D (+ RTPS relaxation), written in FP64.
 // Every mbarrier wait is bounded in time; a wait that gives up makes the CTA
@@ -54,6 +56,23 @@ constexpr int kSelRing = 512;   // selected-entry ring (a 256-candidate block + 
 constexpr int kMaxIt = 14;      // Newton-Schulz iterations before an analysis is handed back
 constexpr float kStop = 0.05f;  // max |Z Y - I| that ends the iteration (after one more step)
 constexpr float kResidMax = 5e-3f;  // max |F| accepted from the first-order finish
+// Accuracy gates.  A is formed in FP32 from the Gram, a backward error of
+// about eps32 ||A||, so the symmetric inverse square root carries a relative
+// error of about eps32 kappa along the smallest eigenvalues (kappa =
+// lambda_max / lambda_min of P A P on the complement of 1); on the GPU,
+// analyses with kappa near 300 reached 1.8e-5 against FP64, those below 150
+// stayed under 2.2e-6.  The first-order finish adds about 1e-4 (kappa
+// max|F|)^2 (CPU model of this kernel's arithmetic).  s / delta >= kappa is
+// known before the iteration (s >= lambda_max, lambda_min >= delta), so an
+// analysis runs here only when s / delta <= kMaxCond, and its finish is
+// accepted only when max|F| <= kCondResid delta / s as well as kResidMax; the
+// others go to the SIMT kernel, whose factor rebuild keeps the small
+// eigenvalues' relative accuracy.
+constexpr float kMaxCond = 100.0f;
+constexpr float kCondResid = 0.1f;
+// max |Z Y - I| above which the iteration has left its basin (a convergent
+// iterate stays below 1); the analysis is handed back at once.
+constexpr float kDiverged = 4.0f;
 constexpr int kVarTile = 16;    // variables per update MMA (N): two 8-column TMEM loads
 
 // Operand region: 96 KB, 1024-byte aligned.
@@ -235,6 +254,9 @@ __device__ __forceinline__ void ns_coeffs(float& l, float& a, float& b) {
   const float ml = fminf(mu * l, 1.0f);
   l = ml * (3.0f - ml) * (3.0f - ml) * 0.25f;
 }
+
+// Maximum that a NaN poisons (fmaxf would drop it): NaN -> +inf.
+__device__ __forceinline__ float nan_max(float m, float x) { return (x != x) ? __int_as_float(0x7f800000) : fmaxf(m, x); }
 
 // FP64 decision for a candidate whose FP32 vertical distance is within 1e-4
 // of the support (kept out of line: a predicated FP64 instruction would
@@ -526,6 +548,19 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     const float s = fmaxf(fminf(ninf, fro), 1e-30f);
     const float is = 1.0f / s;
     float lsp = fminf(delta * is, 1.0f);  // lower end of the spectrum of Z Y (upper end 1)
+    // Points handed to the SIMT Jacobi kernel: nothing is written for them here.
+    auto hand_back = [&]() {
+      if (tid == 0) {
+        const unsigned long long slot = atomicAdd(prm.n_redo, 1ull);
+        prm.redo_out[slot] = (int32_t)(col * prm.nlev + lev);
+      }
+      __syncthreads();
+    };
+    const float l0 = lsp;  // delta / s, at most 1 / kappa
+    if (!(l0 * kMaxCond >= 1.0f)) {
+      hand_back();
+      continue;
+    }
     float nsa, nsb;
     ns_coeffs(lsp, nsa, nsb);
     // M = PAP / s + 1 1^T / k (identity on unused member slots); STACK <- [I; M]
@@ -554,6 +589,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     int its = 0;
     bool stop = false;  // decided from max |Z Y - I| of the current iterate
     bool conv = false;
+    bool diverged = false;
     for (;;) {
       // [Z; Y] <- [Z; Y] T
       operands_ready();
@@ -625,20 +661,29 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
           for (int j = 0; j < 8; ++j) {
             const int c = c0 + j;
             const float d = __uint_as_float(v[j]) - ((row == c) ? 1.0f : 0.0f);
-            emax = fmaxf(emax, fabsf(d));
+            emax = nan_max(emax, fabsf(d));
             t[j] = ((row == c) ? nsa - nsb : 0.0f) - nsb * d;  // a I - b P, P = I + d
           }
           put_col8(TBH, TBL, row, c0, 64, t);
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, off));
-        // a NaN compares false: treat it as not converged
         if (lane == 0 && !(emax < kStop)) atomicOr(&s_flag[0], 1u);
+        if (lane == 0 && !(emax < kDiverged)) atomicOr(&s_flag[0], 2u);
       }
       __syncthreads();
-      stop = s_flag[0] == 0u;
+      const unsigned fl = s_flag[0];
+      stop = fl == 0u;
+      if (fl & 2u) {
+        diverged = true;
+        break;
+      }
     }
     if (!alive) break;
+    if (diverged) {
+      hand_back();
+      continue;
+    }
 
     // ---------------- 4. finish ----------------
     // The iterate is Z = p(M) up to rounding errors that the coupled
@@ -705,7 +750,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
           const float pij = (row < k && c < k) ? (((row == c) ? 1.0f : 0.0f) - ik) : 0.0f;
           const float x = (row < k && c < k) ? __uint_as_float(v[j]) - pij : 0.0f;
           f[j] = x;
-          fm = fmaxf(fm, fabsf(x));
+          fm = nan_max(fm, fabsf(x));
           fu += x * V.u[c];
         }
         put_col8(TBH, TBL, row, c0, 64, f);
@@ -742,14 +787,9 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     }
     if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
     mma_ph ^= 1u;
-    const bool redo = !conv || !(resid <= kResidMax);
+    const bool redo = !conv || !(resid <= fminf(kResidMax, kCondResid * l0));
     if (redo) {
-      // handed to the SIMT Jacobi kernel; nothing written for this point
-      if (tid == 0) {
-        const unsigned long long slot = atomicAdd(prm.n_redo, 1ull);
-        prm.redo_out[slot] = (int32_t)(col * prm.nlev + lev);
-      }
-      __syncthreads();
+      hand_back();
       continue;
     }
     if (rowwarp) {  // W rows -> U^T = W^T into STACK rows 0-63 (A operand of the update)

@@ -145,3 +145,26 @@ def test_fp32_member_storage_highres_shape(dev, k):
     want = ob.letkf_points(Xw, base, c.nvar, c.var_stride, HXo, c.yo, c.rvar, poff, pidx, pw, c.rho, ob.ORC_RTPS)
     got = X32.double().cpu().numpy()
     assert rel_err(_gather(got, c, base), want) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("sigma_o", [0.2, 0.01])
+def test_ill_conditioned_points_go_to_the_simt_kernel(dev, sigma_o):
+    """Accurate obs over a wide support make the deflated local matrix far
+    worse conditioned than 3-pass TF32 products resolve.  Such points (a lower
+    spectrum bound below the threshold, an iteration that leaves its basin,
+    a finish residual above the bar) are re-run by the SIMT kernel: no
+    non-finite value reaches the output, and every point matches the
+    SIMT-only run (the re-run points bit for bit, since the SIMT kernel
+    treats each point alone) and, on sampled columns, the oracle."""
+    c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=4, nvar=2, k=64, p=40_000, T=20, sigma_o=sigma_o,
+                              hsupport_km=900.0, case=46)
+    got, HX, off, idx, dist, st = _run(dev, c)
+    print(f"sigma_o {sigma_o}: {st.n_fallback} of {st.n_points} points re-run, max residual {st.max_residual:.2e}")
+    assert st.tensor_path == 1 and st.n_fallback > 0
+    assert np.isfinite(got).all()
+    simt, _, _, _, _, st2 = _run(dev, c, flags=_lib.MG_SOLVE_SIMT)
+    assert st2.tensor_path == 0
+    assert rel_err(got, simt) <= MIXED_TOL
+    cols = np.random.default_rng(3).choice(c.nlat * c.nlon, 80, replace=False)
+    base, want = _oracle(c, HX, off, idx, dist, cols, 0)
+    assert rel_err(_gather(got, c, base), want) <= MIXED_TOL
