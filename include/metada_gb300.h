@@ -342,14 +342,22 @@ int mg_gemm_bf16_tc_wait_selftest(mg_context* ctx, const void* A, const void* B,
  * text length (MG_ERR_CAPACITY, without writing, if out is NULL or cap is
  * smaller).
  *
- * Numbers are converted exactly as strtod/printf do (device fast paths,
- * host for the rest).  No counterpart for the device placement in the
- * reference. */
+ * Numbers are converted exactly as strtod/printf do.  The device reads
+ * every number whose result is a normal double (Clinger's fast path, else
+ * Eisel-Lemire; more than 19 significant digits when the two 19-digit
+ * bounds round alike) and writes every value below 2^53 in magnitude; the
+ * rest (subnormal or overflowing results, the rare long mantissas whose
+ * bounds round apart, large or non-finite values to write) goes through
+ * the host's std::istringstream / std::ostream, the reference's own
+ * conversions.  mg_last_io_host_items gives how many lines (parsers) or
+ * values (writer) of the last such call on the context went that way.  No
+ * counterpart for the device placement in the reference. */
 int mg_parse_grid_obs(mg_context* ctx, const char* text, int64_t nbytes, double missing_value, int32_t* xyz,
                       double* vals, int64_t cap, int64_t* count);
 int mg_parse_values(mg_context* ctx, const char* text, int64_t nbytes, double* out, int64_t cap, int64_t* count);
 int mg_format_state(mg_context* ctx, const double* values, int32_t nx, int32_t ny, char* out, int64_t cap,
                     int64_t* nbytes);
+int mg_last_io_host_items(mg_context* ctx, int64_t* count);
 
 /* Nearest grid node of geographic observations on a curvilinear nx x ny
  * grid (node n = j*nx + i at node_lat[n], node_lon[n], degrees), replacing

@@ -180,6 +180,7 @@ _SIGNATURES = {
     "mg_parse_grid_obs": [c_void_p, c_char_p, c_int64, c_double, c_void_p, c_void_p, c_int64, POINTER(c_int64)],
     "mg_parse_values": [c_void_p, c_char_p, c_int64, c_void_p, c_int64, POINTER(c_int64)],
     "mg_format_state": [c_void_p, c_void_p, c_int32, c_int32, c_void_p, c_int64, POINTER(c_int64)],
+    "mg_last_io_host_items": [c_void_p, POINTER(c_int64)],
     "mg_nearest_node": [c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_int64, c_void_p,
                         c_int32, c_void_p, c_void_p, c_void_p],
     "mg_enkf": [c_void_p, c_void_p, c_int64, c_int32, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_int64,

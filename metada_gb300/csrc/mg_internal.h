@@ -20,6 +20,7 @@ struct mg_context {
   size_t host_stage_bytes = 0;
   std::string last_error;
   mg_letkf_stats stats{};
+  int64_t io_host_items = 0;  // lines or values the last text I/O call converted on the host
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // stage timing
 };
 

@@ -12,10 +12,18 @@
 //   * double: skip white space, [sign] (digits [. digits] | . digits)
 //     [(e|E) [sign] digits]; no inf/nan/hex (libstdc++ rejects them);
 //   * the next extraction starts right after the previous one.
-// Decimal to binary: a mantissa of at most 19 digits that is below 2^53 with
-// a decimal exponent in [-22, 22] is converted by one correctly rounded
-// multiplication or division by an exact power of ten (Clinger's fast path),
-// which equals strtod; every other number sends its line to the host, where
+// Decimal to binary, each step exact (equal to strtod):
+//   * a mantissa below 2^53 with a decimal exponent in [-22, 22]: one
+//     correctly rounded multiplication or division by an exact power of ten
+//     (Clinger's fast path);
+//   * any other mantissa of at most 19 significant digits: the Eisel-Lemire
+//     algorithm (a 128-bit product with a table of powers of five), when the
+//     result is a normal double;
+//   * more than 19 significant digits: the first 19 (w) decide alone when
+//     the dropped digits are zeros, otherwise w and w + 1 are converted and
+//     the result stands when both give the same double.
+// Numbers left over (subnormal or overflowing results, and the rare long
+// mantissas whose two bounds round apart) send their line to the host, where
 // std::istringstream (the reference's own extraction) reads it.
 // The writer prints "%12.6f" values (std::fixed, setprecision(6),
 // setw(12)) joined by one space, one row of x values per line: |v| < 2^53
@@ -31,6 +39,7 @@
 #include <vector>
 
 #include "mg_internal.h"
+#include "mg_pow5.h"
 
 namespace {
 
@@ -110,14 +119,55 @@ __device__ const double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  
                                       1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
 __device__ __forceinline__ double pow10_exact(int e) { return kPow10[e]; }
 
+// The double nearest w * 10^q (w != 0) by the Eisel-Lemire algorithm
+// (D. Lemire, "Number Parsing at a Gigabyte per Second", Software: Practice
+// and Experience 51(8), 2021; N. Mushtak and D. Lemire, "Fast number parsing
+// without fallback", 2023, show that the 128-bit product always decides for
+// binary64): w normalised, multiplied by the table's 128-bit significand of
+// 5^q (the low word only when the high product's low 9 bits are all ones),
+// the top 54 bits rounded to nearest even, the binary exponent from
+// floor(q log2(10)) = (217706 q) >> 16.  False when the result is not a
+// normal double (the host converts those).
+__device__ bool eisel_lemire(unsigned long long w, int q, unsigned long long& bits) {
+  if (q < MG_POW5_QMIN || q > MG_POW5_QMAX) return false;
+  const int lz = __clzll((long long)w);
+  w <<= lz;
+  const int idx = 2 * (q - MG_POW5_QMIN);
+  const unsigned long long th = kPow5Table[idx], tl = kPow5Table[idx + 1];
+  unsigned long long hi = __umul64hi(w, th), lo = w * th;
+  if ((hi & 0x1FFull) == 0x1FFull) {
+    const unsigned long long p2 = __umul64hi(w, tl);
+    lo += p2;
+    if (p2 > lo) ++hi;
+  }
+  const int upper = (int)(hi >> 63);
+  const int shift = upper + 9;
+  unsigned long long mant = hi >> shift;
+  int power2 = (int)(((217706ll * q) >> 16) + 63) + upper - lz + 1023;
+  if (power2 <= 0) return false;
+  // an exact halfway point (nothing below the kept bits) rounds to even
+  if (lo <= 1 && q >= -4 && q <= 23 && (mant & 3ull) == 1ull && (mant << shift) == hi) mant &= ~1ull;
+  mant += mant & 1ull;
+  mant >>= 1;
+  if (mant >= (2ull << 52)) {
+    mant = 1ull << 52;
+    ++power2;
+  }
+  mant &= ~(1ull << 52);
+  if (power2 >= 0x7FF) return false;
+  bits = ((unsigned long long)power2 << 52) | mant;
+  return true;
+}
+
 // Returns 1 on success, 0 on a failed extraction, 2 if the number is valid
-// but outside the exact fast path (the host converts it).
+// but not converted on the device (the host converts it).
 __device__ int extract_double(const char* t, int64_t& pos, int64_t end, double& out) {
   while (pos < end && is_ws(t[pos])) ++pos;
   bool neg = false;
   if (pos < end && (t[pos] == '+' || t[pos] == '-')) neg = t[pos++] == '-';
   unsigned long long m = 0;
-  int sig = 0, drop = 0, frac = 0, ndig = 0;
+  int sig = 0, drop_int = 0, frac = 0, ndig = 0;
+  bool nz_drop = false;  // a nonzero digit beyond the first 19 significant ones
   while (pos < end && is_digit(t[pos])) {
     const int d = t[pos++] - '0';
     ++ndig;
@@ -126,7 +176,8 @@ __device__ int extract_double(const char* t, int64_t& pos, int64_t end, double& 
       m = m * 10 + d;
       ++sig;
     } else {
-      ++drop;  // digit beyond 19 significant ones
+      ++drop_int;  // an integer digit beyond 19 significant ones scales by ten
+      nz_drop |= d != 0;
     }
   }
   if (pos < end && t[pos] == '.') {
@@ -143,7 +194,7 @@ __device__ int extract_double(const char* t, int64_t& pos, int64_t end, double& 
         ++sig;
         ++frac;
       } else {
-        ++drop;  // a digit beyond 19 significant ones: not exact, the host converts
+        nz_drop |= d != 0;  // a fractional digit beyond 19 significant ones
       }
     }
   }
@@ -166,11 +217,19 @@ __device__ int extract_double(const char* t, int64_t& pos, int64_t end, double& 
     out = neg ? -0.0 : 0.0;
     return 1;
   }
-  if (drop > 0) return 2;
-  const int e10 = ex - frac;
-  if (m >= (1ull << 53) || e10 < -22 || e10 > 22) return 2;
-  const double md = (double)m;  // exact
-  const double v = e10 >= 0 ? __dmul_rn(md, pow10_exact(e10)) : __ddiv_rn(md, pow10_exact(-e10));
+  const int e10 = ex - frac + drop_int;
+  double v;
+  if (!nz_drop && m < (1ull << 53) && e10 >= -22 && e10 <= 22) {
+    const double md = (double)m;  // exact
+    v = e10 >= 0 ? __dmul_rn(md, pow10_exact(e10)) : __ddiv_rn(md, pow10_exact(-e10));
+  } else {
+    unsigned long long b0 = 0, b1 = 0;
+    if (!eisel_lemire(m, e10, b0)) return 2;
+    // dropped nonzero digits: the value lies strictly between m and m + 1
+    // (times 10^e10), so both bounds rounding alike decide it
+    if (nz_drop && (!eisel_lemire(m + 1, e10, b1) || b1 != b0)) return 2;
+    v = __longlong_as_double((long long)b0);
+  }
   out = neg ? -v : v;
   return 1;
 }
@@ -563,6 +622,7 @@ int with_lines(mg_context* ctx, const char* text, int64_t nbytes, F&& body) {
 std::vector<int64_t> host_lines(mg_context* ctx, const int32_t* flags, int64_t L, int32_t want, const int32_t* nflag,
                                 int* rc) {
   *rc = MG_OK;
+  ctx->io_host_items = 0;
   if (L == 0) return {};
   int32_t nf = 0;
   if (cudaMemcpyAsync(&nf, nflag, sizeof(nf), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
@@ -580,6 +640,7 @@ std::vector<int64_t> host_lines(mg_context* ctx, const int32_t* flags, int64_t L
   std::vector<int64_t> out;
   for (int64_t l = 0; l < L; ++l)
     if (h[l] == want) out.push_back(l);
+  ctx->io_host_items = (int64_t)out.size();
   return out;
 }
 
@@ -760,6 +821,12 @@ int mg_parse_values(mg_context* ctx, const char* text, int64_t nbytes, double* o
     release();
     return MG_OK;
   });
+}
+
+int mg_last_io_host_items(mg_context* ctx, int64_t* count) {
+  if (!ctx || !count) return MG_ERR_ARG;
+  *count = ctx->io_host_items;
+  return MG_OK;
 }
 
 int mg_format_state(mg_context* ctx, const double* values, int32_t nx, int32_t ny, char* out, int64_t cap,

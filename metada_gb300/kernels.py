@@ -139,6 +139,14 @@ def format_state(values: torch.Tensor, nx: int, ny: int) -> bytes:
     return buf[: nbytes.value].numpy().tobytes()
 
 
+def last_io_host_items(device: int = 0) -> int:
+    """Lines (parsers) or values (writer) of the last text I/O call on the
+    device's context that were converted on the host."""
+    n = c_int64(0)
+    context(device).call("mg_last_io_host_items", byref(n))
+    return n.value
+
+
 def nearest_node(node_lat: torch.Tensor, node_lon: torch.Tensor, nx: int, ny: int, obs_lat: torch.Tensor,
                  obs_lon: torch.Tensor, vcoord: torch.Tensor | None = None,
                  obs_level: torch.Tensor | None = None) -> tuple[torch.Tensor, torch.Tensor | None]:

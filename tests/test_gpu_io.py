@@ -76,7 +76,7 @@ def test_parse_grid_obs_line_rules_and_number_forms(dev):
         "0\t1\t3\t9\t0.7035\t-79.8571\t32.6471\t-999.0",   # missing value: dropped
         "0 1 5 6 .5 +1.25 -0.0 1e-3",
         "0 1 5 7 7.0e+1 1E2 3.5E-2 -0.0",
-        "0 1 5 8 0.1 0.2 0.3 123456789012345678901234.5",    # long mantissa: host path
+        "0 1 5 8 0.1 0.2 0.3 123456789012345678901234.5",    # 25 digits: both 19-digit bounds round alike
         "0 1 5 9 0.1 0.2 0.3 4.9e-324",                      # subnormal: host path
         "bad line with words",
         "0 1 5",                                             # too few fields
@@ -101,6 +101,7 @@ def test_parse_grid_obs_line_rules_and_number_forms(dev):
     got = vals.cpu().numpy()
     assert np.array_equal(got, w[:, 3:])
     assert math.copysign(1.0, got[1, 2]) < 0 and math.copysign(1.0, got[2, 3]) < 0  # -0.0 kept
+    assert K.last_io_host_items() == 1  # only the subnormal's line went to the host
 
 
 @pytest.mark.parametrize("nx,ny", [(36, 18), (360, 180)])
@@ -175,3 +176,61 @@ def test_save_ensemble_writes_the_reference_text(dev, tmp_path):
     assert (tmp_path / "out" / "analysis_mean.txt").read_bytes() == text(ens.Mean())
     for i in range(k):
         assert (tmp_path / "out" / f"analysis_member_{i}.txt").read_bytes() == text(X[i])
+
+
+def _number_strings(rng, n, digits_lo, digits_hi):
+    """Decimal strings of normal doubles in the forms std::istream reads:
+    random significant digits, a decimal point anywhere (or none), an
+    optional exponent (e/E, signed), an optional sign."""
+    out = []
+    for _ in range(n):
+        nd = int(rng.integers(digits_lo, digits_hi + 1))
+        digs = str(int(rng.integers(1, 10))) + "".join(str(d) for d in rng.integers(0, 10, nd - 1))
+        point = int(rng.integers(0, nd + 1))
+        body = digs[:point] + "." + digs[point:] if point < nd else digs
+        if body.startswith("."):
+            body = "0" + body if rng.random() < 0.5 else body
+        mag = point  # decimal exponent of the leading digit + 1
+        e = int(rng.integers(-300 - mag + 2, 300 - mag))
+        s = body
+        if rng.random() < 0.8:
+            s += ("e" if rng.random() < 0.5 else "E") + (("+" if rng.random() < 0.3 else "") if e >= 0 else "") + str(e)
+        if rng.random() < 0.3:
+            s = "-" + s
+        out.append(s)
+    return out
+
+
+def _bits(a):
+    return np.asarray(a, dtype=np.float64).view(np.uint64)
+
+
+def test_parse_values_decides_normal_numbers_on_the_device(dev):
+    """Numbers of 1 to 19 significant digits whose values are normal doubles,
+    with exponents across the whole range: every one is converted on the
+    device (Clinger's path or Eisel-Lemire), bit for bit as Python's
+    correctly rounded float(); none goes to the host."""
+    rng = np.random.default_rng(11)
+    toks = _number_strings(rng, 40_000, 1, 19)
+    text = "\n".join(" ".join(toks[i:i + 10]) for i in range(0, len(toks), 10)).encode() + b"\n"
+    got = K.parse_values(text).cpu().numpy()
+    assert K.last_io_host_items() == 0
+    want = np.array([float(t) for t in toks])
+    assert np.array_equal(_bits(got), _bits(want))
+
+
+def test_parse_values_long_mantissas_and_the_host_rest(dev):
+    """20 to 40 significant digits: decided on the device when the two
+    19-digit bounds round alike (nearly always), otherwise by the host; a
+    line with a subnormal result goes to the host.  Every value bit for bit
+    as float()."""
+    rng = np.random.default_rng(12)
+    toks = _number_strings(rng, 20_000, 20, 40)
+    lines = [" ".join(toks[i:i + 10]) for i in range(0, len(toks), 10)]
+    lines.append("1.5 4.9e-324 2.5")
+    text = ("\n".join(lines) + "\n").encode()
+    got = K.parse_values(text).cpu().numpy()
+    host = K.last_io_host_items()
+    assert 1 <= host <= len(lines) // 20
+    want = np.array([float(t) for t in toks] + [1.5, 4.9e-324, 2.5])
+    assert np.array_equal(_bits(got), _bits(want))
