@@ -67,14 +67,15 @@ def parse():
     ap.add_argument("--train-batch", type=int, default=4096, help="column workload: columns per Adam step")
     ap.add_argument("--profile-case", default=None,
                     choices=["mixed", "fp64", "uneven", "uneven-small", "enkf", "metrics", "column",
-                             "column-small"],
+                             "column-small", "highres-small"],
                     help="run a profiler case and exit: mixed/fp64 = one batched LETKF on the reduced "
                          "180x90x10x4 case (125k obs); uneven = the 512-case mixed batch run twice without "
                          "the graph; uneven-small = its first 64 cases; enkf = the mixed EnKF (2.59M values, "
                          "k=64, 500k obs) twice; metrics = Metrics::CalculateAll of that ensemble twice; column = "
                          "H(x) of 200k column obs x 64 members (720x360 columns, 30 levels), plain and "
                          "surrogate (untrained weights), twice each; column-small = the same on 360x180 columns with "
-                         "50k obs (2 GB state)")
+                         "50k obs (2 GB state); highres-small = two cycles of the high-resolution LETKF (k=80, FP32 "
+                         "members, RTPS) on a 360x180x10x4 grid with 500k obs, 60%% clustered")
     return ap.parse_args()
 
 
@@ -400,6 +401,27 @@ def profile_case(precision_name: str) -> None:
         print(json.dumps({"profile_case": precision_name, "ms": ms}))
         return
 
+    if precision_name == "highres-small":
+        # the high-resolution configuration's analysis on a 360 x 180 x 10 x 4
+        # grid (k = 80 stored as FP32: 0.83 GB), 500k obs (60 % in patches)
+        c = syn.highres_letkf_case(dev, nlon=360, nlat=180, nlev=10, p=500_000)
+        la, lo = c.col_lat_lon()
+        clat, clon = torch.tensor(la, device=dev), torch.tensor(lo, device=dev)
+        col_base = torch.tensor(c.col_base(), device=dev)
+        rvar = torch.full_like(c.yo, c.sigma_o ** 2)
+        out = []
+        for _ in range(2):
+            HX = K.hx_latlon(c.X, c.nlon, c.nlat, c.nlev, c.obs_lat, c.obs_lon, c.obs_lev, c.obs_var)
+            off, idx, dist = K.select_geo(clat, clon, c.obs_lat, c.obs_lon, c.hsupport_km)
+            _, st = K.letkf_batched(c.X, col_base=col_base, nlev=c.nlev, n_var=c.nvar, lev_stride=c.lev_stride,
+                                    var_stride=c.var_stride, HX=HX, yo=c.yo, rvar=rvar, loc_off=off, loc_idx=idx,
+                                    loc_dist=dist, obs_lev=c.obs_lev, hsupport=c.hsupport_km, vsupport=c.vsupport,
+                                    rho=c.rho, flags=_lib.MG_RTPS, precision=_lib.MG_PREC_MIXED, want_mean=False)
+            torch.cuda.synchronize()
+            out.append({"ms_analysis": st.ms_analysis, "handed_back": st.n_fallback,
+                        "mean_local": st.total_local / max(1, st.n_points - st.n_empty), "max_local": st.max_local})
+        print(json.dumps({"profile_case": precision_name, "analyses": st.n_points, "cycles": out}))
+        return
     c = syn.latlon_letkf_case(nlon=180, nlat=90, nlev=10, nvar=4, k=64, p=125_000, T=45, case=40)
     w = Workload(c, dev)
     st = w.step(_lib.MG_PREC_MIXED if precision_name == "mixed" else _lib.MG_PREC_FP64)
@@ -932,8 +954,11 @@ def run_highres(args) -> None:
     ms_cycle = sum(ms)
     line = {"metric": "local analyses/s, high-resolution LETKF (FP32 members)", "value": st.n_points / (ms_cycle / 1e3),
             "unit": "analyses/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": ms_cycle,
-            "higher_is_better": True, "dtype": "f32 storage; FP32 anomalies and solve (SIMT two-stage Jacobi: "
-                                            "k = 80 > 64); FP64 means and innovations",
+            "higher_is_better": True,
+            "dtype": ("f32 storage; 3-pass TF32 tensor-core Gram, Newton-Schulz solve and update (96-slot layout), "
+                      "handed-back points on the SIMT two-stage solve; FP64 means and innovations"
+                      if st.tensor_path else
+                      "f32 storage; FP32 anomalies and SIMT two-stage Jacobi solve; FP64 means and innovations"),
             "data": "synthetic (seeded Gaussian random fields on the GPU)",
             "config": {"workload": "1440x720 grid, 30 levels, 4 vars (124.4M values), k=80 (FP32), 5M obs "
                                    "(60% in 20 Gaussian patches of 800 km), 300 km / 2 levels, RTPS 0.9",
@@ -941,7 +966,8 @@ def run_highres(args) -> None:
                                "cycle's output with the same obs)"},
             "ms": {"hx": ms[0], "search": ms[1], "analysis_call": ms[2], "analysis_kernel": st.ms_analysis,
                    "generation_s": t_gen},
-            "analyses": st.n_points, "tensor_path": st.tensor_path,
+            "analyses": st.n_points, "tensor_path": st.tensor_path, "handed_back_to_simt": st.n_fallback,
+            "solver_iterations_per_analysis": st.total_sweeps / max(1, st.n_points - st.n_empty),
             "local_obs": {"mean_per_analysis": st.total_local / max(1, st.n_points - st.n_empty),
                           "max_per_analysis": st.max_local, "empty_points": st.n_empty,
                           "column_candidates_histogram": {"edges": edges.tolist(), "counts": hist.tolist()},

@@ -915,7 +915,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
       fb.warm_start = 0;
       fb.next = cnt + 6;  // reused as the work counter of the re-run
       MG_TRY_CUDA(cudaMemsetAsync(cnt + 6, 0, sizeof(unsigned long long), s));
-      rc = launch_batched<float, 64>(ctx, fb);
+      rc = (k <= 64) ? launch_batched<float, 64>(ctx, fb) : launch_batched<float, 96>(ctx, fb);
     }
   } else if (fp64) {
     if (k <= 32) rc = launch_batched<double, 32>(ctx, prm);

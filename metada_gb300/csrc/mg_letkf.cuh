@@ -68,11 +68,12 @@ __device__ __forceinline__ T gaspari_cohn(T z) {
          T(2) / (T(3) * z);
 }
 
-// Tensor-core local analyses (mixed precision, Hunt transform, k <= 64):
+// Tensor-core local analyses (mixed precision, Hunt transform, k <= 96):
 // true when this build and the parameters take that path.
 bool letkf_tc_supported(const LetkfParams& prm);
-// Launches them on `stream` as a persistent grid (two CTAs per SM when they
-// fit); returns a cudaError_t value (0 on success) and the CTA count.
+// Launches them on `stream` as a persistent grid (two CTAs per SM for
+// k <= 64, one for 64 < k <= 96); returns a cudaError_t value (0 on success)
+// and the CTA count.
 int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream, int* ctas);
 
 }  // namespace mg

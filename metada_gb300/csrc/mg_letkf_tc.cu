@@ -1,5 +1,5 @@
 // Batched LETKF local analyses on the tensor cores (mixed precision, Hunt
-// transform, k <= 64): the k x k Gram Y'^T R^-1 Y', the products of the
+// transform, k <= 96): the k x k Gram Y'^T R^-1 Y', the products of the
 // symmetric inverse square root and the update X' W all run as tcgen05.mma
 // kind::tf32 products with an error-compensated 3-pass split
 // (hi*hi + hi*lo + lo*hi, hi = x rounded to TF32, lo = x - hi), accumulated in
@@ -8,8 +8,17 @@
 // (LETKF.hpp:214-238) in the Hunt et al. (2007) form with Gaspari-Cohn
 // R-localisation.
 //
-// Per local analysis (one CTA of 256 threads, two CTAs per SM, persistent,
-// points pulled longest list first from a work counter):
+// Two instantiations by member slots KP:
+//  * KP = 64 (k <= 64): 256 threads, two CTAs per SM (256 TMEM columns each);
+//    Z and Y are stacked as the 128 rows of one operand, so [Z; Y] T is one
+//    M = 128 product.
+//  * KP = 96 (64 < k <= 96, the high-resolution configuration's k = 80): 384
+//    threads, one CTA per SM with all 512 TMEM columns and 216 KB of
+//    operands; Z, Y and T are separate 96-row operands and [Z; Y] T is two
+//    products.
+//
+// Per local analysis (one CTA, persistent, points pulled longest list first
+// from a work counter):
 //  1. Gram: the candidate list is filtered and weighted, the kept rows
 //     sqrt(w) Y'_o are gathered 64 at a time into a K-major, 128-byte
 //     swizzled operand (members x obs) with sqrt(w) d_o as an extra row, and
@@ -22,10 +31,10 @@
 //     s = min(||A||_inf, ||PAP||_F) >= lambda_max keeps M's spectrum in (0, 1].
 //  3. Coupled Newton-Schulz with scaled steps: T = a I - b Z Y (a, b from
 //     ns_coeffs: the classic (3I - Z Y)/2 after scaling Z and Y by sqrt(mu),
-//     mu from the known spectrum bounds [delta/s, 1]), [Z; Y] <- [Z; Y] T, with
-//     Z and Y stacked as the 128 rows of one MMA operand; it stops once
-//     max |Z Y - I| < 0.05 (one more step squares that error).  Z -> M^-1/2,
-//     and A^-1/2 = (Z - 1 1^T / k) / sqrt(s) on the complement of 1.
+//     mu from the known spectrum bounds [delta/s, 1]), [Z; Y] <- [Z; Y] T; it
+//     stops once max |Z Y - I| < 0.05 (one more step squares that error).
+//     Z -> M^-1/2, and A^-1/2 = (Z - 1 1^T / k) / sqrt(s) on the complement
+//     of 1.
 //  4. First-order finish from the matrix itself: C = Z^T A Z, F = C - P,
 //     W = sqrt((k-1) c) Z (I - F/2), wa = c Z (P - F) Z^T b (c = rho for the
 //     reference's inflation placement, else 1).  max |F| is the per-analysis
@@ -34,7 +43,8 @@
 //     residual is above the gates (kResidMax, kCondResid delta / s) or whose
 //     values are not finite are listed and re-run by the SIMT Jacobi kernel.
 //  5. Update: D = W^T X'^T (members x variables) on the tensor core, then
-//     x_a = x_mean + X' wa + D (+ RTPS relaxation), written in FP64.
+//     x_a = x_mean + X' wa + D (+ RTPS relaxation), written in FP64 (or FP32
+//     storage).
 // Every mbarrier wait is bounded in time; a wait that gives up makes the CTA
 // set the status word, drain its own MMAs (bounded) and free its TMEM.
 #include <cuda_runtime.h>
@@ -47,12 +57,9 @@ namespace {
 
 using namespace mg::t5;
 
-constexpr int kThreads = 256;
-constexpr int KP = 64;          // member slots
 constexpr int kChunk = 64;      // obs per Gram chunk: two 128-byte swizzle atoms of TF32
-constexpr int kGramN = 80;      // Gram MMA N: 64 member rows, the innovation row, 15 unused
 constexpr int kNBuf = 2;        // Gram chunk buffers
-constexpr int kSelRing = 512;   // selected-entry ring (a 256-candidate block + carry-over < 32)
+constexpr int kSelRing = 512;   // selected-entry ring (a candidate block + carry-over < kChunk)
 constexpr int kMaxIt = 14;      // Newton-Schulz iterations before an analysis is handed back
 constexpr float kStop = 0.05f;  // max |Z Y - I| that ends the iteration (after one more step)
 constexpr float kResidMax = 5e-3f;  // max |F| accepted from the first-order finish
@@ -75,45 +82,71 @@ constexpr float kCondResid = 0.1f;
 constexpr float kDiverged = 4.0f;
 constexpr int kVarTile = 16;    // variables per update MMA (N): two 8-column TMEM loads
 
-// Operand region: 96 KB, 1024-byte aligned.
-//   Newton-Schulz view: STACK (128 rows x 64 columns, two 16 KB slabs, hi
-//   and lo copies) and TB (64 rows x 64 columns, two 8 KB slabs, hi and lo).
-//   Gram view: two chunk buffers of 40 KB (64 obs: two 10 KB slabs, hi and lo).
-constexpr uint32_t kSlabS = 128 * 128;  // STACK slab / Gram slab
-constexpr uint32_t kSlabT = 64 * 128;   // TB slab
-constexpr uint32_t OFF_STACK_HI = 0;
-constexpr uint32_t OFF_STACK_LO = 2 * kSlabS;
-constexpr uint32_t OFF_TB_HI = 4 * kSlabS;
-constexpr uint32_t OFF_TB_LO = OFF_TB_HI + 2 * kSlabT;
-constexpr uint32_t kRegion = OFF_TB_LO + 2 * kSlabT;  // 96 KB
-// Gram chunk: 80 operand rows per slab (64 members, the innovation row, 15
-// unused) so a slab is 10 KB; as the 128-row A operand a slab's last 48 rows
-// read the next slab (their products land in unused accumulator rows).
-constexpr int kGramRows = 80;
-constexpr uint32_t kGramSlab = kGramRows * 128;
-constexpr uint32_t kGramBuf = 4 * kGramSlab;  // hi (2 slabs), lo (2 slabs)
-static_assert(kGramSlab % 1024 == 0, "swizzle atoms are 1024-byte aligned");
-static_assert(kNBuf * kGramBuf + (128 - kGramRows) * 128 <= kRegion, "Gram buffers and the A-operand overhang");
-
-// Tensor memory: columns [0, 64) product scratch, [128, 208) the Gram.
-constexpr uint32_t kTmemCols = 256;
-constexpr uint32_t kTmGram = 128;
-
-// Vectors after the operand region.
-struct Vecs {
-  float b[KP], r[KP], u[KP], v[KP], wa[KP];
-  float part[4][KP];
-  float red[16];
-  float xsq[kVarTile], inc[kVarTile], fac[kVarTile], one[kVarTile];
-  float ssa[2][kVarTile];
-  double xm[kVarTile];
-  int sel_o[kSelRing];
-  float sel_sw[kSelRing];
-  float sel_sd[kSelRing];
-  int wcnt[kThreads / 32];
+// Shared and tensor memory of one CTA, by member slots KP (a multiple of 32).
+// Every operand is K-major with the 128-byte swizzle: a slab holds 32 TF32
+// columns of all its rows (128 bytes per row), with a hi and a lo copy.
+//   KP = 64: STACK (Z in rows 0-63, Y in rows 64-127; 16 KB slabs) and T
+//   (64 rows, 8 KB slabs): 96 KB.
+//   KP = 96: Z, Y and T, each 96 rows in 12 KB slabs: 216 KB.  As a 128-row
+//   A operand, Z's and Y's last 32 rows read the following 4 KB (the lo copy
+//   or the next operand); those products land in TMEM lanes 96-127, never read.
+// Gram view of the same region: two chunk buffers of KP + 16 rows (KP
+// members, the innovation row, 15 unused), then the selected-entry ring.
+template <int KP>
+struct Lay {
+  static_assert(KP == 64 || KP == 96, "member slots");
+  static constexpr int NG = KP / 32;          // 32-column groups = TMEM lane quadrants holding rows
+  static constexpr int kThreads = 128 * NG;   // four lane quadrants x NG column groups of warps
+  static constexpr int kWarps = kThreads / 32;
+  static constexpr bool kStack = KP == 64;    // [Z; Y] as one 128-row operand
+  static constexpr int kMinBlocks = kStack ? 2 : 1;
+  static constexpr uint32_t ZR = kStack ? 128u : (uint32_t)KP;  // rows per slab of Z and Y
+  static constexpr uint32_t TR = KP;                            // rows per slab of T
+  static constexpr uint32_t kSlabZ = ZR * 128u;
+  static constexpr uint32_t kSlabT = TR * 128u;
+  static constexpr uint32_t OFF_Z_HI = 0;
+  static constexpr uint32_t OFF_Z_LO = NG * kSlabZ;
+  static constexpr uint32_t OFF_Y_HI = kStack ? OFF_Z_HI + KP * 128u : 2 * NG * kSlabZ;
+  static constexpr uint32_t OFF_Y_LO = kStack ? OFF_Z_LO + KP * 128u : 3 * NG * kSlabZ;
+  static constexpr uint32_t OFF_T_HI = (kStack ? 2 : 4) * NG * kSlabZ;
+  static constexpr uint32_t OFF_T_LO = OFF_T_HI + NG * kSlabT;
+  static constexpr uint32_t kRegion = OFF_T_LO + NG * kSlabT;
+  static constexpr int kGramRows = KP + 16;
+  static constexpr int kGramN = KP + 16;      // Gram MMA N: members, the innovation row, 15 unused
+  static constexpr uint32_t kGramSlab = kGramRows * 128u;
+  static constexpr uint32_t kGramBuf = 4 * kGramSlab;  // hi (2 slabs), lo (2 slabs)
+  static constexpr uint32_t OFF_SEL = kNBuf * kGramBuf + (128 - kGramRows) * 128u;
+  static constexpr uint32_t kSelBytes = kSelRing * 12u;  // obs index, sqrt(w), sqrt(w) d
+  // Tensor memory: product scratch at column 0 (and a second product at
+  // kTmB for KP = 96), the Gram at kTmGram.
+  static constexpr uint32_t kTmemCols = kStack ? 256u : 512u;
+  static constexpr uint32_t kTmB = 128;
+  static constexpr uint32_t kTmGram = kStack ? 128u : 256u;
+  static_assert(kGramSlab % 1024 == 0 && kSlabZ % 1024 == 0 && kSlabT % 1024 == 0,
+                "swizzle atoms are 1024-byte aligned");
+  static_assert(OFF_SEL + kSelBytes <= kRegion, "Gram buffers, A-operand overhang and the ring");
+  static_assert(kStack || (kTmB + KP <= kTmGram && kTmGram + kGramN <= kTmemCols), "tensor memory");
+  static_assert(kSelRing >= kThreads + kChunk, "ring holds a candidate block and the carry-over");
 };
 
-constexpr size_t kSmemBytes = 1024 + kRegion + sizeof(Vecs);
+// Vectors after the operand region.
+template <int KP>
+struct Vecs {
+  static constexpr int NG = KP / 32;
+  float b[KP], r[KP], u[KP], v[KP], wa[KP];
+  float part[2 * NG][KP];
+  float red[32];
+  float xsq[kVarTile], inc[kVarTile], fac[kVarTile], one[kVarTile];
+  float ssa[NG][kVarTile];
+  double xm[kVarTile];
+  int wcnt[Lay<KP>::kWarps];
+};
+
+template <int KP>
+constexpr size_t smem_bytes() {
+  return 1024 + Lay<KP>::kRegion + sizeof(Vecs<KP>);
+}
+static_assert(smem_bytes<96>() + 1024 <= 233472, "one KP = 96 CTA fits the SM's shared memory");
 
 // ---- operand addressing: K-major, 128-byte swizzle, TF32 in 32-bit words ----
 // Byte offset of element (row r, column c) in an operand whose slabs (32
@@ -265,14 +298,24 @@ __device__ __noinline__ bool vertical_keep_fp64(int lev, double obs_lev, double 
   return fabs((double)lev - obs_lev) <= vsupport;
 }
 
-__global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams prm) {
+template <int KP>
+__global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_tc_kernel(mg::LetkfParams prm) {
+  using L = Lay<KP>;
+  constexpr int NG = L::NG;
+  constexpr int kThreads = L::kThreads;
+  constexpr uint32_t ZR = L::ZR, TR = L::TR;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* R = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  Vecs& V = *reinterpret_cast<Vecs*>(R + kRegion);
-  unsigned char* const STH = R + OFF_STACK_HI;
-  unsigned char* const STL = R + OFF_STACK_LO;
-  unsigned char* const TBH = R + OFF_TB_HI;
-  unsigned char* const TBL = R + OFF_TB_LO;
+  Vecs<KP>& V = *reinterpret_cast<Vecs<KP>*>(R + L::kRegion);
+  unsigned char* const ZH = R + L::OFF_Z_HI;
+  unsigned char* const ZL = R + L::OFF_Z_LO;
+  unsigned char* const YH = R + L::OFF_Y_HI;
+  unsigned char* const YL = R + L::OFF_Y_LO;
+  unsigned char* const TH = R + L::OFF_T_HI;
+  unsigned char* const TL = R + L::OFF_T_LO;
+  int* const sel_o = reinterpret_cast<int*>(R + L::OFF_SEL);
+  float* const sel_sw = reinterpret_cast<float*>(R + L::OFF_SEL + 4 * kSelRing);
+  float* const sel_sd = reinterpret_cast<float*>(R + L::OFF_SEL + 8 * kSelRing);
   __shared__ uint64_t mma_bar;
   __shared__ uint64_t buf_bar[kNBuf];
   __shared__ uint32_t tmem_s;
@@ -280,7 +323,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
   __shared__ unsigned s_flag[4];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int q = warp & 3, hh = warp >> 2;  // TMEM lane quadrant, column half
+  const int q = warp & 3, g = warp >> 2;  // TMEM lane quadrant, 32-column group
   const int k = prm.k;
   const float ik = 1.0f / (float)k;
   const float* __restrict__ Y = static_cast<const float*>(prm.Y);
@@ -299,15 +342,18 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     for (int b = 0; b < kNBuf; ++b) mbar_init(&buf_bar[b], 1);
     mbar_fence_init();
   }
-  if (warp == 0) tmem_alloc(&tmem_s, kTmemCols);
+  if (warp == 0) tmem_alloc(&tmem_s, L::kTmemCols);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_s;
   const uint32_t tm_row = ((uint32_t)(32 * q) << 16);  // this warp's TMEM lanes
   const uint32_t sR = smem_u32(R);
-  const uint32_t idesc64 = idesc_tf32_f32(128, 64);
-  const uint32_t idescG = idesc_tf32_f32(128, kGramN);
+  const uint32_t sZH = sR + L::OFF_Z_HI, sZL = sR + L::OFF_Z_LO;
+  const uint32_t sYH = sR + L::OFF_Y_HI, sYL = sR + L::OFF_Y_LO;
+  const uint32_t sTH = sR + L::OFF_T_HI, sTL = sR + L::OFF_T_LO;
+  const uint32_t idescK = idesc_tf32_f32(128, KP);
+  const uint32_t idescG = idesc_tf32_f32(128, L::kGramN);
   const uint32_t idescU = idesc_tf32_f32(128, kVarTile);
 
   uint32_t mma_ph = 0;      // parity of the next mma_bar phase
@@ -335,9 +381,9 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     auto load_rows = [&](int pos, int cnt, float (&x)[16], float& sd) {
       if (slot < cnt) {
         const int e = (pos + slot) & (kSelRing - 1);
-        const int o = V.sel_o[e];
-        const float sw = V.sel_sw[e];
-        sd = V.sel_sd[e];
+        const int o = sel_o[e];
+        const float sw = sel_sw[e];
+        sd = sel_sd[e];
         const float* yr = Y + (int64_t)o * k;
         if (vec4 && m0 + 16 <= k) {
 #pragma unroll
@@ -387,15 +433,15 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
         __syncthreads();
         int wb = 0, cnt = 0;
 #pragma unroll
-        for (int w = 0; w < kThreads / 32; ++w) {
+        for (int w = 0; w < L::kWarps; ++w) {
           if (w < warp) wb += V.wcnt[w];
           cnt += V.wcnt[w];
         }
         if (keep) {
           const int pos = (head + nsel + wb + __popc(bal & ((1u << lane) - 1u))) & (kSelRing - 1);
-          V.sel_o[pos] = o;
-          V.sel_sw[pos] = sw;
-          V.sel_sd[pos] = sd;
+          sel_o[pos] = o;
+          sel_sw[pos] = sw;
+          sel_sd[pos] = sd;
         }
         __syncthreads();
         nsel += cnt;
@@ -410,18 +456,18 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
         const int b = (int)(gchunk % kNBuf);
         const uint32_t use = gchunk / kNBuf;
         if (use > 0 && !wait_all(&buf_bar[b], (use - 1) & 1u)) { alive = false; break; }
-        unsigned char* bh = R + b * kGramBuf;
-        unsigned char* bl = bh + 2 * kGramSlab;
+        unsigned char* bh = R + b * L::kGramBuf;
+        unsigned char* bl = bh + 2 * L::kGramSlab;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const uint32_t off = sw_off(m0 + j, slot, kGramRows);
+          const uint32_t off = sw_off(m0 + j, slot, L::kGramRows);
           float h, l;
           split(x[j], h, l);
           *reinterpret_cast<float*>(bh + off) = h;
           *reinterpret_cast<float*>(bl + off) = l;
         }
         if (m0 == 0) {  // the innovation row
-          const uint32_t off = sw_off(KP, slot, kGramRows);
+          const uint32_t off = sw_off(KP, slot, L::kGramRows);
           float h, l;
           split(sdv, h, l);
           *reinterpret_cast<float*>(bh + off) = h;
@@ -434,9 +480,9 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
         operands_ready();
         if (warp == 0) {
           tc_fence_after();
-          const uint32_t a = sR + b * kGramBuf;
-          issue3(tmem + kTmGram, a, a + 2 * kGramSlab, kGramSlab, a, a + 2 * kGramSlab, kGramSlab, 2, idescG,
-                 nch > 0);
+          const uint32_t a = sR + b * L::kGramBuf;
+          issue3(tmem + L::kTmGram, a, a + 2 * L::kGramSlab, L::kGramSlab, a, a + 2 * L::kGramSlab, L::kGramSlab, 2,
+                 idescG, nch > 0);
           mma_commit_elect(&buf_bar[b]);
         }
         ++gchunk;
@@ -466,17 +512,17 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     mma_ph ^= 1u;
 
     // ---------------- 2. A, b, deflation and scaling ----------------
-    // Warps of quadrants 0-1 hold rows 0-63 (their TMEM lanes), column half
-    // hh; each walks its 32 columns 8 at a time.
-    const bool rowwarp = q < 2;
+    // Warps of quadrants 0 .. NG-1 hold rows 0 .. KP-1 (their TMEM lanes),
+    // column group g; each walks its 32 columns 8 at a time.
+    const bool rowwarp = q < NG;
     const int row = 32 * q + lane;
-    const int cb = 32 * hh;
+    const int cb = 32 * g;
     if (rowwarp) {
       float rs = 0.0f, as = 0.0f;
 #pragma unroll 1
       for (int c0 = cb; c0 < cb + 32; c0 += 8) {
         uint32_t v[8];
-        tmem_ld8(tmem + tm_row + kTmGram + c0, v);
+        tmem_ld8(tmem + tm_row + L::kTmGram + c0, v);
         tmem_wait_ld();
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -488,19 +534,26 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
           }
         }
       }
-      V.part[hh][row] = rs;
-      V.part[2 + hh][row] = as;
-      if (hh == 0) {
-        const uint32_t bv = tmem_ld1(tmem + tm_row + kTmGram + KP);
+      V.part[g][row] = rs;
+      V.part[NG + g][row] = as;
+      if (g == 0) {
+        const uint32_t bv = tmem_ld1(tmem + tm_row + L::kTmGram + KP);
         tmem_wait_ld();
         V.b[row] = (row < k) ? __uint_as_float(bv) : 0.0f;
       }
     }
     __syncthreads();
-    if (warp < 2) {  // row means r, grand mean c, infinity norm
+    if (warp < NG) {  // row means r, grand mean c, infinity norm
       const int i = tid;
-      const float r = (i < k) ? (V.part[0][i] + V.part[1][i]) * ik : 0.0f;
-      const float ab = (i < k) ? V.part[2][i] + V.part[3][i] : 0.0f;
+      float r = 0.0f, ab = 0.0f;
+      if (i < k) {
+#pragma unroll
+        for (int gg = 0; gg < NG; ++gg) {
+          r += V.part[gg][i];
+          ab += V.part[NG + gg][i];
+        }
+        r *= ik;
+      }
       V.r[i] = r;
       float sr = r, mx = ab;
 #pragma unroll
@@ -510,17 +563,22 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       }
       if (lane == 0) {
         V.red[warp] = sr;
-        V.red[2 + warp] = mx;
+        V.red[NG + warp] = mx;
       }
     }
     __syncthreads();
-    const float cbar = (V.red[0] + V.red[1]) * ik;
-    const float ninf = fmaxf(V.red[2], V.red[3]);
+    float cbar = 0.0f, ninf = 0.0f;
+#pragma unroll
+    for (int gg = 0; gg < NG; ++gg) {
+      cbar += V.red[gg];
+      ninf = fmaxf(ninf, V.red[NG + gg]);
+    }
+    cbar *= ik;
     // Row `row` of P A P, columns c0 .. c0+7, from the Gram in TMEM (zero
     // outside the member block).
     auto pap8 = [&](int c0, float (&x)[8]) {
       uint32_t v[8];
-      tmem_ld8(tmem + tm_row + kTmGram + c0, v);
+      tmem_ld8(tmem + tm_row + L::kTmGram + c0, v);
       tmem_wait_ld();
       const float ri = V.r[row];
 #pragma unroll
@@ -541,10 +599,13 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) fs += __shfl_xor_sync(0xffffffffu, fs, off);
-      if (lane == 0) V.red[4 + q + 2 * hh] = fs;
+      if (lane == 0) V.red[2 * NG + q * NG + g] = fs;
     }
     __syncthreads();
-    const float fro = sqrtf(V.red[4] + V.red[5] + V.red[6] + V.red[7]);
+    float fro2 = 0.0f;
+#pragma unroll
+    for (int e = 0; e < NG * NG; ++e) fro2 += V.red[2 * NG + e];
+    const float fro = sqrtf(fro2);
     const float s = fmaxf(fminf(ninf, fro), 1e-30f);
     const float is = 1.0f / s;
     float lsp = fminf(delta * is, 1.0f);  // lower end of the spectrum of Z Y (upper end 1)
@@ -563,25 +624,25 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     }
     float nsa, nsb;
     ns_coeffs(lsp, nsa, nsb);
-    // M = PAP / s + 1 1^T / k (identity on unused member slots); STACK <- [I; M]
-    // (row-major), TB <- T0 = a I - b M stored transposed.
+    // M = PAP / s + 1 1^T / k (identity on unused member slots); Z <- I,
+    // Y <- M (row-major), T <- T0 = a I - b M stored transposed.
     if (rowwarp) {
 #pragma unroll 1
       for (int c0 = cb; c0 < cb + 32; c0 += 8) {
         float x[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[j] = (row == c0 + j) ? 1.0f : 0.0f;
-        put_row8(STH, STL, row, c0, 128, x);
+        put_row8(ZH, ZL, row, c0, ZR, x);
         pap8(c0, x);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int c = c0 + j;
           x[j] = (row < k && c < k) ? x[j] * is + ik : ((row == c) ? 1.0f : 0.0f);
         }
-        put_row8(STH, STL, KP + row, c0, 128, x);
+        put_row8(YH, YL, row, c0, ZR, x);
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[j] = ((row == c0 + j) ? nsa : 0.0f) - nsb * x[j];
-        put_col8(TBH, TBL, row, c0, 64, x);
+        put_col8(TH, TL, row, c0, TR, x);
       }
     }
 
@@ -595,8 +656,12 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       operands_ready();
       if (warp == 0) {
         tc_fence_after();
-        issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2,
-               idesc64, false);
+        if constexpr (L::kStack) {
+          issue3(tmem, sZH, sZL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescK, false);
+        } else {
+          issue3(tmem, sZH, sZL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescK, false);
+          issue3(tmem + L::kTmB, sYH, sYL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescK, false);
+        }
         mma_commit_elect(&mma_bar);
       }
       ++its;
@@ -604,21 +669,39 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       conv = stop;
       if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
       mma_ph ^= 1u;
-      if (!last) {  // all eight warps: rows 0-63 Z, 64-127 Y
+      if (!last) {
+        if constexpr (L::kStack) {  // all warps: rows 0-63 Z, 64-127 Y
 #pragma unroll 1
-        for (int c0 = cb; c0 < cb + 32; c0 += 8) {
-          uint32_t v[8];
-          tmem_ld8(tmem + tm_row + c0, v);
-          tmem_wait_ld();
-          float x[8];
+          for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+            uint32_t v[8];
+            tmem_ld8(tmem + tm_row + c0, v);
+            tmem_wait_ld();
+            float x[8];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) x[j] = __uint_as_float(v[j]);
-          put_row8(STH, STL, 32 * q + lane, c0, 128, x);
+            for (int j = 0; j < 8; ++j) x[j] = __uint_as_float(v[j]);
+            put_row8(ZH, ZL, 32 * q + lane, c0, ZR, x);
+          }
+        } else if (rowwarp) {  // Z from the first product, Y from the second
+#pragma unroll 1
+          for (int c0 = cb; c0 < cb + 32; c0 += 8) {
+            uint32_t v[8];
+            float x[8];
+            tmem_ld8(tmem + tm_row + c0, v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) x[j] = __uint_as_float(v[j]);
+            put_row8(ZH, ZL, row, c0, ZR, x);
+            tmem_ld8(tmem + tm_row + L::kTmB + c0, v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int j = 0; j < 8; ++j) x[j] = __uint_as_float(v[j]);
+            put_row8(YH, YL, row, c0, ZR, x);
+          }
         }
       } else if (rowwarp) {
         // Final Z -> (Z - 1 1^T / k) / sqrt(s) on the member block, 0 elsewhere,
-        // stored transposed (rows 0-63 hold Z^T); rows 64-127 <- P A P
-        // (from the Gram in TMEM) for the finish.
+        // stored transposed (Z's operand holds Z^T); Y's operand <- P A P (from
+        // the Gram in TMEM) for the finish.
         const float isq = rsqrtf(s);
 #pragma unroll 1
         for (int c0 = cb; c0 < cb + 32; c0 += 8) {
@@ -631,18 +714,17 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
             const int c = c0 + j;
             x[j] = (row < k && c < k) ? (__uint_as_float(v[j]) - ik) * isq : 0.0f;
           }
-          put_col8(STH, STL, row, c0, 128, x);
+          put_col8(ZH, ZL, row, c0, ZR, x);
           pap8(c0, x);
-          put_row8(STH, STL, KP + row, c0, 128, x);
+          put_row8(YH, YL, row, c0, ZR, x);
         }
       }
       if (last) break;
-      // P = Z Y (Y as stored, rows 64-127), T = a I - b P (scaled step) -> TB transposed.
+      // P = Z Y (Y as stored), T = a I - b P (scaled step) -> T transposed.
       operands_ready();
       if (warp == 0) {
         tc_fence_after();
-        issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_STACK_HI + KP * 128,
-               sR + OFF_STACK_LO + KP * 128, kSlabS, 2, idesc64, false);
+        issue3(tmem, sZH, sZL, L::kSlabZ, sYH, sYL, L::kSlabZ, NG, idescK, false);
         mma_commit_elect(&mma_bar);
       }
       if (tid == 0) s_flag[0] = 0u;
@@ -664,7 +746,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
             emax = nan_max(emax, fabsf(d));
             t[j] = ((row == c) ? nsa - nsb : 0.0f) - nsb * d;  // a I - b P, P = I + d
           }
-          put_col8(TBH, TBL, row, c0, 64, t);
+          put_col8(TH, TL, row, c0, TR, t);
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, off));
@@ -688,13 +770,12 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     // ---------------- 4. finish ----------------
     // The iterate is Z = p(M) up to rounding errors that the coupled
     // iteration leaves as right factors, so the finish takes C = Z^T A Z:
-    // Q = (P A P) Z (A operand STACK rows 64.. = P A P, B operand Z^T rows),
-    // then C = Z^T Q; A^-1 = Z C^-1 Z^T, A^-1/2 ~ Z C^-1/2.
+    // Q = (P A P) Z (A operand: Y's rows = P A P; B operand: Z^T rows), then
+    // C = Z^T Q; A^-1 = Z C^-1 Z^T, A^-1/2 ~ Z C^-1/2.
     operands_ready();
     if (warp == 0) {
       tc_fence_after();
-      issue3(tmem, sR + OFF_STACK_HI + KP * 128, sR + OFF_STACK_LO + KP * 128, kSlabS, sR + OFF_STACK_HI,
-             sR + OFF_STACK_LO, kSlabS, 2, idesc64, false);
+      issue3(tmem, sYH, sYL, L::kSlabZ, sZH, sZL, L::kSlabZ, NG, idescK, false);
       mma_commit_elect(&mma_bar);
     }
     if (tid < KP) {  // u = Z^T b (row tid of Z^T)
@@ -702,7 +783,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
 #pragma unroll 1
       for (int c0 = 0; c0 < KP; c0 += 8) {
         float z[8];
-        get_row8(STH, STL, tid, c0, 128, z);
+        get_row8(ZH, ZL, tid, c0, ZR, z);
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc += z[j] * V.b[c0 + j];
       }
@@ -710,7 +791,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     }
     if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
     mma_ph ^= 1u;
-    if (rowwarp) {  // Q -> TB transposed
+    if (rowwarp) {  // Q -> T transposed
 #pragma unroll 1
       for (int c0 = cb; c0 < cb + 32; c0 += 8) {
         uint32_t v[8];
@@ -719,23 +800,22 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
         float x[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[j] = __uint_as_float(v[j]);
-        put_col8(TBH, TBL, row, c0, 64, x);
+        put_col8(TH, TL, row, c0, TR, x);
       }
     }
     // C = Z^T Q
     operands_ready();
     if (warp == 0) {
       tc_fence_after();
-      issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2, idesc64,
-             false);
+      issue3(tmem, sZH, sZL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescK, false);
       mma_commit_elect(&mma_bar);
       if (lane == 0) s_flag[1] = 0u;
     }
     if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
     mma_ph ^= 1u;
-    // F = C - P (residual, partial F u) -> TB transposed (B operand of Z F);
-    // Z rows, read from the columns of Z^T, -> STACK rows 64-127 row-major
-    // (A operand of Z F; P A P there is not read any more).
+    // F = C - P (residual, partial F u) -> T transposed (B operand of Z F);
+    // Z rows, read from the columns of Z^T, -> Y's operand row-major (A
+    // operand of Z F; P A P there is not read any more).
     if (rowwarp) {
       float fu = 0.0f, fm = 0.0f;
 #pragma unroll 1
@@ -753,11 +833,11 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
           fm = nan_max(fm, fabsf(x));
           fu += x * V.u[c];
         }
-        put_col8(TBH, TBL, row, c0, 64, f);
-        get_col8(STH, STL, row, c0, 128, f);
-        put_row8(STH, STL, KP + row, c0, 128, f);
+        put_col8(TH, TL, row, c0, TR, f);
+        get_col8(ZH, ZL, row, c0, ZR, f);
+        put_row8(YH, YL, row, c0, ZR, f);
       }
-      V.part[hh][row] = fu;
+      V.part[g][row] = fu;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) fm = fmaxf(fm, __shfl_xor_sync(0xffffffffu, fm, off));
       // NaN or Inf residuals map to the maximum (positive floats order as integers)
@@ -767,19 +847,23 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     operands_ready();
     if (warp == 0) {
       tc_fence_after();
-      issue3(tmem, sR + OFF_STACK_HI + KP * 128, sR + OFF_STACK_LO + KP * 128, kSlabS, sR + OFF_TB_HI,
-             sR + OFF_TB_LO, kSlabT, 2, idesc64, false);
+      issue3(tmem, sYH, sYL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescK, false);
       mma_commit_elect(&mma_bar);
     }
     const float resid = __uint_as_float(s_flag[1]);
-    if (tid < KP) V.v[tid] = (tid < k) ? V.u[tid] - (V.part[0][tid] + V.part[1][tid]) : 0.0f;
+    if (tid < KP) {
+      float fu = 0.0f;
+#pragma unroll
+      for (int gg = 0; gg < NG; ++gg) fu += V.part[gg][tid];
+      V.v[tid] = (tid < k) ? V.u[tid] - fu : 0.0f;
+    }
     __syncthreads();
-    if (tid < KP) {  // wa = c Z v (row tid of Z, STACK row 64 + tid)
+    if (tid < KP) {  // wa = c Z v (row tid of Z, in Y's operand)
       float acc = 0.0f;
 #pragma unroll 1
       for (int c0 = 0; c0 < KP; c0 += 8) {
         float z[8];
-        get_row8(STH, STL, KP + tid, c0, 128, z);
+        get_row8(YH, YL, tid, c0, ZR, z);
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc += z[j] * V.v[c0 + j];
       }
@@ -792,17 +876,17 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       hand_back();
       continue;
     }
-    if (rowwarp) {  // W rows -> U^T = W^T into STACK rows 0-63 (A operand of the update)
+    if (rowwarp) {  // W rows -> U^T = W^T into Z's operand (A operand of the update)
 #pragma unroll 1
       for (int c0 = cb; c0 < cb + 32; c0 += 8) {
         uint32_t v[8];
         tmem_ld8(tmem + tm_row + c0, v);
         tmem_wait_ld();
         float w[8];
-        get_row8(STH, STL, KP + row, c0, 128, w);
+        get_row8(YH, YL, row, c0, ZR, w);
 #pragma unroll
         for (int j = 0; j < 8; ++j) w[j] = cw * (w[j] - 0.5f * __uint_as_float(v[j]));
-        put_col8(STH, STL, row, c0, 128, w);
+        put_col8(ZH, ZL, row, c0, ZR, w);
       }
     }
 
@@ -810,25 +894,24 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
     const float c1 = cw * rsqrtf(delta);  // W's eigenvalue on the mean direction
     for (int v0 = 0; v0 < prm.n_var; v0 += kVarTile) {
       const int nv = (prm.n_var - v0 < kVarTile) ? prm.n_var - v0 : kVarTile;
-      // X' rows of the variables -> TB rows 0..15 (B operand, K = members);
-      // one warp per two variables: X' wa, the mean of X', sum of X'^2.
-      for (int vv = warp; vv < kVarTile; vv += kThreads / 32) {
+      // X' rows of the variables -> T rows 0..15 (B operand, K = members);
+      // one warp per variable: X' wa, the mean of X', sum of X'^2.
+      for (int vv = warp; vv < kVarTile; vv += L::kWarps) {
         const float* xr = (vv < nv) ? Xp + (base + (int64_t)(v0 + vv) * prm.var_stride) * k : nullptr;
-        float x0 = 0.0f, x1 = 0.0f;
-        if (xr) {
-          if (lane < k) x0 = xr[lane];
-          if (lane + 32 < k) x1 = xr[lane + 32];
+        float dw = 0.0f, sx = 0.0f, sq = 0.0f;
+#pragma unroll
+        for (int gg = 0; gg < NG; ++gg) {
+          const int m = lane + 32 * gg;
+          const float x0 = (xr && m < k) ? xr[m] : 0.0f;
+          const uint32_t o0 = sw_off(vv, m, TR);
+          float h, l;
+          split(x0, h, l);
+          *reinterpret_cast<float*>(TH + o0) = h;
+          *reinterpret_cast<float*>(TL + o0) = l;
+          dw += x0 * V.wa[m];
+          sx += x0;
+          sq += x0 * x0;
         }
-        const uint32_t o0 = sw_off(vv, lane, 64), o1 = sw_off(vv, lane + 32, 64);
-        float h, l;
-        split(x0, h, l);
-        *reinterpret_cast<float*>(TBH + o0) = h;
-        *reinterpret_cast<float*>(TBL + o0) = l;
-        split(x1, h, l);
-        *reinterpret_cast<float*>(TBH + o1) = h;
-        *reinterpret_cast<float*>(TBL + o1) = l;
-        float dw = x0 * V.wa[lane] + x1 * V.wa[lane + 32];
-        float sx = x0 + x1, sq = x0 * x0 + x1 * x1;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
           dw += __shfl_xor_sync(0xffffffffu, dw, off);
@@ -845,14 +928,13 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       operands_ready();
       if (warp == 0) {
         tc_fence_after();
-        issue3(tmem, sR + OFF_STACK_HI, sR + OFF_STACK_LO, kSlabS, sR + OFF_TB_HI, sR + OFF_TB_LO, kSlabT, 2,
-               idescU, false);
+        issue3(tmem, sZH, sZL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescU, false);
         mma_commit_elect(&mma_bar);
       }
       if (!wait_all(&mma_bar, mma_ph)) { alive = false; break; }
       mma_ph ^= 1u;
       float dv[kVarTile];
-      if (rowwarp && hh == 0) {
+      if (rowwarp && g == 0) {
         uint32_t v[8], v2[8];
         tmem_ld8(tmem + tm_row, v);
         tmem_ld8(tmem + tm_row + 8, v2);
@@ -862,7 +944,7 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
           dv[vv] = __uint_as_float(v[vv]) + V.one[vv];
           dv[8 + vv] = __uint_as_float(v2[vv]) + V.one[8 + vv];
         }
-        if (rtps) {  // analysis spread per variable (members = threads 0..63)
+        if (rtps) {  // analysis spread per variable (members = rows 0 .. KP-1)
 #pragma unroll
           for (int vv = 0; vv < kVarTile; ++vv) {
             float s2 = (row < k) ? dv[vv] * dv[vv] : 0.0f;
@@ -875,20 +957,23 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
       if (rtps) {
         __syncthreads();
         if (tid < kVarTile) {
+          float s2 = 0.0f;
+#pragma unroll
+          for (int qq = 0; qq < NG; ++qq) s2 += V.ssa[qq][tid];
           const float sb = sqrtf(V.xsq[tid] / (float)(k - 1));
-          const float sa = sqrtf((V.ssa[0][tid] + V.ssa[1][tid]) / (float)(k - 1));
+          const float sa = sqrtf(s2 / (float)(k - 1));
           V.fac[tid] = (sa > 0.0f) ? (float)prm.rho * (sb - sa) / sa : 0.0f;  // factor - 1
         }
         __syncthreads();
       }
-      if (rowwarp && hh == 0 && row < k) {
+      if (rowwarp && g == 0 && row < k) {
         for (int vv = 0; vv < nv; ++vv) {
           const float a2 = rtps ? dv[vv] * (1.0f + V.fac[vv]) : dv[vv];
           mg::letkf_store(prm, (base + (int64_t)(v0 + vv) * prm.var_stride) * k + row,
                           (V.xm[vv] + (double)V.inc[vv]) + (double)a2);
         }
       }
-      __syncthreads();  // TB and the vectors are rewritten by the next tile
+      __syncthreads();  // T and the vectors are rewritten by the next tile
     }
     if (!alive) break;
     if (tid == 0) {
@@ -911,30 +996,25 @@ __global__ void __launch_bounds__(kThreads, 2) letkf_tc_kernel(mg::LetkfParams p
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+  if (warp == 0) tmem_dealloc(tmem, L::kTmemCols);
 }
 
-}  // namespace
-
-namespace mg {
-
-bool letkf_tc_supported(const LetkfParams& prm) {
-  const bool chol = prm.flags & MG_SQRT_CHOLESKY, upd = prm.flags & MG_UPDATE_COMPAT;
-  return prm.k >= 2 && prm.k <= KP && !chol && !upd && !prm.warm_start && prm.redo_out && prm.n_redo;
-}
-
-int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream, int* ctas) {
-  cudaError_t e = cudaFuncSetAttribute(letkf_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kSmemBytes);
+template <int KP>
+int launch_tc(const mg::LetkfParams& prm, int num_sms, void* stream, int* ctas) {
+  using L = Lay<KP>;
+  constexpr size_t kSmem = smem_bytes<KP>();
+  auto kern = letkf_tc_kernel<KP>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
   if (e != cudaSuccess) return (int)e;
-  // The whole unified L1/shared array as shared memory, so two CTAs fit.
-  e = cudaFuncSetAttribute(letkf_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+  // The whole unified L1/shared array as shared memory (two KP = 64 CTAs or
+  // one KP = 96 CTA per SM).
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                            (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return (int)e;
-  // CTAs per SM from the SM's shared memory and register file (the design
-  // point is two, which also share the SM's 512 TMEM columns evenly).
+  // CTAs per SM from the SM's shared memory and register file, at most the
+  // design point (which also divides the SM's 512 TMEM columns evenly).
   cudaFuncAttributes fa{};
-  e = cudaFuncGetAttributes(&fa, letkf_tc_kernel);
+  e = cudaFuncGetAttributes(&fa, kern);
   if (e != cudaSuccess) return (int)e;
   int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
@@ -944,19 +1024,32 @@ int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream, int* ctas
     return (int)e;
   if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess)
     return (int)e;
-  const size_t per_cta = kSmemBytes + fa.sharedSizeBytes + (size_t)reserved;
+  const size_t per_cta = kSmem + fa.sharedSizeBytes + (size_t)reserved;
   int per_sm = (int)((size_t)smem_sm / per_cta);
-  const int by_regs = fa.numRegs > 0 ? regs_sm / (fa.numRegs * kThreads) : 2;
+  const int by_regs = fa.numRegs > 0 ? regs_sm / (fa.numRegs * L::kThreads) : L::kMinBlocks;
   if (by_regs < per_sm) per_sm = by_regs;
-  if (per_sm > 2) per_sm = 2;
+  if (per_sm > L::kMinBlocks) per_sm = L::kMinBlocks;
   if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
   int64_t grid = (int64_t)per_sm * num_sms;
   if (grid > prm.npoints) grid = prm.npoints;
   if (grid < 1) grid = 1;
   if (ctas) *ctas = (int)grid;
-  letkf_tc_kernel<<<(unsigned)grid, kThreads, kSmemBytes, static_cast<cudaStream_t>(stream)>>>(prm);
+  kern<<<(unsigned)grid, L::kThreads, kSmem, static_cast<cudaStream_t>(stream)>>>(prm);
   MG_COUNT_LAUNCH();
   return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+namespace mg {
+
+bool letkf_tc_supported(const LetkfParams& prm) {
+  const bool chol = prm.flags & MG_SQRT_CHOLESKY, upd = prm.flags & MG_UPDATE_COMPAT;
+  return prm.k >= 2 && prm.k <= 96 && !chol && !upd && !prm.warm_start && prm.redo_out && prm.n_redo;
+}
+
+int letkf_tc_launch(const LetkfParams& prm, int num_sms, void* stream, int* ctas) {
+  return prm.k <= 64 ? launch_tc<64>(prm, num_sms, stream, ctas) : launch_tc<96>(prm, num_sms, stream, ctas);
 }
 
 }  // namespace mg

@@ -1,5 +1,5 @@
 """GPU parity of the tensor-core local analyses (mixed precision, Hunt
-transform, k <= 64): the Gram, the Newton-Schulz inverse square root and the
+transform, k <= 96; two kernel layouts, k <= 64 and 64 < k <= 96): the Gram, the Newton-Schulz inverse square root and the
 update X' W on tcgen05 kind::tf32 with 3-pass products.  Each case checks that
 the tensor-core kernel ran (stats.tensor_path), compares it with the oracle
 (FP64, Jacobi eigen-solve) at 1e-5 relative, and with the SIMT Jacobi path."""
@@ -51,7 +51,7 @@ def _gather(X, c, base):
     return np.stack([X[:, base + v * c.var_stride].T for v in range(c.nvar)], axis=1)
 
 
-@pytest.mark.parametrize("k", [4, 9, 16, 33, 47, 64])
+@pytest.mark.parametrize("k", [4, 9, 16, 33, 47, 64, 65, 80, 96])
 def test_tensor_path_matches_oracle_and_simt(dev, k):
     c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=5, nvar=2, k=k, p=20_000, T=20, case=41)
     got, HX, off, idx, dist, st = _run(dev, c)
@@ -88,10 +88,11 @@ def test_tensor_path_many_variables_per_point(dev):
     assert rel_err(_gather(got, c, base), want) <= MIXED_TOL
 
 
-def test_tensor_path_uneven_clustered_lists(dev):
+@pytest.mark.parametrize("k", [64, 80])
+def test_tensor_path_uneven_clustered_lists(dev, k):
     """Clustered obs: lists from a handful to thousands of candidates per
-    column, so the Gram runs from one to many chunks."""
-    c = syn.latlon_letkf_case(nlon=120, nlat=60, nlev=4, nvar=2, k=64, p=60_000, T=30, hsupport_km=600.0,
+    column, so the Gram runs from one to many chunks (both kernel layouts)."""
+    c = syn.latlon_letkf_case(nlon=120, nlat=60, nlev=4, nvar=2, k=k, p=60_000, T=30, hsupport_km=600.0,
                               case=44, clustered=0.7, n_patches=6)
     got, HX, off, idx, dist, st = _run(dev, c)
     counts = np.diff(off)
@@ -106,9 +107,9 @@ def test_tensor_path_uneven_clustered_lists(dev):
 def test_fp32_member_storage_highres_shape(dev, k):
     """The high-resolution configuration's analysis at reduced size with the
     members stored as FP32: 60 % of the obs in Gaussian patches, 300 km
-    support, RTPS 0.9; k = 64 runs the tensor-core kernel, k = 80 the SIMT
-    kernel.  H(X) of the FP32 members is bit-identical to the oracle's on the
-    widened values; the analysis of sampled columns (the longest lists among
+    support, RTPS 0.9; both run the tensor-core kernel (k = 80 in its
+    96-slot layout).  H(X) of the FP32 members is bit-identical to the
+    oracle's on the widened values; the analysis of sampled columns (the longest lists among
     them) matches the oracle run on its own lists and H(X)."""
     c = syn.latlon_letkf_case(nlon=144, nlat=72, nlev=6, nvar=3, k=k, p=60_000, T=40, hsupport_km=300.0,
                               rho=0.9, case=45, clustered=0.6)
@@ -125,7 +126,7 @@ def test_fp32_member_storage_highres_shape(dev, k):
                             obs_lev=olev, hsupport=c.hsupport_km, vsupport=c.vsupport, rho=c.rho,
                             flags=_lib.MG_RTPS, precision=_lib.MG_PREC_MIXED, want_mean=False)
     assert X32.dtype == torch.float32
-    assert st.tensor_path == (1 if k <= 64 else 0)
+    assert st.tensor_path == 1 and st.n_fallback <= st.n_points // 100
     counts = np.diff(off.cpu().numpy())
     assert counts.max() > 8 * max(1.0, np.median(counts))
     cols = np.unique(np.concatenate([np.argsort(counts)[-20:],
@@ -147,8 +148,8 @@ def test_fp32_member_storage_highres_shape(dev, k):
     assert rel_err(_gather(got, c, base), want) <= MIXED_TOL
 
 
-@pytest.mark.parametrize("sigma_o", [0.2, 0.01])
-def test_ill_conditioned_points_go_to_the_simt_kernel(dev, sigma_o):
+@pytest.mark.parametrize("sigma_o,k", [(0.2, 64), (0.01, 64), (0.2, 80)])
+def test_ill_conditioned_points_go_to_the_simt_kernel(dev, sigma_o, k):
     """Accurate obs over a wide support make the deflated local matrix far
     worse conditioned than 3-pass TF32 products resolve.  Such points (a lower
     spectrum bound below the threshold, an iteration that leaves its basin,
@@ -156,7 +157,7 @@ def test_ill_conditioned_points_go_to_the_simt_kernel(dev, sigma_o):
     non-finite value reaches the output, and every point matches the
     SIMT-only run (the re-run points bit for bit, since the SIMT kernel
     treats each point alone) and, on sampled columns, the oracle."""
-    c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=4, nvar=2, k=64, p=40_000, T=20, sigma_o=sigma_o,
+    c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=4, nvar=2, k=k, p=40_000, T=20, sigma_o=sigma_o,
                               hsupport_km=900.0, case=46)
     got, HX, off, idx, dist, st = _run(dev, c)
     print(f"sigma_o {sigma_o}: {st.n_fallback} of {st.n_points} points re-run, max residual {st.max_residual:.2e}")
