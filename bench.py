@@ -75,7 +75,8 @@ def parse():
                          "H(x) of 200k column obs x 64 members (720x360 columns, 30 levels), plain and "
                          "surrogate (untrained weights), twice each; column-small = the same on 360x180 columns with "
                          "50k obs (2 GB state); highres-small = two cycles of the high-resolution LETKF (k=80, FP32 "
-                         "members, RTPS) on a 360x180x10x4 grid with 500k obs, 60%% clustered")
+                         "members, RTPS) on a 180x90x10x4 grid with 1.67M obs, 60%% clustered (the full "
+                         "configuration's obs per level)")
     return ap.parse_args()
 
 
@@ -402,9 +403,10 @@ def profile_case(precision_name: str) -> None:
         return
 
     if precision_name == "highres-small":
-        # the high-resolution configuration's analysis on a 360 x 180 x 10 x 4
-        # grid (k = 80 stored as FP32: 0.83 GB), 500k obs (60 % in patches)
-        c = syn.highres_letkf_case(dev, nlon=360, nlat=180, nlev=10, p=500_000)
+        # the high-resolution configuration's analysis on a 180 x 90 x 10 x 4
+        # grid (k = 80 stored as FP32: 207 MB) with its obs density per level:
+        # 5M obs over 30 levels -> 1.67M over 10 (60 % in patches)
+        c = syn.highres_letkf_case(dev, nlon=180, nlat=90, nlev=10, p=1_670_000)
         la, lo = c.col_lat_lon()
         clat, clon = torch.tensor(la, device=dev), torch.tensor(lo, device=dev)
         col_base = torch.tensor(c.col_base(), device=dev)

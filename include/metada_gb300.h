@@ -54,7 +54,7 @@ extern "C" {
                             eigen-solve warm-started from the previous level's eigenvectors
                             (default: every eigen-solve starts from the identity) */
 #define MG_SOLVE_SIMT 64 /* batched LETKF, mixed precision: the SIMT Jacobi solve instead of
-                            the tensor-core Newton-Schulz route (which serves k <= 64 with the
+                            the tensor-core Newton-Schulz route (which serves k <= 96 with the
                             Hunt transform and update) */
 
 /* Arithmetic of the analysis. */
