@@ -21,6 +21,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -590,6 +591,79 @@ __global__ void obs_pack_kernel(const double* __restrict__ obs_lev, const double
     out[o] = make_float4(obs_lev ? (float)obs_lev[o] : 0.0f, (float)rinv[o], (float)dinn[o], 0.0f);
 }
 
+// Level bucket of each observation for the tensor-core path's sorted lists:
+// floor(level) clamped to [0, nlev - 1] (non-finite levels to 0; the
+// analyses that use the buckets drop them with a zero weight anyway).
+__global__ void obs_bucket_kernel(const double* __restrict__ obs_lev, int64_t p, int nlev,
+                                  uint8_t* __restrict__ out) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < p; o += stride) {
+    const double l = obs_lev[o];
+    int b = 0;
+    if (l == l) {
+      const double f = floor(l);
+      b = (f <= 0.0) ? 0 : ((f >= (double)(nlev - 1)) ? nlev - 1 : (int)f);
+    }
+    out[o] = (uint8_t)b;
+  }
+}
+
+// Stable counting sort of each column's candidate list by level bucket, one
+// warp per column: counts per bucket (lanes of one bucket found with
+// match_any, the lowest of them adds the group's size), the bucket starts
+// (relative to the column's start) to boff, then the entries scattered in
+// list order within each bucket.  nlev <= kBucketMaxLev.
+constexpr int kBucketMaxLev = 64;
+__global__ void __launch_bounds__(256) level_bucket_kernel(const int64_t* __restrict__ off,
+                                                           const int32_t* __restrict__ idx,
+                                                           const double* __restrict__ dist,
+                                                           const uint8_t* __restrict__ obkt, int nlev, int64_t ncol,
+                                                           int32_t* __restrict__ idx2, double* __restrict__ dist2,
+                                                           int32_t* __restrict__ boff) {
+  __shared__ int cur[8][kBucketMaxLev];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int* c = cur[w];
+  const int64_t nwarps = (int64_t)gridDim.x * 8;
+  for (int64_t col = (int64_t)blockIdx.x * 8 + w; col < ncol; col += nwarps) {
+    const int64_t e0 = off[col], e1 = off[col + 1];
+    for (int b = lane; b < nlev; b += 32) c[b] = 0;
+    __syncwarp();
+    for (int64_t e = e0; e < e1; e += 32) {
+      const bool v = e + lane < e1;
+      const int b = v ? (int)obkt[idx[e + lane]] : 255;  // 255: no bucket
+      const unsigned m = __match_any_sync(0xffffffffu, b);
+      if (v && lane == __ffs(m) - 1) c[b] += __popc(m);
+      __syncwarp();
+    }
+    if (lane == 0) {
+      int run = 0;
+      int32_t* bo = boff + col * (int64_t)(nlev + 1);
+      for (int b = 0; b < nlev; ++b) {
+        bo[b] = run;
+        const int t = c[b];
+        c[b] = run;
+        run += t;
+      }
+      bo[nlev] = run;
+    }
+    __syncwarp();
+    for (int64_t e = e0; e < e1; e += 32) {
+      const bool v = e + lane < e1;
+      const int o = v ? idx[e + lane] : 0;
+      const int b = v ? (int)obkt[o] : 255;
+      const unsigned m = __match_any_sync(0xffffffffu, b);
+      const int pos = v ? c[b] + __popc(m & ((1u << lane) - 1u)) : 0;
+      __syncwarp();
+      if (v) {
+        idx2[e0 + pos] = o;
+        if (dist) dist2[e0 + pos] = dist[e + lane];
+        if (lane == __ffs(m) - 1) c[b] += __popc(m);
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // Column list lengths (keys) for the longest-first order.
 __global__ void list_len_kernel(const int64_t* __restrict__ off, int64_t ncol,
                                 uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
@@ -788,6 +862,21 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   const int64_t n = d->n, p = d->p;
   const int64_t npoints = d->ncol * d->nlev;
   const size_t te = fp64 ? sizeof(double) : sizeof(float);
+  // Level-bucketed candidate lists for the tensor-core path (it filters by
+  // obs level with Gaspari-Cohn weights, so candidates outside the vertical
+  // support never count): an analysis then walks about (2 vsupport + 1) /
+  // nlev of its column's list instead of all of it.
+  const bool bucket = !fp64 && !(d->flags & (MG_SOLVE_SIMT | MG_R_IDENTITY | MG_SQRT_CHOLESKY | MG_UPDATE_COMPAT |
+                                             MG_WARM_START)) &&
+                      k <= 96 && d->obs_lev && p > 0 && d->nlev >= 2 && d->nlev <= kBucketMaxLev &&
+                      std::isfinite(d->vsupport) && d->vsupport >= 0.0;
+  int64_t n_entries = 0;
+  if (bucket) {
+    MG_TRY_CUDA(cudaMemcpyAsync(&n_entries, d->loc_off + d->ncol, sizeof(n_entries), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    MG_TRY_CUDA(cudaStreamSynchronize(ctx->stream));
+    MG_CHECK_ARG(n_entries >= 0, "mg_letkf_batched: bad candidate offsets");
+  }
   const size_t sort_bytes = [&] {
     size_t b = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, b, (const uint32_t*)nullptr, (uint32_t*)nullptr,
@@ -807,6 +896,10 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   cv.reserve<int32_t>((size_t)npoints);            // points handed back by the tensor-core path
   cv.reserve<float4>((size_t)p + 1);               // per-obs FP32 pack (tensor-core path)
   cv.reserve<char>(sort_bytes);
+  cv.reserve<uint8_t>(bucket ? (size_t)p + 1 : 1);                          // obs level buckets
+  cv.reserve<int32_t>(bucket ? (size_t)d->ncol * (d->nlev + 1) : 1);       // bucket starts
+  cv.reserve<int32_t>(bucket ? (size_t)n_entries + 1 : 1);                 // sorted obs indices
+  cv.reserve<double>(bucket && d->loc_dist ? (size_t)n_entries + 1 : 1);   // sorted distances
   void* ws = mg::workspace(ctx, cv.off);
   if (!ws) return MG_ERR_NOMEM;
   cv = mg::Carver{static_cast<char*>(ws), 0};
@@ -822,6 +915,10 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
   int32_t* redo = cv.take<int32_t>((size_t)npoints);
   float4* opack = cv.take<float4>((size_t)p + 1);
   void* sort_tmp = cv.take<char>(sort_bytes);
+  uint8_t* obkt = cv.take<uint8_t>(bucket ? (size_t)p + 1 : 1);
+  int32_t* lev_boff = cv.take<int32_t>(bucket ? (size_t)d->ncol * (d->nlev + 1) : 1);
+  int32_t* bidx = cv.take<int32_t>(bucket ? (size_t)n_entries + 1 : 1);
+  double* bdist = cv.take<double>(bucket && d->loc_dist ? (size_t)n_entries + 1 : 1);
   cudaStream_t s = ctx->stream;
 
   MG_TRY_CUDA(cudaEventRecord(ctx->ev[0], s));
@@ -900,6 +997,20 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
       MG_TRY_CUDA(cudaGetLastError());
     }
     prm.opack = opack;
+    if (bucket) {
+      const unsigned pb = (unsigned)std::min<int64_t>((p + 255) / 256, (int64_t)ctx->num_sms * 16);
+      obs_bucket_kernel<<<pb, 256, 0, s>>>(d->obs_lev, p, d->nlev, obkt);
+      MG_COUNT_LAUNCH();
+      MG_TRY_CUDA(cudaGetLastError());
+      const unsigned cbk = (unsigned)std::min<int64_t>((d->ncol + 7) / 8, (int64_t)ctx->num_sms * 8);
+      level_bucket_kernel<<<cbk, 256, 0, s>>>(d->loc_off, d->loc_idx, d->loc_dist, obkt, d->nlev, d->ncol, bidx,
+                                             d->loc_dist ? bdist : nullptr, lev_boff);
+      MG_COUNT_LAUNCH();
+      MG_TRY_CUDA(cudaGetLastError());
+      prm.lev_boff = lev_boff;
+      prm.bidx = bidx;
+      prm.bdist = d->loc_dist ? bdist : nullptr;
+    }
     const int e = mg::letkf_tc_launch(prm, ctx->num_sms, s, &tc_ctas);
     if (e != 0)
       return mg::fail(ctx, MG_ERR_CUDA, std::string("letkf_tc_kernel: ") + cudaGetErrorString((cudaError_t)e));
@@ -914,6 +1025,7 @@ int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* d) {
       fb.npoints = n_fallback;
       fb.warm_start = 0;
       fb.next = cnt + 6;  // reused as the work counter of the re-run
+      fb.lev_boff = nullptr;  // the SIMT kernel walks the column lists as given
       MG_TRY_CUDA(cudaMemsetAsync(cnt + 6, 0, sizeof(unsigned long long), s));
       rc = (k <= 64) ? launch_batched<float, 64>(ctx, fb) : launch_batched<float, 96>(ctx, fb);
     }

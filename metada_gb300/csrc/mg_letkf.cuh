@@ -46,6 +46,15 @@ struct LetkfParams {
   // SIMT path: when set, item i is the point redo_in[i] (col * nlev + lev)
   // instead of the longest-first order.
   const int32_t* redo_in;
+  // Tensor-core path: when set, each column's candidates sorted by obs level
+  // bucket (stable; bucket = floor(obs level) clamped to the grid's levels):
+  // lev_boff[col * (nlev + 1) + b] is bucket b's start within the column's
+  // range of loc_off, and bidx / bdist the sorted entries (same index space
+  // as loc_idx / loc_dist).  An analysis at level l walks only the buckets
+  // floor(l - vsupport) .. floor(l + vsupport).
+  const int32_t* lev_boff;
+  const int32_t* bidx;
+  const double* bdist;
 };
 
 // Analysis value of point-major element idx, in the output's precision.

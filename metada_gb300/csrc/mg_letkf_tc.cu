@@ -369,7 +369,19 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
     const int lev = (int)(item % prm.nlev);
     const int64_t col = prm.order[item / prm.nlev];
     const int64_t base = prm.col_base[col] + (int64_t)lev * prm.lev_stride;
-    const int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
+    int64_t e0 = prm.loc_off[col], e1 = prm.loc_off[col + 1];
+    const int32_t* lidx = prm.loc_idx;
+    const double* ldist = prm.loc_dist;
+    if (prm.lev_boff) {  // only the level buckets that can reach this level
+      const int32_t* bo = prm.lev_boff + col * (int64_t)(prm.nlev + 1);
+      const double fl = floor((double)lev - prm.vsupport), fh = floor((double)lev + prm.vsupport);
+      const int lo = (fl <= 0.0) ? 0 : (int)fl;
+      const int hi = (fh >= (double)(prm.nlev - 1)) ? prm.nlev - 1 : (int)fh;
+      e1 = e0 + bo[hi + 1];
+      e0 = e0 + bo[lo];
+      lidx = prm.bidx;
+      ldist = prm.bdist;
+    }
 
     // ---------------- 1. selection and Gram ----------------
     // Rounds: compact candidates into the ring (up to kSelRing - kThreads
@@ -408,7 +420,7 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
         float sw = 0.0f, sd = 0.0f;
         if (cpos + tid < e1) {
           const int64_t e = cpos + tid;
-          o = prm.loc_idx[e];
+          o = lidx[e];
           const float4 pk = prm.opack[o];  // (level, 1/sigma^2, innovation, 0) as FP32
           float w = 1.0f;
           keep = true;
@@ -419,7 +431,7 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
             if (keep && !r_identity) w *= mg::gaspari_cohn<float>(dl / vc);
           }
           if (keep && !r_identity) {
-            if (prm.loc_dist) w *= mg::gaspari_cohn<float>((float)prm.loc_dist[e] / hc);
+            if (ldist) w *= mg::gaspari_cohn<float>((float)ldist[e] / hc);
             w *= pk.y;
             if (!(w > 0.0f)) keep = false;
           }
