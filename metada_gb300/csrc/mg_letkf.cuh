@@ -67,14 +67,29 @@ __device__ __forceinline__ void letkf_add(const LetkfParams& prm, int64_t idx, d
   else prm.Xa[idx] += dv;
 }
 
+// Gaspari-Cohn (1999, eq. 4.10) fifth-order compactly supported function of
+// z = distance / (support / 2).  FP64 evaluates the published polynomials
+// in the oracle's operation order (the FP64 path's local lists are
+// bit-identical to the oracle's).  In FP32 the outer polynomial cancels
+// near z = 2, where the function vanishes to fourth order, and rounds to
+// zero or below for z within about 1 % of the support, dropping candidates
+// that FP64 keeps with tiny weights; FP32 uses the exact factored form
+// z f(z) = (2 - z)^4 (z^2 + 2z - 1/2) / 12 instead (2 - z is exact for
+// 1 <= z <= 2), which is positive for every z < 2.
 template <typename T>
 __device__ __forceinline__ T gaspari_cohn(T z) {
   z = fabs(z);
   if (z >= T(2)) return T(0);
   if (z <= T(1))
     return (((T(-0.25) * z + T(0.5)) * z + T(0.625)) * z - T(5.0 / 3.0)) * z * z + T(1);
-  return ((((z / T(12) - T(0.5)) * z + T(0.625)) * z + T(5.0 / 3.0)) * z - T(5)) * z + T(4) -
-         T(2) / (T(3) * z);
+  if constexpr (sizeof(T) == sizeof(float)) {
+    const T t = T(2) - z;
+    const T t2 = t * t;
+    return (t2 * t2) * ((z + T(2)) * z - T(0.5)) / (T(12) * z);
+  } else {
+    return ((((z / T(12) - T(0.5)) * z + T(0.625)) * z + T(5.0 / 3.0)) * z - T(5)) * z + T(4) -
+           T(2) / (T(3) * z);
+  }
 }
 
 // Tensor-core local analyses (mixed precision, Hunt transform, k <= 96):

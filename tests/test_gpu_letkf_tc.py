@@ -56,7 +56,7 @@ def test_tensor_path_matches_oracle_and_simt(dev, k):
     c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=5, nvar=2, k=k, p=20_000, T=20, case=41)
     got, HX, off, idx, dist, st = _run(dev, c)
     assert st.tensor_path == 1 and st.tensor_ctas >= torch.cuda.get_device_properties(dev).multi_processor_count
-    assert st.n_fallback == 0 and 0.0 < st.max_residual < 5e-3
+    assert st.n_fallback <= st.n_points // 1000 and 0.0 < st.max_residual < 5e-3
     assert st.total_sweeps > 0 and st.max_sweeps <= 14
     cols = np.arange(c.nlat * c.nlon)
     base, want = _oracle(c, HX, off, idx, dist, cols, 0)
@@ -169,3 +169,55 @@ def test_ill_conditioned_points_go_to_the_simt_kernel(dev, sigma_o, k):
     cols = np.random.default_rng(3).choice(c.nlat * c.nlon, 80, replace=False)
     base, want = _oracle(c, HX, off, idx, dist, cols, 0)
     assert rel_err(_gather(got, c, base), want) <= MIXED_TOL
+
+
+def test_tensor_path_level_bucket_edges(dev):
+    """The tensor-core kernel walks only the obs-level buckets (floor of the
+    level, clamped to the grid) that can reach each analysis level.  Obs
+    levels below level 0 and above the top level, levels at exact integers
+    and a non-integer vertical support (1.5) sit at the bucket bounds; the
+    localisation levels differ from the levels H interpolates at, so H(X)
+    stays inside the grid.  Against the oracle on every column and against
+    the SIMT kernel, which walks the unsorted lists."""
+    c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=6, nvar=2, k=48, p=20_000, T=20, case=47)
+    rng = np.random.default_rng(5)
+    lev = c.obs_lev.copy()
+    u = rng.random(lev.size)
+    lo, hi, ints = u < 0.1, (u >= 0.1) & (u < 0.2), (u >= 0.2) & (u < 0.35)
+    lev[lo] = -rng.uniform(0.0, 1.6, lo.sum())
+    lev[hi] = (c.nlev - 1) + rng.uniform(0.0, 1.6, hi.sum())
+    lev[ints] = rng.integers(0, c.nlev, ints.sum())
+    vsupport = 1.5
+    Xd = T(c.X, dev)
+    olat, olon = T(c.obs_lat, dev), T(c.obs_lon, dev)
+    HX = K.hx_latlon(Xd, c.nlon, c.nlat, c.nlev, olat, olon, T(c.obs_lev, dev), T(c.obs_var, dev))
+    clat, clon = c.col_lat_lon()
+    off, idx, dist = K.select_geo(T(clat, dev), T(clon, dev), olat, olon, c.hsupport_km)
+    yo = T(c.yo, dev)
+    rvar = torch.full_like(yo, c.sigma_o ** 2)
+
+    def run(flags):
+        X = Xd.clone()
+        _, st = K.letkf_batched(X, col_base=T(c.col_base(), dev), nlev=c.nlev, n_var=c.nvar,
+                                lev_stride=c.lev_stride, var_stride=c.var_stride, HX=HX, yo=yo, rvar=rvar,
+                                loc_off=off, loc_idx=idx, loc_dist=dist, obs_lev=T(lev, dev), hsupport=c.hsupport_km,
+                                vsupport=vsupport, rho=c.rho, flags=flags, precision=_lib.MG_PREC_MIXED,
+                                want_mean=False)
+        return X.cpu().numpy(), st
+
+    got, st = run(0)
+    assert st.tensor_path == 1 and st.n_fallback <= st.n_points // 100
+    cols = np.arange(c.nlat * c.nlon)
+    offh, idxh, disth = off.cpu().numpy(), idx.cpu().numpy(), dist.cpu().numpy()
+    pts, poff, pidx, pw = point_lists(cols, c.nlev, offh, idxh, disth, lev, c.hsupport_km, vsupport)
+    # the same candidates kept: a bucket bound that dropped one level's obs
+    # would lose thousands; a few differ at the support's edge, where the
+    # oracle's FP64 polynomial cancels to zero and the FP32 factored form
+    # stays positive
+    assert abs(st.total_local - poff[-1]) <= poff[-1] // 1000
+    base = c.col_base()[pts[:, 0]] + pts[:, 1] * c.lev_stride
+    want = ob.letkf_points(c.X, base, c.nvar, c.var_stride, HX.cpu().numpy(), c.yo, c.rvar, poff, pidx, pw, c.rho, 0)
+    assert rel_err(_gather(got, c, base), want) <= MIXED_TOL
+    simt, st2 = run(_lib.MG_SOLVE_SIMT)
+    assert st2.tensor_path == 0 and st2.total_local == st.total_local
+    assert rel_err(got, simt) <= MIXED_TOL
