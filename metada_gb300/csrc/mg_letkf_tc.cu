@@ -81,6 +81,7 @@ constexpr float kCondResid = 0.1f;
 // iterate stays below 1); the analysis is handed back at once.
 constexpr float kDiverged = 4.0f;
 constexpr int kVarTile = 16;    // variables per update MMA (N): two 8-column TMEM loads
+constexpr int kPre = 4;         // variables whose X' rows and means are prefetched during the finish
 
 // Shared and tensor memory of one CTA, by member slots KP (a multiple of 32).
 // Every operand is K-major with the 128-byte swizzle: a slab holds 32 TF32
@@ -139,6 +140,8 @@ struct Vecs {
   float xsq[kVarTile], inc[kVarTile], fac[kVarTile], one[kVarTile];
   float ssa[NG][kVarTile];
   double xm[kVarTile];
+  double xmpre[kPre];
+  float xpre[kPre][KP];
   int wcnt[Lay<KP>::kWarps];
 };
 
@@ -291,6 +294,15 @@ __device__ __forceinline__ void ns_coeffs(float& l, float& a, float& b) {
 // Maximum that a NaN poisons (fmaxf would drop it): NaN -> +inf.
 __device__ __forceinline__ float nan_max(float m, float x) { return (x != x) ? __int_as_float(0x7f800000) : fmaxf(m, x); }
 
+// Asynchronous global -> shared copies (no registers held while in flight).
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // FP64 decision for a candidate whose FP32 vertical distance is within 1e-4
 // of the support (kept out of line: a predicated FP64 instruction would
 // occupy the FP64 pipe for every candidate).
@@ -361,6 +373,7 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
   bool alive = true;
 
   for (;;) {
+    cp_async_wait_all();  // a handed-back analysis may leave its prefetch in flight
     if (tid == 0) s_item = (long long)atomicAdd(prm.next, 1ull);
     __syncthreads();
     const long long item = s_item;
@@ -530,7 +543,7 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
     const int row = 32 * q + lane;
     const int cb = 32 * g;
     if (rowwarp) {
-      float rs = 0.0f, as = 0.0f;
+      float rs = 0.0f, as = 0.0f, fa = 0.0f;
 #pragma unroll 1
       for (int c0 = cb; c0 < cb + 32; c0 += 8) {
         uint32_t v[8];
@@ -543,11 +556,15 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
           if (row < k && c < k) {
             rs += x;
             as += fabsf(x);
+            fa += x * x;
           }
         }
       }
       V.part[g][row] = rs;
       V.part[NG + g][row] = as;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) fa += __shfl_xor_sync(0xffffffffu, fa, off);
+      if (lane == 0) V.red[3 * NG + q * NG + g] = fa;  // ||A||_F^2, by warp
       if (g == 0) {
         const uint32_t bv = tmem_ld1(tmem + tm_row + L::kTmGram + KP);
         tmem_wait_ld();
@@ -567,15 +584,17 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
         r *= ik;
       }
       V.r[i] = r;
-      float sr = r, mx = ab;
+      float sr = r, mx = ab, s2 = r * r;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
         sr += __shfl_xor_sync(0xffffffffu, sr, off);
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+        s2 += __shfl_xor_sync(0xffffffffu, s2, off);
       }
       if (lane == 0) {
         V.red[warp] = sr;
         V.red[NG + warp] = mx;
+        V.red[2 * NG + warp] = s2;
       }
     }
     __syncthreads();
@@ -600,24 +619,18 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
         x[j] = (row < k && c < k) ? (av - ri - V.r[c] + cbar) : 0.0f;
       }
     };
-    if (rowwarp) {  // Frobenius norm of P A P
-      float fs = 0.0f;
-#pragma unroll 1
-      for (int c0 = cb; c0 < cb + 32; c0 += 8) {
-        float x[8];
-        pap8(c0, x);
+    // Frobenius norm of P A P from the same pass (A symmetric, A 1 = k r):
+    // ||P A P||_F^2 = ||A||_F^2 - 2 k sum r_i^2 + k^2 cbar^2.  With A 1 =
+    // delta 1 up to rounding the subtracted part is about delta^2, at most
+    // 1/k of ||A||_F^2 >= k delta^2, so the difference keeps FP32 accuracy
+    // (and s only has to bound lambda_max).
+    float fa2 = 0.0f, sr2 = 0.0f;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) fs += x[j] * x[j];
-      }
+    for (int e = 0; e < NG * NG; ++e) fa2 += V.red[3 * NG + e];
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) fs += __shfl_xor_sync(0xffffffffu, fs, off);
-      if (lane == 0) V.red[2 * NG + q * NG + g] = fs;
-    }
-    __syncthreads();
-    float fro2 = 0.0f;
-#pragma unroll
-    for (int e = 0; e < NG * NG; ++e) fro2 += V.red[2 * NG + e];
-    const float fro = sqrtf(fro2);
+    for (int gg = 0; gg < NG; ++gg) sr2 += V.red[2 * NG + gg];
+    const float kf = (float)k;
+    const float fro = sqrtf(fmaxf(fa2 - 2.0f * kf * sr2 + kf * kf * cbar * cbar, 0.0f));
     const float s = fmaxf(fminf(ninf, fro), 1e-30f);
     const float is = 1.0f / s;
     float lsp = fminf(delta * is, 1.0f);  // lower end of the spectrum of Z Y (upper end 1)
@@ -779,6 +792,16 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
       continue;
     }
 
+    // X' rows and means of the first kPre variables for the update, in
+    // flight during the finish (members beyond k read as zero).
+    const int npre = (prm.n_var < kPre) ? prm.n_var : kPre;
+    for (int e = tid; e < kPre * KP; e += kThreads) {
+      const int vv = e / KP, m = e - vv * KP;
+      if (vv < npre && m < k) cp_async4(&V.xpre[vv][m], Xp + (base + (int64_t)vv * prm.var_stride) * k + m);
+      else V.xpre[vv][m] = 0.0f;
+    }
+    if (tid < npre) cp_async8(&V.xmpre[tid], prm.xmean + base + (int64_t)tid * prm.var_stride);
+
     // ---------------- 4. finish ----------------
     // The iterate is Z = p(M) up to rounding errors that the coupled
     // iteration leaves as right factors, so the finish takes C = Z^T A Z:
@@ -904,17 +927,20 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
 
     // ---------------- 5. update ----------------
     const float c1 = cw * rsqrtf(delta);  // W's eigenvalue on the mean direction
+    cp_async_wait_all();
+    __syncthreads();  // the prefetched rows visible to every thread
     for (int v0 = 0; v0 < prm.n_var; v0 += kVarTile) {
       const int nv = (prm.n_var - v0 < kVarTile) ? prm.n_var - v0 : kVarTile;
       // X' rows of the variables -> T rows 0..15 (B operand, K = members);
       // one warp per variable: X' wa, the mean of X', sum of X'^2.
       for (int vv = warp; vv < kVarTile; vv += L::kWarps) {
-        const float* xr = (vv < nv) ? Xp + (base + (int64_t)(v0 + vv) * prm.var_stride) * k : nullptr;
+        const bool pre = v0 == 0 && vv < npre;
+        const float* xr = (vv < nv && !pre) ? Xp + (base + (int64_t)(v0 + vv) * prm.var_stride) * k : nullptr;
         float dw = 0.0f, sx = 0.0f, sq = 0.0f;
 #pragma unroll
         for (int gg = 0; gg < NG; ++gg) {
           const int m = lane + 32 * gg;
-          const float x0 = (xr && m < k) ? xr[m] : 0.0f;
+          const float x0 = pre ? V.xpre[vv][m] : ((xr && m < k) ? xr[m] : 0.0f);
           const uint32_t o0 = sw_off(vv, m, TR);
           float h, l;
           split(x0, h, l);
@@ -934,7 +960,7 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
           V.one[vv] = c1 * sx * ik;  // X' W on the mean direction (X' 1 is zero up to rounding)
           V.inc[vv] = dw;
           V.xsq[vv] = sq;
-          V.xm[vv] = (vv < nv) ? prm.xmean[base + (int64_t)(v0 + vv) * prm.var_stride] : 0.0;
+          V.xm[vv] = pre ? V.xmpre[vv] : ((vv < nv) ? prm.xmean[base + (int64_t)(v0 + vv) * prm.var_stride] : 0.0);
         }
       }
       operands_ready();
@@ -1005,6 +1031,7 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
       mbar_wait(&mma_bar, mma_ph);
     }
   }
+  cp_async_wait_all();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
