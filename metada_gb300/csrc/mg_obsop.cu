@@ -44,57 +44,100 @@ __global__ void hx_idw4_kernel(const double* __restrict__ X, int k, int64_t ld, 
 // Bilinear in (lon, lat), linear in level; the operation order matches the
 // oracle's restatement exactly.
 // TX: the members' storage type (FP64, or FP32 widened to FP64 on load).
+//
+// Each warp takes 32 obs.  Lane j first computes obs j's grid geometry
+// (fractional indices, weights, plane offsets: about 30 FP64 operations,
+// which GB300 runs at 1/64 of the FP32 rate) and leaves it in shared memory;
+// then the warp walks the 32 obs with its lanes over the members, so the
+// geometry is computed once per obs instead of once per (obs, member).
+struct LatLonGeom {
+  double ax, fx, ay, fy, az, fz;
+  int64_t lo, hi;  // offsets of the two level planes from the member's start
+  int64_t r0, r1;  // j0 nlon, (j0 + 1) nlon
+  int32_t i0, i1;
+  int32_t valid;
+};
+
 template <typename TX>
-__global__ void hx_latlon_kernel(const TX* __restrict__ X, int k, int64_t ld, int nlon,
-                                 int nlat, int nlev, const double* __restrict__ olat,
-                                 const double* __restrict__ olon, const double* __restrict__ olev,
-                                 const int32_t* __restrict__ ovar, int64_t p,
-                                 double* __restrict__ HX) {
-  const int64_t total = p * k;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
-    const int64_t o = e / k;
-    const int m = (int)(e - o * k);
-    const int64_t plane = (int64_t)nlat * nlon;
-    // Reads stay inside member m: the variable must fit within the member
-    // stride and the coordinates must be finite; otherwise the value is NaN.
-    if (!isfinite(olon[o]) || !isfinite(olat[o]) || !isfinite(olev[o]) || ovar[o] < 0 ||
-        ((int64_t)ovar[o] + 1) * nlev * plane > ld) {
-      HX[e] = __longlong_as_double(0x7ff8000000000000LL);
-      continue;
+__global__ void __launch_bounds__(256) hx_latlon_kernel(const TX* __restrict__ X, int k, int64_t ld, int nlon,
+                                                        int nlat, int nlev, const double* __restrict__ olat,
+                                                        const double* __restrict__ olon,
+                                                        const double* __restrict__ olev,
+                                                        const int32_t* __restrict__ ovar, int64_t p,
+                                                        double* __restrict__ HX) {
+  __shared__ LatLonGeom geo[8][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t plane = (int64_t)nlat * nlon;
+  const int64_t nwarps = (int64_t)gridDim.x * 8;
+  for (int64_t o0 = ((int64_t)blockIdx.x * 8 + w) * 32; o0 < p; o0 += nwarps * 32) {
+    {
+      const int64_t o = o0 + lane;
+      LatLonGeom g{};
+      // Reads stay inside member m: the variable must fit within the member
+      // stride and the coordinates must be finite; otherwise the value is NaN.
+      if (o < p && isfinite(olon[o]) && isfinite(olat[o]) && isfinite(olev[o]) && ovar[o] >= 0 &&
+          ((int64_t)ovar[o] + 1) * nlev * plane <= ld) {
+        // Fractional grid indices: lon_i = (i + 0.5) dlon, lat_j = -90 + (j + 0.5) dlat.
+        const double dlon = 360.0 / (double)nlon, dlat = 180.0 / (double)nlat;
+        const double gx = __dsub_rn(__ddiv_rn(olon[o], dlon), 0.5);
+        const double fxl = floor(gx);
+        const double fx = __dsub_rn(gx, fxl);
+        long long i0 = (long long)fxl % nlon;
+        if (i0 < 0) i0 += nlon;
+        const long long i1 = (i0 + 1) % nlon;
+        double gy = __dsub_rn(__ddiv_rn(__dadd_rn(olat[o], 90.0), dlat), 0.5);
+        gy = fmax(0.0, fmin((double)(nlat - 1), gy));
+        long long j0 = (long long)floor(gy);
+        if (j0 > nlat - 2) j0 = nlat - 2;
+        const double fy = __dsub_rn(gy, (double)j0);
+        const double gz = fmax(0.0, fmin((double)(nlev - 1), olev[o]));
+        long long l0 = (long long)floor(gz);
+        if (l0 > nlev - 2) l0 = nlev - 2;
+        if (l0 < 0) l0 = 0;
+        const double fz = (nlev > 1) ? __dsub_rn(gz, (double)l0) : 0.0;
+        const long long l1 = (nlev > 1) ? l0 + 1 : l0;
+        const int64_t vb = (int64_t)ovar[o] * nlev * plane;
+        g.ax = __dsub_rn(1.0, fx);
+        g.fx = fx;
+        g.ay = __dsub_rn(1.0, fy);
+        g.fy = fy;
+        g.az = __dsub_rn(1.0, fz);
+        g.fz = fz;
+        g.lo = vb + l0 * plane;
+        g.hi = vb + l1 * plane;
+        g.r0 = (int64_t)j0 * nlon;
+        g.r1 = (int64_t)(j0 + 1) * nlon;
+        g.i0 = (int32_t)i0;
+        g.i1 = (int32_t)i1;
+        g.valid = 1;
+      }
+      geo[w][lane] = g;
     }
-    // Fractional grid indices: lon_i = (i + 0.5) dlon, lat_j = -90 + (j + 0.5) dlat.
-    const double dlon = 360.0 / (double)nlon, dlat = 180.0 / (double)nlat;
-    const double gx = __dsub_rn(__ddiv_rn(olon[o], dlon), 0.5);
-    const double fxl = floor(gx);
-    const double fx = __dsub_rn(gx, fxl);
-    long long i0 = (long long)fxl % nlon;
-    if (i0 < 0) i0 += nlon;
-    const long long i1 = (i0 + 1) % nlon;
-    double gy = __dsub_rn(__ddiv_rn(__dadd_rn(olat[o], 90.0), dlat), 0.5);
-    gy = fmax(0.0, fmin((double)(nlat - 1), gy));
-    long long j0 = (long long)floor(gy);
-    if (j0 > nlat - 2) j0 = nlat - 2;
-    const double fy = __dsub_rn(gy, (double)j0);
-    const double gz = fmax(0.0, fmin((double)(nlev - 1), olev[o]));
-    long long l0 = (long long)floor(gz);
-    if (l0 > nlev - 2) l0 = nlev - 2;
-    if (l0 < 0) l0 = 0;
-    const double fz = (nlev > 1) ? __dsub_rn(gz, (double)l0) : 0.0;
-    const long long l1 = (nlev > 1) ? l0 + 1 : l0;
-    const TX* x = X + (int64_t)m * ld + (int64_t)ovar[o] * nlev * plane;
-    const TX* lo = x + l0 * plane;
-    const TX* hi = x + l1 * plane;
-    const double ax = __dsub_rn(1.0, fx), ay = __dsub_rn(1.0, fy), az = __dsub_rn(1.0, fz);
-    const double l00 = (double)lo[j0 * nlon + i0], l01 = (double)lo[j0 * nlon + i1];
-    const double l10 = (double)lo[(j0 + 1) * nlon + i0], l11 = (double)lo[(j0 + 1) * nlon + i1];
-    const double h00 = (double)hi[j0 * nlon + i0], h01 = (double)hi[j0 * nlon + i1];
-    const double h10 = (double)hi[(j0 + 1) * nlon + i0], h11 = (double)hi[(j0 + 1) * nlon + i1];
-    const double b0 = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(l00, ax), __dmul_rn(l01, fx)), ay),
-                                __dmul_rn(__dadd_rn(__dmul_rn(l10, ax), __dmul_rn(l11, fx)), fy));
-    const double b1 = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(h00, ax), __dmul_rn(h01, fx)), ay),
-                                __dmul_rn(__dadd_rn(__dmul_rn(h10, ax), __dmul_rn(h11, fx)), fy));
-    HX[e] = __dadd_rn(__dmul_rn(b0, az), __dmul_rn(b1, fz));
+    __syncwarp();
+    const int nob = (p - o0 < 32) ? (int)(p - o0) : 32;
+    for (int j = 0; j < nob; ++j) {
+      const LatLonGeom& g = geo[w][j];
+      const int64_t o = o0 + j;
+      for (int m = lane; m < k; m += 32) {
+        const int64_t e = o * k + m;
+        if (!g.valid) {
+          HX[e] = __longlong_as_double(0x7ff8000000000000LL);
+          continue;
+        }
+        const TX* lo = X + (int64_t)m * ld + g.lo;
+        const TX* hi = X + (int64_t)m * ld + g.hi;
+        const double l00 = (double)lo[g.r0 + g.i0], l01 = (double)lo[g.r0 + g.i1];
+        const double l10 = (double)lo[g.r1 + g.i0], l11 = (double)lo[g.r1 + g.i1];
+        const double h00 = (double)hi[g.r0 + g.i0], h01 = (double)hi[g.r0 + g.i1];
+        const double h10 = (double)hi[g.r1 + g.i0], h11 = (double)hi[g.r1 + g.i1];
+        const double b0 = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(l00, g.ax), __dmul_rn(l01, g.fx)), g.ay),
+                                    __dmul_rn(__dadd_rn(__dmul_rn(l10, g.ax), __dmul_rn(l11, g.fx)), g.fy));
+        const double b1 = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(h00, g.ax), __dmul_rn(h01, g.fx)), g.ay),
+                                    __dmul_rn(__dadd_rn(__dmul_rn(h10, g.ax), __dmul_rn(h11, g.fx)), g.fy));
+        HX[e] = __dadd_rn(__dmul_rn(b0, g.az), __dmul_rn(b1, g.fz));
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -170,7 +213,7 @@ int mg_hx_latlon(mg_context* ctx, const double* X, int32_t k, int64_t ld, int32_
                    nlat > 1 && nlev > 0 && p >= 0,
                "mg_hx_latlon: bad arguments");
   if (p == 0) return MG_OK;
-  hx_latlon_kernel<double><<<grid_for(p * k, 256), 256, 0, ctx->stream>>>(X, k, ld, nlon, nlat, nlev,
+  hx_latlon_kernel<double><<<grid_for((p + 31) / 32 * 32, 256), 256, 0, ctx->stream>>>(X, k, ld, nlon, nlat, nlev,
                                                                           obs_lat, obs_lon, obs_lev,
                                                                           obs_var, p, HX);
   MG_COUNT_LAUNCH();
@@ -186,7 +229,7 @@ int mg_hx_latlon_f32(mg_context* ctx, const float* X, int32_t k, int64_t ld, int
                    nlat > 1 && nlev > 0 && p >= 0,
                "mg_hx_latlon_f32: bad arguments");
   if (p == 0) return MG_OK;
-  hx_latlon_kernel<float><<<grid_for(p * k, 256), 256, 0, ctx->stream>>>(X, k, ld, nlon, nlat, nlev,
+  hx_latlon_kernel<float><<<grid_for((p + 31) / 32 * 32, 256), 256, 0, ctx->stream>>>(X, k, ld, nlon, nlat, nlev,
                                                                          obs_lat, obs_lon, obs_lev,
                                                                          obs_var, p, HX);
   MG_COUNT_LAUNCH();

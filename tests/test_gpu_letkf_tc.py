@@ -66,11 +66,12 @@ def test_tensor_path_matches_oracle_and_simt(dev, k):
     assert rel_err(got, simt) <= MIXED_TOL
 
 
+@pytest.mark.parametrize("k", [32, 80])
 @pytest.mark.parametrize("flags", [_lib.MG_RTPS, _lib.MG_INFL_COMPAT, _lib.MG_R_IDENTITY])
-def test_tensor_path_semantics_flags(dev, flags):
+def test_tensor_path_semantics_flags(dev, flags, k):
     """RTPS relaxation, the reference's inflation placement (Pa *= rho) and
-    R = I on the tensor-core path, against the oracle."""
-    c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=4, nvar=3, k=32, p=15_000, T=20, case=42,
+    R = I on the tensor-core path (both layouts), against the oracle."""
+    c = syn.latlon_letkf_case(nlon=72, nlat=36, nlev=4, nvar=3, k=k, p=15_000, T=20, case=42,
                               rho=0.8 if flags == _lib.MG_RTPS else 1.05)
     got, HX, off, idx, dist, st = _run(dev, c, flags)
     assert st.tensor_path == 1
@@ -78,9 +79,11 @@ def test_tensor_path_semantics_flags(dev, flags):
     assert rel_err(_gather(got, c, base), want) <= MIXED_TOL
 
 
-def test_tensor_path_many_variables_per_point(dev):
-    """More variables per analysis point than one update tile (16) holds."""
-    c = syn.latlon_letkf_case(nlon=48, nlat=24, nlev=2, nvar=37, k=24, p=6_000, T=12, case=43)
+@pytest.mark.parametrize("k", [24, 72])
+def test_tensor_path_many_variables_per_point(dev, k):
+    """More variables per analysis point than one update tile (16) holds,
+    and more than the four whose update rows are prefetched."""
+    c = syn.latlon_letkf_case(nlon=48, nlat=24, nlev=2, nvar=37, k=k, p=6_000, T=12, case=43)
     got, HX, off, idx, dist, st = _run(dev, c)
     assert st.tensor_path == 1
     cols = np.random.default_rng(0).choice(c.nlat * c.nlon, 200, replace=False)
