@@ -27,7 +27,7 @@ struct LetkfParams {
   const double* loc_dist;  // or null
   double hsupport, vsupport, rho;
   int flags;
-  const int32_t* order;  // columns, longest list first
+  const int32_t* order;  // columns in work order (the grid's order)
   unsigned long long* next;
   unsigned long long* n_empty;
   unsigned long long* total_local;
@@ -44,7 +44,7 @@ struct LetkfParams {
   unsigned long long* n_redo;
   unsigned* max_resid_bits;
   // SIMT path: when set, item i is the point redo_in[i] (col * nlev + lev)
-  // instead of the longest-first order.
+  // instead of the column work order.
   const int32_t* redo_in;
   // Tensor-core path: when set, each column's candidates sorted by obs level
   // bucket (stable; bucket = floor(obs level) clamped to the grid's levels):

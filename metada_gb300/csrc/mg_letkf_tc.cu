@@ -17,8 +17,8 @@
 //    operands; Z, Y and T are separate 96-row operands and [Z; Y] T is two
 //    products.
 //
-// Per local analysis (one CTA, persistent, points pulled longest list first
-// from a work counter):
+// Per local analysis (one CTA, persistent, points pulled in the grid's
+// column order from a work counter):
 //  1. Gram: the candidate list is filtered and weighted, the kept rows
 //     sqrt(w) Y'_o are gathered 64 at a time into a K-major, 128-byte
 //     swizzled operand (members x obs) with sqrt(w) d_o as an extra row, and
