@@ -123,6 +123,7 @@ struct Lay {
   // kTmB for KP = 96), the Gram at kTmGram.
   static constexpr uint32_t kTmemCols = kStack ? 256u : 512u;
   static constexpr uint32_t kTmB = 128;
+  static constexpr uint32_t kTmE = KP;  // E = Z^T X'^T (16 columns) beside the products
   static constexpr uint32_t kTmGram = kStack ? 128u : 256u;
   static_assert(kGramSlab % 1024 == 0 && kSlabZ % 1024 == 0 && kSlabT % 1024 == 0,
                 "swizzle atoms are 1024-byte aligned");
@@ -553,6 +554,20 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
       }
     }
 
+    // X' rows and means of the first kPre variables, in flight during the
+    // Newton-Schulz iteration (members beyond k read as zero).
+    const int npre = (prm.n_var < kPre) ? prm.n_var : kPre;
+    for (int e = tid; e < kPre * KP; e += kThreads) {
+      const int vv = e / KP, m = e - vv * KP;
+      if (vv < npre && m < k) cp_async4(&V.xpre[vv][m], Xp + (base + (int64_t)vv * prm.var_stride) * k + m);
+      else V.xpre[vv][m] = 0.0f;
+    }
+    if (tid < npre) cp_async8(&V.xmpre[tid], prm.xmean + base + (int64_t)tid * prm.var_stride);
+    // Points with at most kPre variables take the short finish: E = Z^T X'^T
+    // is computed beside Q, and X' W = cw (E - F^T E / 2), so W itself is
+    // never formed (one dependent product and two epilogues fewer).
+    const bool fast = prm.n_var <= kPre;
+
     // ---------------- 3. coupled Newton-Schulz ----------------
     int its = 0;
     bool stop = false;  // decided from max |Z Y - I| of the current iterate
@@ -674,25 +689,28 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
       continue;
     }
 
-    // X' rows and means of the first kPre variables for the update, in
-    // flight during the finish (members beyond k read as zero).
-    const int npre = (prm.n_var < kPre) ? prm.n_var : kPre;
-    for (int e = tid; e < kPre * KP; e += kThreads) {
-      const int vv = e / KP, m = e - vv * KP;
-      if (vv < npre && m < k) cp_async4(&V.xpre[vv][m], Xp + (base + (int64_t)vv * prm.var_stride) * k + m);
-      else V.xpre[vv][m] = 0.0f;
-    }
-    if (tid < npre) cp_async8(&V.xmpre[tid], prm.xmean + base + (int64_t)tid * prm.var_stride);
-
     // ---------------- 4. finish ----------------
     // The iterate is Z = p(M) up to rounding errors that the coupled
     // iteration leaves as right factors, so the finish takes C = Z^T A Z:
     // Q = (P A P) Z (A operand: Y's rows = P A P; B operand: Z^T rows), then
     // C = Z^T Q; A^-1 = Z C^-1 Z^T, A^-1/2 ~ Z C^-1/2.
+    if (fast) {  // X' rows -> T rows 0..15 (B operand of E; T is free here)
+      cp_async_wait_all();
+      __syncthreads();
+      for (int e = tid; e < kVarTile * KP; e += kThreads) {
+        const int vv = e / KP, m = e - vv * KP;
+        const uint32_t off = sw_off(vv, m, TR);
+        float h, l;
+        split((vv < npre) ? V.xpre[vv][m] : 0.0f, h, l);
+        *reinterpret_cast<float*>(TH + off) = h;
+        *reinterpret_cast<float*>(TL + off) = l;
+      }
+    }
     operands_ready();
     if (warp == 0) {
       tc_fence_after();
       issue3(tmem, sYH, sYL, L::kSlabZ, sZH, sZL, L::kSlabZ, NG, idescK, false);
+      if (fast) issue3(tmem + L::kTmE, sZH, sZL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescU, false);
       mma_commit_elect(&mma_bar);
     }
     if (tid < KP) {  // u = Z^T b (row tid of Z^T)
@@ -732,7 +750,9 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
     mma_ph ^= 1u;
     // F = C - P (residual, partial F u) -> T transposed (B operand of Z F);
     // Z rows, read from the columns of Z^T, -> Y's operand row-major (A
-    // operand of Z F; P A P there is not read any more).
+    // operand of Z F; P A P there is not read any more).  Short finish:
+    // F^T -> Y's operand (A operand of F^T E) and E -> T rows 0..15 (its B
+    // operand).
     if (rowwarp) {
       float fu = 0.0f, fm = 0.0f;
 #pragma unroll 1
@@ -750,9 +770,25 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
           fm = nan_max(fm, fabsf(x));
           fu += x * V.u[c];
         }
-        put_col8(TH, TL, row, c0, TR, f);
-        get_col8(ZH, ZL, row, c0, ZR, f);
-        put_row8(YH, YL, row, c0, ZR, f);
+        if (fast) {
+          put_col8(YH, YL, row, c0, ZR, f);
+        } else {
+          put_col8(TH, TL, row, c0, TR, f);
+          get_col8(ZH, ZL, row, c0, ZR, f);
+          put_row8(YH, YL, row, c0, ZR, f);
+        }
+      }
+      if (fast && g == 0) {
+        uint32_t v[8];
+#pragma unroll 1
+        for (int c0 = 0; c0 < kVarTile; c0 += 8) {
+          tmem_ld8(tmem + tm_row + L::kTmE + c0, v);
+          tmem_wait_ld();
+          float e8[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) e8[j] = __uint_as_float(v[j]);
+          put_col8(TH, TL, row, c0, TR, e8);
+        }
       }
       V.part[g][row] = fu;
 #pragma unroll
@@ -760,11 +796,12 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
       // NaN or Inf residuals map to the maximum (positive floats order as integers)
       if (lane == 0) atomicMax(&s_flag[1], (fm == fm && fm < 3.0e38f) ? __float_as_uint(fm) : 0x7f800000u);
     }
-    // W = cw Z (I - F/2): D = Z F
+    // W = cw Z (I - F/2): D = Z F (short finish: D = F^T E, 16 columns)
     operands_ready();
     if (warp == 0) {
       tc_fence_after();
-      issue3(tmem, sYH, sYL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescK, false);
+      if (fast) issue3(tmem, sYH, sYL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescU, false);
+      else issue3(tmem, sYH, sYL, L::kSlabZ, sTH, sTL, L::kSlabT, NG, idescK, false);
       mma_commit_elect(&mma_bar);
     }
     const float resid = __uint_as_float(s_flag[1]);
@@ -775,12 +812,13 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
       V.v[tid] = (tid < k) ? V.u[tid] - fu : 0.0f;
     }
     __syncthreads();
-    if (tid < KP) {  // wa = c Z v (row tid of Z, in Y's operand)
+    if (tid < KP) {  // wa = c Z v (row tid of Z: in Y's operand, or column tid of Z^T)
       float acc = 0.0f;
 #pragma unroll 1
       for (int c0 = 0; c0 < KP; c0 += 8) {
         float z[8];
-        get_row8(YH, YL, tid, c0, ZR, z);
+        if (fast) get_col8(ZH, ZL, tid, c0, ZR, z);
+        else get_row8(YH, YL, tid, c0, ZR, z);
 #pragma unroll
         for (int j = 0; j < 8; ++j) acc += z[j] * V.v[c0 + j];
       }
@@ -793,7 +831,7 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
       hand_back();
       continue;
     }
-    if (rowwarp) {  // W rows -> U^T = W^T into Z's operand (A operand of the update)
+    if (!fast && rowwarp) {  // W rows -> U^T = W^T into Z's operand (A operand of the update)
 #pragma unroll 1
       for (int c0 = cb; c0 < cb + 32; c0 += 8) {
         uint32_t v[8];
@@ -811,7 +849,78 @@ __global__ void __launch_bounds__(Lay<KP>::kThreads, Lay<KP>::kMinBlocks) letkf_
     const float c1 = cw * rsqrtf(delta);  // W's eigenvalue on the mean direction
     cp_async_wait_all();
     __syncthreads();  // the prefetched rows visible to every thread
-    for (int v0 = 0; v0 < prm.n_var; v0 += kVarTile) {
+    if (fast) {
+      // X' W = cw (E - D / 2), D = F^T E, from TMEM; X' wa, the mean of X'
+      // and sum of X'^2 from the prefetched rows (one warp per variable).
+      const int nv = prm.n_var;
+      for (int vv = warp; vv < nv; vv += L::kWarps) {
+        float dw = 0.0f, sx = 0.0f, sq = 0.0f;
+#pragma unroll
+        for (int gg = 0; gg < NG; ++gg) {
+          const int m = lane + 32 * gg;
+          const float x0 = V.xpre[vv][m];
+          dw += x0 * V.wa[m];
+          sx += x0;
+          sq += x0 * x0;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          dw += __shfl_xor_sync(0xffffffffu, dw, off);
+          sx += __shfl_xor_sync(0xffffffffu, sx, off);
+          sq += __shfl_xor_sync(0xffffffffu, sq, off);
+        }
+        if (lane == 0) {
+          V.one[vv] = c1 * sx * ik;
+          V.inc[vv] = dw;
+          V.xsq[vv] = sq;
+          V.xm[vv] = V.xmpre[vv];
+        }
+      }
+      __syncthreads();
+      float dv[kPre];
+      if (rowwarp && g == 0) {
+        uint32_t dd[8], ee[8];
+        tmem_ld8(tmem + tm_row, dd);
+        tmem_ld8(tmem + tm_row + L::kTmE, ee);
+        tmem_wait_ld();
+#pragma unroll
+        for (int vv = 0; vv < kPre; ++vv)
+          dv[vv] = cw * (__uint_as_float(ee[vv]) - 0.5f * __uint_as_float(dd[vv])) + V.one[vv];
+        if (rtps) {
+#pragma unroll
+          for (int vv = 0; vv < kPre; ++vv) {
+            float s2 = (row < k && vv < nv) ? dv[vv] * dv[vv] : 0.0f;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, off);
+            if (lane == 0) V.ssa[q][vv] = s2;
+          }
+        }
+      }
+      if (rtps) {
+        __syncthreads();
+        if (tid < nv) {
+          float s2 = 0.0f;
+#pragma unroll
+          for (int qq = 0; qq < NG; ++qq) s2 += V.ssa[qq][tid];
+          const float sb = sqrtf(V.xsq[tid] / (float)(k - 1));
+          const float sa = sqrtf(s2 / (float)(k - 1));
+          V.fac[tid] = (sa > 0.0f) ? (float)prm.rho * (sb - sa) / sa : 0.0f;  // factor - 1
+        }
+        __syncthreads();
+      }
+      if (rowwarp && g == 0 && row < k) {
+#pragma unroll
+        for (int vv = 0; vv < kPre; ++vv) {
+          if (vv < nv) {
+            const float a2 = rtps ? dv[vv] * (1.0f + V.fac[vv]) : dv[vv];
+            mg::letkf_store(prm, (base + (int64_t)vv * prm.var_stride) * k + row,
+                            (V.xm[vv] + (double)V.inc[vv]) + (double)a2);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    for (int v0 = 0; !fast && v0 < prm.n_var; v0 += kVarTile) {
       const int nv = (prm.n_var - v0 < kVarTile) ? prm.n_var - v0 : kVarTile;
       // X' rows of the variables -> T rows 0..15 (B operand, K = members);
       // one warp per variable: X' wa, the mean of X', sum of X'^2.
