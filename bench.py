@@ -185,7 +185,7 @@ class ClockSampler:
 # workload by its analyses (x4): every stream of the kernel (perturbations
 # read, analysis written, lists, obs rows) grows with the analysis count.
 # A constant of the build, not a measurement of this run.
-TC_TRAFFIC_REDUCED_BYTES = 6.331e8
+TC_TRAFFIC_REDUCED_BYTES = 5.311e8
 TC_TRAFFIC_REDUCED_ANALYSES = 162_000
 
 
