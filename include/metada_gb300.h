@@ -219,7 +219,7 @@ typedef struct mg_letkf_desc {
  * local analysis per (column, level), all sharing the background obs-space
  * prior.  With MG_COMPAT flags each analysis follows updateGridPoint's
  * arithmetic; without them, the Hunt et al. (2007) LETKF with Gaspari-Cohn
- * R-localisation.  Points are scheduled longest-list first. */
+ * R-localisation.  Points are scheduled in the grid's column order. */
 int mg_letkf_batched(mg_context* ctx, const mg_letkf_desc* desc);
 
 /* One case of an uneven batch of global ETKF analyses (see mg_etkf_batch_*). */
