@@ -44,7 +44,9 @@
 //     values are not finite are listed and re-run by the SIMT Jacobi kernel.
 //  5. Update: D = W^T X'^T (members x variables) on the tensor core, then
 //     x_a = x_mean + X' wa + D (+ RTPS relaxation), written in FP64 (or FP32
-//     storage).
+//     storage).  Points with at most kPre variables take the short finish:
+//     E = Z^T X'^T is issued beside the finish's first product and
+//     W^T X'^T = cw (E - F^T E / 2), so W is never formed.
 // Every mbarrier wait is bounded in time; a wait that gives up makes the CTA
 // set the status word, drain its own MMAs (bounded) and free its TMEM.
 #include <cuda_runtime.h>
