@@ -1123,27 +1123,40 @@ def main():
     if rank == 0 and world == 1 and not args.no_extras:
         del w
         torch.cuda.empty_cache()
-        u = uneven_results(warmup=1, steps=3)
-        extras["uneven_batch"] = {
-            "workload": u["config"]["workload"], "metric": "analyses/s (512 cases, one captured graph)",
-            "mixed": u["mixed"], "fp64": {kk: u["fp64"][kk] for kk in ("analyses_per_s", "ms_per_batch")},
-            "max_rel_err_mixed_vs_fp64": u["max_rel_err_mixed_vs_fp64"], "steps": 3, "warmup": 1}
-        torch.cuda.empty_cache()
-        extras["global_etkf_small"] = global_etkf_results(warmup=3, steps=20)
-        col = column_results(args.extra_train_steps, 4096)
-        extras["column_operator"] = {
-            "workload": col["config"]["workload"],
-            "surrogate_training": f"{args.extra_train_steps} Adam steps of 4096 columns in this run "
-                                  f"(--workload column trains 6000)",
-            "hx": col["hx"], "heldout_rel_rms_err": col["training"]["heldout_rel_rms_err"],
-            "letkf_gain_kept_by_surrogate": col["letkf"]["gain_kept_by_surrogate"]}
-        torch.cuda.empty_cache()
-        hr = highres_results()
-        extras["highres_letkf"] = {kk: hr[kk] for kk in ("metric", "value", "unit", "ms_per_step", "dtype", "config",
-                                                         "ms", "analyses", "tensor_path", "handed_back_to_simt",
-                                                         "local_obs", "device_memory_gb", "oracle_check")}
-        del hr
-        torch.cuda.empty_cache()
+
+        def extra(name, fn):
+            # One configuration's summary; a failure is recorded in its key
+            # and does not cost the headline line.
+            try:
+                extras[name] = fn()
+            except Exception as exc:  # noqa: BLE001
+                extras[name] = {"error": f"{type(exc).__name__}: {exc}"}
+            torch.cuda.empty_cache()
+
+        def uneven():
+            u = uneven_results(warmup=1, steps=3)
+            return {"workload": u["config"]["workload"], "metric": "analyses/s (512 cases, one captured graph)",
+                    "mixed": u["mixed"], "fp64": {kk: u["fp64"][kk] for kk in ("analyses_per_s", "ms_per_batch")},
+                    "max_rel_err_mixed_vs_fp64": u["max_rel_err_mixed_vs_fp64"], "steps": 3, "warmup": 1}
+
+        def column():
+            col = column_results(args.extra_train_steps, 4096)
+            return {"workload": col["config"]["workload"],
+                    "surrogate_training": f"{args.extra_train_steps} Adam steps of 4096 columns in this run "
+                                          f"(--workload column trains 6000)",
+                    "hx": col["hx"], "heldout_rel_rms_err": col["training"]["heldout_rel_rms_err"],
+                    "letkf_gain_kept_by_surrogate": col["letkf"]["gain_kept_by_surrogate"]}
+
+        def highres():
+            hr = highres_results()
+            return {kk: hr[kk] for kk in ("metric", "value", "unit", "ms_per_step", "dtype", "config", "ms",
+                                         "analyses", "tensor_path", "handed_back_to_simt", "local_obs",
+                                         "device_memory_gb", "oracle_check")}
+
+        extra("uneven_batch", uneven)
+        extra("global_etkf_small", lambda: global_etkf_results(warmup=3, steps=20))
+        extra("column_operator", column)
+        extra("highres_letkf", highres)
 
     if rank == 0:
         line = {
